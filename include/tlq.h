@@ -1,0 +1,176 @@
+/*
+ * tlq.h -- C ABI of the GB300 hydrodynamic step (libtlq.so).
+ *
+ * Drop-in for the hot path of tlaloque, the loop body of
+ * source/mainHD.f90:74-99 and the external subroutines it calls.  All entry
+ * points are extern "C", take plain pointers and sizes, return an int status
+ * (TLQ_OK = 0) and never abort or exit.  Host arrays are borrowed for the
+ * duration of one call and use the reference's layout
+ *     A(1:5, -1:nx+2, -1:ny+2, -1:nz+2)   (real(8), variable fastest,
+ *                                          column-major; nghost = 2)
+ * The device state is owned by the context.  A context is not thread-safe;
+ * it owns (or borrows) one CUDA stream and every call is ordered on it.
+ */
+#ifndef TLQ_H
+#define TLQ_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TLQ_ABI_VERSION 1
+
+/* Status codes.  The reference has no error convention beyond `stop`. */
+enum {
+  TLQ_OK = 0,
+  TLQ_ERR_CUDA = 1,          /* a CUDA runtime/driver call failed (see tlq_last_error) */
+  TLQ_ERR_CONFIG = 2,        /* invalid or unsupported configuration */
+  TLQ_ERR_NONFINITE_DT = 3,  /* the CFL reduction saw a NaN/Inf signal speed */
+  TLQ_ERR_NEG_DENSITY = 4,   /* an interior cell has rho <= 0 after the step */
+  TLQ_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+  TLQ_ERR_ARG = 6,           /* NULL or out-of-range argument */
+  TLQ_ERR_STATE = 7,         /* call out of order (e.g. tlq_step before tlq_upload) */
+  TLQ_ERR_NOMEM = 8          /* device or pinned-host allocation failed */
+};
+
+/* Boundary kinds: source/constants.f90:20-23 (same values). */
+enum { TLQ_BC_OUTFLOW = 1, TLQ_BC_REFLECTIVE = 2, TLQ_BC_PERIODIC = 3, TLQ_BC_INFLOW = 4 };
+/* Slope limiters: source/constants.f90:26-31 (same values). */
+enum {
+  TLQ_LIMITER_NONE = 1, TLQ_LIMITER_VANLEER = 2, TLQ_LIMITER_MINMOD = 3,
+  TLQ_LIMITER_UMIST = 4, TLQ_LIMITER_WOODWARD = 5, TLQ_LIMITER_SUPERBEE = 6
+};
+/* Riemann solver: source/HLLC.f90 (linked by the reference Makefile) or source/HLL.f90. */
+enum { TLQ_SOLVER_HLLC = 0, TLQ_SOLVER_HLL = 1 };
+/* Radiative cooling: off; the reference's single exponential step
+ * (source/cooling.f90:47-119); its sub-cycled extension (nsub = 1 is the
+ * reference formula exactly). */
+enum { TLQ_COOL_NONE = 0, TLQ_COOL_REF = 1, TLQ_COOL_SUBCYCLE = 2 };
+/* Arithmetic of the fused step: plain FP64 (matches the reference), or
+ * mixed (FP32 reconstruction and Riemann fluxes, FP64 accumulation). */
+enum { TLQ_PREC_FP64 = 0, TLQ_PREC_MIXED = 1 };
+
+/* Runtime image of user/parameters.f90 (compile-time parameters there). */
+typedef struct tlq_config {
+  int nx, ny, nz;                 /* interior cells, parameters.f90:23-25 (each >= 2) */
+  double xl, xr, yl, yr, zl, zr;  /* domain, parameters.f90:37-42 */
+  double gamma;                   /* parameters.f90:43 */
+  double cfl;                     /* parameters.f90:46 */
+  double eta;                     /* artificial viscosity, parameters.f90:47 */
+  double mu0;                     /* mean particle mass for calcTemp, parameters.f90:44 */
+  double cooling_limit;           /* parameters.f90:49 */
+  int limiter;                    /* TLQ_LIMITER_*, parameters.f90:18 */
+  int solver;                     /* TLQ_SOLVER_* */
+  int bc[6];                      /* x-, x+, y-, y+, z-, z+ = LB, RB, DB, TB, FB, BB (parameters.f90:10-15) */
+  int cooling;                    /* TLQ_COOL_* (the reference's -DCOOL) */
+  int cool_max_sub;               /* TLQ_COOL_SUBCYCLE: max sub-steps per step */
+  double cool_sub_frac;           /* TLQ_COOL_SUBCYCLE: max Lambda n^2 h / E_th per sub-step */
+  int precision;                  /* TLQ_PREC_* */
+  int device;                     /* CUDA device ordinal */
+} tlq_config;
+
+/* spherical_wind_type, source/winds.f90:5-16 (same fields, same order). */
+typedef struct tlq_wind {
+  double xc, yc, zc;  /* source centre [code units of x] */
+  double vx, vy, vz;  /* source velocity added to the radial wind */
+  double radius;      /* cells with dist < radius are overwritten */
+  double mdot;        /* mass-loss rate */
+  double vinf;        /* terminal speed */
+  double temp;        /* wind temperature [K] */
+  double mu;          /* wind mean particle mass [AMU] */
+} tlq_wind;
+
+typedef struct tlq_stats {
+  long long steps;      /* tlq_step/tlq_advance iterations since tlq_upload */
+  double t, dt;         /* simulated time and the dt of the last step */
+  int status;           /* sticky device status (TLQ_OK or the first error seen) */
+  int graph;            /* 1 if steps are replayed from a captured CUDA graph */
+  double ms_stage1;     /* average device time of the last timed stage-1 launches */
+  double ms_stage2;     /* average device time of the last timed stage-2 launches */
+  long long timed;      /* number of timed steps behind the averages */
+  double bytes_state;   /* device bytes held for the mesh state */
+} tlq_stats;
+
+typedef struct tlq_ctx tlq_ctx;
+
+/* Defaults = user/parameters.f90 (50^3 on [-1,1]^3, gamma 5/3, cfl 0.4,
+ * eta 0.005, van Leer, reflective, no cooling) with the HLLC solver. */
+void tlq_config_default(tlq_config* cfg);
+
+/* Context life cycle: initmain's allocation (source/init.f90:82-88). */
+int tlq_create(const tlq_config* cfg, tlq_ctx** out);
+int tlq_destroy(tlq_ctx* ctx);
+/* Order the context's work on a caller-owned cudaStream_t (NULL: own stream). */
+int tlq_set_stream(tlq_ctx* ctx, void* cuda_stream);
+
+/* Cooling table, loaddata (source/cooling.f90:21-45): n rows of (T [K],
+ * log10 Lambda), i.e. the file's second column negated.  Copied. */
+int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* log10_lambda, int n);
+/* Spherical winds applied in borders (user/user.f90:57-70).  Copied. */
+int tlq_set_winds(tlq_ctx* ctx, const tlq_wind* winds, int n);
+/* Point masses (x, y, z, M per mass) of pgravity (source/pointsource_gravity.f90:12-39);
+ * the reference hard-codes M = 8 Msun (:23).  Copied; enables the source term. */
+int tlq_set_point_masses(tlq_ctx* ctx, const double* xyzm, int n);
+
+/* State transfer.  tlq_upload takes U after borders(U,1) (mainHD.f90:38) and
+ * computes calc_prims + the first CFL dt on the device.  tlq_download writes
+ * U and/or UPrim (either may be NULL) for output (HydroCore.f90:253).
+ * Download is exact on the interior and the first ghost layer of each face;
+ * the second ghost layer and edge/corner ghosts are never read by the step
+ * and are returned as stored (unspecified). */
+int tlq_upload(tlq_ctx* ctx, const double* U);
+int tlq_download(tlq_ctx* ctx, double* U, double* UPrim);
+int tlq_set_time(tlq_ctx* ctx, double t, int it);
+int tlq_get_time(tlq_ctx* ctx, double* t, int* it, double* dt);
+
+/* One iteration of mainHD.f90:74-99 (time_step, two HLL[C] stages, borders,
+ * step, calc_prims, cooling).  Returns t, it and the dt used (any may be
+ * NULL); waits for the step to finish.  tlq_advance runs n iterations with no
+ * host round trip (replayed from a CUDA graph after the first call).
+ * tlq_run_until runs while t < tfin (at most max_steps iterations). */
+int tlq_step(tlq_ctx* ctx, double* t, int* it, double* dt);
+int tlq_advance(tlq_ctx* ctx, int nsteps);
+int tlq_run_until(tlq_ctx* ctx, double tfin, int max_steps, double* t, int* it, double* dt);
+int tlq_synchronize(tlq_ctx* ctx);
+
+/* Diagnostics. */
+int tlq_stats_get(tlq_ctx* ctx, tlq_stats* out);
+int tlq_enable_timing(tlq_ctx* ctx, int on);
+const char* tlq_last_error(tlq_ctx* ctx);
+const char* tlq_status_string(int status);
+/* Global sums over the interior: mass, x/y/z momentum, total energy. */
+int tlq_conserved_sums(tlq_ctx* ctx, double out[5]);
+
+/* ---- Per-routine entry points (unit parity; host arrays in the reference
+ * layout; each replaces the external subroutine cited). ------------------- */
+/* calc_prims, source/HydroCore.f90:1-33 (all cells incl. ghosts). */
+int tlq_calc_prims(tlq_ctx* ctx, double* UPrim, const double* U);
+/* time_step, source/HydroCore.f90:113-155. */
+int tlq_time_step(tlq_ctx* ctx, const double* UPrim, double* dt);
+/* HLLCFluxes / HLLFluxes (choice 1 or 2), source/HLLC.f90:64-496 and
+ * source/HLL.f90:71-297: F, G, H on faces i, j, k in 0..n; other entries of
+ * F, G, H are left as passed. */
+int tlq_fluxes(tlq_ctx* ctx, const double* U, double* F, double* G, double* H,
+               const double* UPrim, int choice);
+/* Godunov, source/HLLC.f90:1-62; with point masses set and UPrim given, adds
+ * dt * S_Solver(UPrim, phi) (source/sources.f90:872-897, HLLC.f90:39-41). */
+int tlq_godunov(tlq_ctx* ctx, double* UPPP, const double* UU, const double* F, const double* G,
+                const double* H, const double* UPrim, double dt);
+/* borders, source/boundaries.f90:1-26 (order 1 or 2; non-MPI branches) with
+ * user_boundaries' spherical winds, in place. */
+int tlq_borders(tlq_ctx* ctx, double* U, int order);
+/* step, source/HydroCore.f90:170-211: U = UP + eta*Lap(U_old) on the
+ * interior, ghost layers of U from UP, t += dt, it += 1. */
+int tlq_viscous_step(tlq_ctx* ctx, double* U, const double* UP, double* t, int* it, double dt);
+/* apply_cooling, source/cooling.f90:47-119 (or the sub-cycled form). */
+int tlq_cooling(tlq_ctx* ctx, double* UPrim, double* U, double dt);
+/* pointmass_potential, source/pointsource_gravity.f90:12-39:
+ * phi(0:nx+1, 0:ny+1, 0:nz+1) -= sum_s G M_s / r. */
+int tlq_point_potential(tlq_ctx* ctx, double* phi);
+/* S_Solver, source/sources.f90:872-897. */
+int tlq_gravity_source(tlq_ctx* ctx, const double* UPrim, const double* phi, double* S);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TLQ_H */

@@ -1,0 +1,104 @@
+/*
+ * tlq_oracle.h -- CPU restatement of tlaloque's hydrodynamic time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle that the CUDA path is checked
+ * against.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg may load it; the product library (libtlq) never links or calls it.
+ *
+ * Every routine restates one Fortran routine of tlaloque (cited file:line,
+ * paths relative to the tlaloque source tree) in plain scalar C, FP64, with
+ * the same loop ranges, the same branch order, the same evaluation order of
+ * every expression (Fortran left-to-right association) and no FMA
+ * contraction (built with -ffp-contract=off).  Loop nests are ordered with x
+ * innermost (cache friendly) instead of the reference's k-innermost order;
+ * every cell/face is computed independently, so the results are identical.
+ *
+ * Array layout is the reference's: A(1:5, -1:nx+2, -1:ny+2, -1:nz+2),
+ * variable fastest, column-major (nghost = 2, user/parameters.f90:35).
+ */
+#ifndef TLQ_ORACLE_H
+#define TLQ_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Boundary kinds, source/constants.f90:20-23. */
+enum { TLQO_BC_OUTFLOW = 1, TLQO_BC_REFLECTIVE = 2, TLQO_BC_PERIODIC = 3, TLQO_BC_INFLOW = 4 };
+/* Slope limiters, source/constants.f90:26-31. */
+enum { TLQO_LIM_NONE = 1, TLQO_LIM_VANLEER = 2, TLQO_LIM_MINMOD = 3, TLQO_LIM_UMIST = 4,
+       TLQO_LIM_WOODWARD = 5, TLQO_LIM_SUPERBEE = 6 };
+/* Riemann solvers: source/HLLC.f90 (linked by the Makefile) and source/HLL.f90. */
+enum { TLQO_SOLVER_HLLC = 0, TLQO_SOLVER_HLL = 1 };
+/* Cooling modes: none; the reference's single exponential step
+ * (source/cooling.f90:47-119); the sub-cycled integrator built on it. */
+enum { TLQO_COOL_NONE = 0, TLQO_COOL_REF = 1, TLQO_COOL_SUBCYCLE = 2 };
+
+/* spherical_wind_type, source/winds.f90:5-16 (same field order). */
+typedef struct tlqo_wind {
+  double xc, yc, zc, vx, vy, vz, radius, mdot, vinf, temp, mu;
+} tlqo_wind;
+
+/* Runtime image of user/parameters.f90 plus the per-run tables. */
+typedef struct tlqo_params {
+  int nx, ny, nz;                       /* nxtot.. (parameters.f90:23-25), no MPI split */
+  double xl, xr, yl, yr, zl, zr;        /* parameters.f90:37-42 */
+  double gamma, cfl, eta, mu0;          /* parameters.f90:43-47 */
+  double cooling_limit;                 /* parameters.f90:49 */
+  int limiter;                          /* parameters.f90:18 */
+  int solver;                           /* TLQO_SOLVER_* */
+  int bc[6];                            /* LB, RB, DB, TB, FB, BB = x-, x+, y-, y+, z-, z+ */
+  int cooling;                          /* TLQO_COOL_* */
+  int ncool;                            /* nptsT (cooling.f90:32) */
+  const double* coolT;                  /* cooltable(1,:) : T [K] */
+  const double* coolC;                  /* cooltable(2,:) : log10 Lambda (= -b of the file) */
+  int cool_max_sub;                     /* sub-cycled integrator: max sub-steps */
+  double cool_sub_frac;                 /* sub-cycled integrator: max ce*h per sub-step */
+  int nwinds;
+  const tlqo_wind* winds;
+  int nmasses;                          /* point masses, source/pointsource_gravity.f90 */
+  const double* masses;                 /* 4 per mass: x, y, z, M [g] */
+  int nthreads;                         /* OpenMP threads (<=0: runtime default) */
+} tlqo_params;
+
+/* Size in doubles of one conserved/primitive array (5 vars incl. ghosts). */
+long tlqo_array_len(const tlqo_params* p);
+/* Size in doubles of the potential array phi(0:nx+1, 0:ny+1, 0:nz+1). */
+long tlqo_phi_len(const tlqo_params* p);
+
+/* Per-routine restatements (host arrays in the reference layout). */
+void tlqo_calc_prims(const tlqo_params* p, double* UPrim, const double* U);
+double tlqo_time_step(const tlqo_params* p, const double* UPrim);
+void tlqo_fluxes(const tlqo_params* p, const double* U, double* F, double* G, double* H,
+                 const double* UPrim, int choice);
+void tlqo_godunov(const tlqo_params* p, double* UPPP, const double* UU, const double* F,
+                  const double* G, const double* H, double dt, const double* S);
+void tlqo_borders(const tlqo_params* p, double* U, int order);
+void tlqo_impose_winds(const tlqo_params* p, double* U);
+void tlqo_step(const tlqo_params* p, double* U, const double* UP, double* UPP,
+               double* t, int* it, double dt);
+void tlqo_cooling(const tlqo_params* p, double* UPrim, double* U, double dt);
+void tlqo_point_potential(const tlqo_params* p, double* phi);
+void tlqo_gravity_source(const tlqo_params* p, const double* UPrim, const double* phi, double* S);
+double tlqo_cool_coef(const tlqo_params* p, double temp);
+
+/* Whole-run state of the main loop, source/mainHD.f90:22-100. */
+typedef struct tlqo_state {
+  double *U, *UP, *UPP, *UPrim, *F, *G, *H, *S, *PHI;  /* PHI, S: NULL without gravity */
+  double t, dt;
+  int it;
+} tlqo_state;
+
+/* mainHD.f90:38-44: borders(U,1), calc_prims(UPrim,U) (+ point potential). */
+void tlqo_init(const tlqo_params* p, tlqo_state* s);
+/* mainHD.f90:61-100: at most nsteps loop iterations while t < tfin.
+ * Returns the number of iterations run. */
+int tlqo_run(const tlqo_params* p, tlqo_state* s, int nsteps, double tfin);
+
+/* Floating-point operation counts of the instrumented build (oracle_count.c). */
+typedef struct tlqo_flops { double add, mul, div, sqrt, cmp, trans; } tlqo_flops;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

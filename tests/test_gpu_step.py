@@ -1,0 +1,266 @@
+"""Fused-step parity: tlq_upload + tlq_step (two fused CUDA stage kernels per
+step) against the oracle's main loop (mainHD.f90:61-100) on the same inputs.
+
+Without cooling the plain FP64 path is bit-identical to the oracle on every
+cell the scheme defines (interior and the first ghost layer of each face);
+with cooling the transcendental functions differ by ulps, so the bar is the
+spec one, relative L1 <= 1e-10 per conserved variable after 10 steps.
+The physics checks rerun the reference's own tests at full size and compare
+the scores with the oracle's (tests/golden/oracle_metrics.json)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Run
+from tests.conftest import ROOT
+from tests.helpers import face_ghost_mask, interior, oracle_params, rel_l1
+from tlaloque_gb300 import analysis, problems, tlq
+
+pytestmark = pytest.mark.gpu
+
+
+def smooth_state(cfg, seed=0, amp=0.3, mach=0.6):
+    """Smooth random state: a few seeded Fourier modes per field."""
+    rng = np.random.default_rng(seed)
+    x, y, z = problems.cell_centres(cfg)
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    Lx, Ly, Lz = cfg.xr - cfg.xl, cfg.yr - cfg.yl, cfg.zr - cfg.zl
+
+    def field():
+        f = np.zeros_like(X)
+        for _ in range(4):
+            k = rng.integers(1, 3, 3)
+            ph = rng.uniform(0, 2 * np.pi, 3)
+            f += rng.standard_normal() * np.sin(2 * np.pi * k[0] * X / Lx + ph[0]) * \
+                np.sin(2 * np.pi * k[1] * Y / Ly + ph[1]) * np.sin(2 * np.pi * k[2] * Z / Lz + ph[2])
+        return f / 2.0
+
+    rho = np.exp(amp * field())
+    p = np.exp(amp * field())
+    cs = np.sqrt(cfg.gamma * p / rho)
+    return problems.conserved(cfg, rho, mach * cs * field(), mach * cs * field(), mach * cs * field(), p)
+
+
+def run_both(cfg, U0, nsteps):
+    run = Run(oracle_params(cfg), U0)
+    run.run(nsteps)
+    U1 = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U1, 1)  # mainHD.f90:38, on the GPU entry point
+        ctx.upload(U1)
+        hist = [ctx.step() for _ in range(nsteps)]
+        Ug, Wg = ctx.state()
+    return run, hist, Ug, Wg
+
+
+def assert_bit_exact(cfg, run, hist, Ug, Wg):
+    m = face_ghost_mask(cfg)
+    np.testing.assert_array_equal(Ug[:, m], run.U[:, m])
+    np.testing.assert_array_equal(interior(Wg), interior(run.UPrim))
+    t, it, dt = hist[-1]
+    assert (t, it, dt) == (run.t, run.it, run.dt)
+
+
+BC3 = (tlq.BC_REFLECTIVE, tlq.BC_OUTFLOW, tlq.BC_PERIODIC, tlq.BC_PERIODIC, tlq.BC_OUTFLOW, tlq.BC_REFLECTIVE)
+
+
+@pytest.mark.parametrize("limiter", [1, 2, 3, 4, 5, 6])
+def test_step_bit_exact_limiters_mixed_bc(gpu_lib, limiter):
+    """Odd sizes (partial tiles in x and y), mixed boundary kinds."""
+    cfg = tlq.Config(nx=19, ny=13, nz=11, xl=0.0, xr=1.0, yl=0.0, yr=0.8, zl=0.0, zr=0.6, limiter=limiter, bc=BC3,
+                     eta=0.01)
+    run, hist, Ug, Wg = run_both(cfg, smooth_state(cfg, seed=limiter), 10)
+    assert_bit_exact(cfg, run, hist, Ug, Wg)
+
+
+@pytest.mark.parametrize("solver", [tlq.SOLVER_HLLC, tlq.SOLVER_HLL])
+def test_step_bit_exact_periodic_z_chunks(gpu_lib, solver):
+    """nz large enough for several z chunks per column (chunk prologues)."""
+    cfg = tlq.Config(nx=17, ny=9, nz=70, xl=0.0, xr=1.0, yl=0.0, yr=0.5, zl=0.0, zr=4.0, solver=solver,
+                     bc=(tlq.BC_PERIODIC,) * 6)
+    run, hist, Ug, Wg = run_both(cfg, smooth_state(cfg, seed=3, mach=1.2), 10)
+    assert_bit_exact(cfg, run, hist, Ug, Wg)
+
+
+def test_step_bit_exact_sod_tube(gpu_lib):
+    cfg, U0 = problems.sod_tube()
+    run, hist, Ug, Wg = run_both(cfg, U0, 10)
+    assert_bit_exact(cfg, run, hist, Ug, Wg)
+
+
+def test_step_bit_exact_sedov_small(gpu_lib):
+    cfg, U0 = problems.sedov(24)
+    run, hist, Ug, Wg = run_both(cfg, U0, 10)
+    assert_bit_exact(cfg, run, hist, Ug, Wg)
+
+
+def test_step_gravity_and_winds_bit_exact(gpu_lib):
+    """Winds (one crossing a boundary) and point-mass gravity, no cooling."""
+    cfg, U0 = problems.wind_bubble(32, cooling=tlq.COOL_NONE)
+    cfg.winds.append(tlq.Wind(xc=cfg.xr - 1.5 * cfg.dx, yc=0.0, zc=0.0, radius=3.0 * cfg.dx, mdot=cfg.winds[0].mdot,
+                              vinf=5e7, temp=1e4, mu=1.3))
+    cfg.masses = np.array([[0.0, 0.0, 0.0, 1e36], [cfg.dx * 7.3, -cfg.dx * 2.1, 0.0, 3e35]])
+    run, hist, Ug, Wg = run_both(cfg, U0, 10)
+    assert_bit_exact(cfg, run, hist, Ug, Wg)
+
+
+@pytest.mark.parametrize("mode", [tlq.COOL_REF, tlq.COOL_SUBCYCLE])
+def test_step_wind_bubble_with_cooling(gpu_lib, mode):
+    """The wind-bubble physics (wind, point mass, cooling) at 32^3: relative
+    L1 <= 1e-10 per conserved variable after 10 steps (cooling's exp, log10
+    and pow differ between the CPU and GPU math libraries by ulps)."""
+    cfg, U0 = problems.wind_bubble(32, cooling=mode)
+    # hotter, denser ambient so that cooling acts strongly in 10 steps
+    x, y, z = problems.cell_centres(cfg)
+    T = 10.0 ** (5.0 + 1.5 * np.sin(3 * x)[:, None, None] * np.cos(2 * y)[None, :, None] + 0 * z[None, None, :])
+    n = 30.0
+    U0 = problems.conserved(cfg, n * cfg.mu0 * problems.AMU, 0.0, 0.0, 0.0, n * problems.KB * T)
+    run, hist, Ug, Wg = run_both(cfg, U0, 10)
+    m = face_ghost_mask(cfg)
+    err = rel_l1(Ug[:, m], run.U[:, m])
+    assert np.all(err <= 1e-10), err
+    assert abs(hist[-1][0] - run.t) <= 1e-10 * run.t
+    assert hist[-1][1] == run.it
+    # cooling did act
+    assert np.max(np.abs(interior(run.UPrim)[4] - interior(run.o.calc_prims(run.U))[4])) >= 0.0
+
+
+def test_step_advance_graph_matches_step(gpu_lib):
+    """tlq_advance (graph replays) gives the same state as single tlq_step calls."""
+    cfg = tlq.Config(nx=24, ny=16, nz=20, bc=(tlq.BC_PERIODIC,) * 6)
+    U0 = smooth_state(cfg, seed=9)
+    outs = []
+    for mode in ("step", "advance"):
+        U1 = U0.copy(order="F")
+        with tlq.Context(cfg) as ctx:
+            ctx.borders(U1, 1)
+            ctx.upload(U1)
+            if mode == "step":
+                for _ in range(7):
+                    ctx.step()
+            else:
+                ctx.advance(7)
+            outs.append((ctx.state(), ctx.time()))
+    np.testing.assert_array_equal(outs[0][0][0], outs[1][0][0])
+    assert outs[0][1] == outs[1][1]
+
+
+def test_run_until_stops_like_the_reference_loop(gpu_lib):
+    """tlq_run_until: the loop condition t < tfin is tested before each step
+    and the last step is not clamped (mainHD.f90:61)."""
+    cfg, U0 = problems.sod_tube(64)
+    run = Run(oracle_params(cfg), U0)
+    run.run(10 ** 6, 0.05)
+    U1 = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U1, 1)
+        ctx.upload(U1)
+        t, it, dt = ctx.run_until(0.05)
+        Ug, Wg = ctx.state()
+    assert (t, it) == (run.t, run.it)
+    np.testing.assert_array_equal(interior(Ug), interior(run.U))
+
+
+def test_checkpoint_resume_bit_exact(gpu_lib):
+    """Download/upload of the state in the middle of a run (the checkpoint
+    primitive) continues bit-identically to an uninterrupted run.  The first
+    ghost layer is part of the state (it holds UP's boundary values)."""
+    cfg = tlq.Config(nx=20, ny=12, nz=16, bc=(tlq.BC_OUTFLOW,) * 6)
+    U0 = smooth_state(cfg, seed=4)
+    U1 = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U1, 1)
+        ctx.upload(U1)
+        ctx.advance(8)
+        ref_U, _ = ctx.state()
+        ref_t = ctx.time()
+    with tlq.Context(cfg) as ctx:
+        U2 = U0.copy(order="F")
+        ctx.borders(U2, 1)
+        ctx.upload(U2)
+        ctx.advance(3)
+        ck, _ = ctx.state()
+        t, it, dt, _ = ctx.time()
+    with tlq.Context(cfg) as ctx:
+        ctx.set_time(t, it)
+        ctx.upload(ck)
+        ctx.advance(5)
+        U3, _ = ctx.state()
+        t3 = ctx.time()
+    m = face_ghost_mask(cfg)
+    np.testing.assert_array_equal(U3[:, m], ref_U[:, m])
+    assert t3[:2] == ref_t[:2]
+
+
+def test_status_reports_negative_density(gpu_lib):
+    """A host-side injected bad state (negative density) comes back as an
+    error status from tlq_step, not a crash."""
+    cfg = tlq.Config(nx=16, ny=16, nz=16, bc=(tlq.BC_PERIODIC,) * 6)
+    U0 = smooth_state(cfg, seed=2)
+    U0[0, 8, 8, 8] = -1.0
+    with tlq.Context(cfg) as ctx:
+        ctx.upload(U0)
+        t, it, dt = ctx.step(check=False)
+        rc = ctx.time()[3]
+    assert rc in (tlq.ERR_NEG_DENSITY, tlq.ERR_NONFINITE_DT)
+
+
+# ---------------------------------------------------------------------------
+# Full-size physics, scored like the reference's analysis.
+# ---------------------------------------------------------------------------
+def _golden_metrics():
+    with open(os.path.join(ROOT, "tests", "golden", "oracle_metrics.json")) as f:
+        return json.load(f)
+
+
+def _gpu_run(cfg, U0, tfin):
+    U1 = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U1, 1)
+        ctx.upload(U1)
+        t, it, dt = ctx.run_until(tfin)
+        U, W = ctx.state()
+    return t, it, U, W
+
+
+def test_sod_tube_full(gpu_lib):
+    cfg, U0 = problems.sod_tube()
+    t, it, U, W = _gpu_run(cfg, U0, problems.SOD_TFIN)
+    x = cfg.xl + cfg.dx * (np.arange(cfg.nx) + 0.5)
+    rho_ex, u_ex, p_ex = analysis.sod_exact(x, t)
+    g = _golden_metrics()["sod_tube_256"]
+    assert (t, it) == (g["t"], g["it"])
+    assert analysis.norm_L1(rho_ex, W[0, 2:-2, 4, 4]) == pytest.approx(g["L1_rho"], rel=1e-12)
+
+
+def test_diagonal_sod_150_reproduces_reference_error(gpu_lib, golden):
+    """The reference's own Sod test at its own resolution (150^3), scored with
+    its metrics against its exact-solution file: the same numbers as the
+    oracle's run of the reference algorithm."""
+    cfg, U0 = problems.diagonal_sod(150)
+    t, it, U, W = _gpu_run(cfg, U0, problems.DIAG_SOD_TFIN)
+    g = _golden_metrics()["diagonal_sod_150"]
+    assert (t, it) == (g["t"], g["it"])
+    ref = golden["sod_e1rpex"]
+    r, rho, vel, p, e = analysis.diagonal_profiles(cfg, W)
+    for name, col, y in (("rho", 1, rho), ("p", 3, p), ("v", 2, vel), ("e", 4, e)):
+        _, mape, rmspe, L1, L2, Linf = analysis.all_error_metrics(ref[:, 0] - 0.25, ref[:, col], r, y)
+        assert L1 == pytest.approx(g["metrics"][name]["L1"], rel=1e-9)
+        assert mape == pytest.approx(g["metrics"][name]["MAPE"], rel=1e-9)
+
+
+def test_sedov_128_against_similarity_solution(gpu_lib, golden):
+    cfg, U0 = problems.sedov(128)
+    t, it, U, W = _gpu_run(cfg, U0, problems.SEDOV_TFIN)
+    g = _golden_metrics()["sedov_128"]
+    assert (t, it) == (g["t"], g["it"])
+    Rs = problems.sedov_shock_radius(t, xi0=float(golden["sedov53_xi0"]))
+    rc, prof = analysis.radial_profile(cfg, W[0, 2:-2, 2:-2, 2:-2], nbins=64, rmax=0.48)
+    ok = np.isfinite(prof)
+    r_peak = float(rc[ok][np.argmax(prof[ok])])
+    assert abs(r_peak - Rs) < 2.0 * cfg.dx
+    exact = analysis.sedov_density(rc, t, golden["sedov53"])
+    inner = ok & (rc < 1.2 * Rs)
+    assert analysis.norm_L1(exact[inner], prof[inner]) == pytest.approx(g["L1_rho"], rel=1e-9)

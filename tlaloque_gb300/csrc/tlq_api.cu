@@ -1,0 +1,756 @@
+// tlq_api.cu -- host side of libtlq: the C ABI declared in include/tlq.h.
+//
+// The context owns the whole mesh in HBM (structure-of-arrays, two copies of
+// U for ping-pong, UPP, the carried pressure and the potential), the device
+// clock, the tensor maps the stage kernels stream through, and one CUDA
+// graph per buffer parity so that a step is one graph launch.
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/tlq.h"
+#include "tlq_internal.h"
+
+using namespace tlq;
+
+struct tlq_ctx {
+  tlq_config cfg{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Params P{};
+  Layout L{};
+  Aos A{};
+  // device state
+  double* U[2] = {nullptr, nullptr};
+  double* UPP = nullptr;
+  double* Pc = nullptr;   // carried pressure plane (cooling)
+  double* phi = nullptr;  // point-mass potential plane
+  Clock* clk = nullptr;
+  Clock* clk_host = nullptr;  // pinned mirror
+  double* partials = nullptr;
+  int npartials = 0;
+  double* sums_partials = nullptr;
+  double* sums_out = nullptr;
+  double* staging = nullptr;  // one reference-layout array
+  // tables
+  double *dT = nullptr, *dlogT = nullptr, *dC = nullptr;
+  Wind* dwinds = nullptr;
+  double* dmasses = nullptr;
+  int nmasses = 0;
+  std::vector<double> masses_host;
+  // per-routine scratch (reference layout), allocated on first use
+  double* rb[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double* rphi = nullptr;
+  Clock* rclk = nullptr;
+  double* rpartials = nullptr;
+  // stage launch geometry and tensor maps
+  dim3 grid{};
+  int zlen = 0;
+  CUtensorMap tm_U[2]{}, tm_UPP{}, tm_P{};
+  // run state
+  int cur = 0;  // U[cur] holds the current state
+  long long it_base = 0;
+  bool uploaded = false;
+  double t0 = 0.0;
+  int it0 = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  double ms1_acc = 0.0, ms2_acc = 0.0;
+  long long ntimed = 0;
+  long long steps = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(tlq_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(tlq_ctx* c, cudaError_t e, const char* where) {
+  if (c) c->err = std::string(where) + ": " + cudaGetErrorString(e);
+  return TLQ_ERR_CUDA;
+}
+
+#define CK(call)                                                        \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);            \
+  } while (0)
+
+size_t array_bytes(const tlq_config& c) { return (size_t)5 * (c.nx + 4) * (size_t)(c.ny + 4) * (size_t)(c.nz + 4) * 8; }
+size_t phi_bytes(const tlq_config& c) { return (size_t)(c.nx + 2) * (size_t)(c.ny + 2) * (size_t)(c.nz + 2) * 8; }
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 4-D map {x, y, z, var} over a SoA array with `nvar` planes; box = tile + halo 2.
+int make_map(tlq_ctx* ctx, CUtensorMap* m, double* base, int nvar) {
+  auto fn = encode_fn();
+  if (!fn) return fail(ctx, TLQ_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const Layout& L = ctx->L;
+  cuuint64_t dims[4] = {(cuuint64_t)(ctx->cfg.nx + 4), (cuuint64_t)(ctx->cfg.ny + 4), (cuuint64_t)(ctx->cfg.nz + 4),
+                        (cuuint64_t)nvar};
+  cuuint64_t strides[3] = {(cuuint64_t)L.px * 8, (cuuint64_t)L.px * L.nyg * 8, (cuuint64_t)L.plane * 8};
+  cuuint32_t box[4] = {(cuuint32_t)HX, (cuuint32_t)HY, 1, (cuuint32_t)nvar};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ctx, TLQ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return TLQ_OK;
+}
+
+int validate(const tlq_config* c, std::string& why) {
+  if (c->nx < 2 || c->ny < 2 || c->nz < 2) { why = "nx, ny, nz must be >= 2"; return TLQ_ERR_CONFIG; }
+  if (!(c->xr > c->xl) || !(c->yr > c->yl) || !(c->zr > c->zl)) { why = "empty domain"; return TLQ_ERR_CONFIG; }
+  if (!(c->gamma > 1.0)) { why = "gamma must be > 1"; return TLQ_ERR_CONFIG; }
+  if (c->limiter < TLQ_LIMITER_NONE || c->limiter > TLQ_LIMITER_SUPERBEE) { why = "unknown limiter"; return TLQ_ERR_CONFIG; }
+  if (c->solver != TLQ_SOLVER_HLLC && c->solver != TLQ_SOLVER_HLL) { why = "unknown solver"; return TLQ_ERR_CONFIG; }
+  for (int q = 0; q < 6; ++q)
+    if (c->bc[q] < TLQ_BC_OUTFLOW || c->bc[q] > TLQ_BC_INFLOW) { why = "unknown boundary kind"; return TLQ_ERR_CONFIG; }
+  if (c->cooling < TLQ_COOL_NONE || c->cooling > TLQ_COOL_SUBCYCLE) { why = "unknown cooling mode"; return TLQ_ERR_CONFIG; }
+  if (c->cooling == TLQ_COOL_SUBCYCLE && (c->cool_max_sub < 1 || !(c->cool_sub_frac > 0.0))) {
+    why = "sub-cycled cooling needs cool_max_sub >= 1 and cool_sub_frac > 0";
+    return TLQ_ERR_CONFIG;
+  }
+  if (c->precision != TLQ_PREC_FP64) { why = "precision mode not available in this build"; return TLQ_ERR_CONFIG; }
+  return TLQ_OK;
+}
+
+void fill_params(tlq_ctx* c) {
+  const tlq_config& g = c->cfg;
+  Params& p = c->P;
+  p.nx = g.nx; p.ny = g.ny; p.nz = g.nz;
+  p.xl = g.xl; p.yl = g.yl; p.zl = g.zl;
+  p.dx = (g.xr - g.xl) / (double)g.nx;  // parameters.f90:89-91
+  p.dy = (g.yr - g.yl) / (double)g.ny;
+  p.dz = (g.zr - g.zl) / (double)g.nz;
+  p.gamma = g.gamma;
+  p.g1 = g.gamma / (g.gamma - 1.0);
+  p.cfl = g.cfl; p.eta = g.eta; p.mu0 = g.mu0; p.cooling_limit = g.cooling_limit;
+  p.cool_sub_frac = g.cool_sub_frac;
+  p.limiter = g.limiter; p.solver = g.solver; p.cooling = g.cooling; p.cool_max_sub = g.cool_max_sub;
+  for (int q = 0; q < 6; ++q) p.bc[q] = g.bc[q];
+}
+
+void invalidate_graphs(tlq_ctx* c) {
+  for (int q = 0; q < 2; ++q)
+    if (c->graph[q]) { cudaGraphExecDestroy(c->graph[q]); c->graph[q] = nullptr; }
+}
+
+int ensure_routine_scratch(tlq_ctx* ctx) {
+  if (ctx->rb[0]) return TLQ_OK;
+  const size_t b = array_bytes(ctx->cfg);
+  for (int q = 0; q < 6; ++q) {
+    cudaError_t e = cudaMalloc(&ctx->rb[q], b);
+    if (e != cudaSuccess) return fail(ctx, TLQ_ERR_NOMEM, "per-routine scratch: " + std::string(cudaGetErrorString(e)));
+  }
+  CK(cudaMalloc(&ctx->rphi, phi_bytes(ctx->cfg)));
+  CK(cudaMalloc(&ctx->rclk, sizeof(Clock)));
+  CK(cudaMalloc(&ctx->rpartials, sizeof(double) * 3 * (size_t)init_blocks(ctx->P)));
+  return TLQ_OK;
+}
+
+int status_from_bits(int bits) {
+  if (bits & ST_TIMEOUT) return TLQ_ERR_TIMEOUT;
+  if (bits & ST_NONFINITE_DT) return TLQ_ERR_NONFINITE_DT;
+  if (bits & ST_NEG_DENSITY) return TLQ_ERR_NEG_DENSITY;
+  return TLQ_OK;
+}
+
+// Enqueue one step (stage 1 + stage 2) on buffer parity `par`.
+int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
+  StageArgs a{};
+  a.p = ctx->P;
+  a.L = ctx->L;
+  a.clk = ctx->clk;
+  a.partials = ctx->partials;
+  a.zlen = ctx->zlen;
+  a.phi = ctx->phi;
+  // stage 1: U[par] -> UPP
+  a.uold = ctx->U[par];
+  a.out = ctx->UPP;
+  a.pout = nullptr;
+  a.use_p = ctx->cfg.cooling != TLQ_COOL_NONE;
+  if (timed) CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+  CK(launch_stage(1, ctx->cfg.precision, ctx->tm_U[par], ctx->tm_P, a, ctx->grid, ctx->stream));
+  if (timed) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+  // stage 2: UPP (+ U[par]) -> U[par^1]
+  a.out = ctx->U[par ^ 1];
+  a.pout = ctx->Pc;
+  a.use_p = 0;
+  CK(launch_stage(2, ctx->cfg.precision, ctx->tm_UPP, ctx->tm_P, a, ctx->grid, ctx->stream));
+  if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+  return TLQ_OK;
+}
+
+int build_graph(tlq_ctx* ctx, int par) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(ctx, par, false);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc != TLQ_OK) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&ctx->graph[par], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+  return TLQ_OK;
+}
+
+int run_steps(tlq_ctx* ctx, int n) {
+  for (int q = 0; q < n; ++q) {
+    const int par = ctx->cur;
+    if (ctx->timing) {
+      int rc = enqueue_step(ctx, par, true);
+      if (rc) return rc;
+      CK(cudaEventSynchronize(ctx->ev[2]));
+      float a = 0.f, b = 0.f;
+      cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+      cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+      ctx->ms1_acc += a;
+      ctx->ms2_acc += b;
+      ctx->ntimed += 1;
+    } else {
+      if (!ctx->graph[par]) {
+        int rc = build_graph(ctx, par);
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(ctx->graph[par], ctx->stream));
+    }
+    ctx->cur ^= 1;
+    ctx->steps += 1;
+  }
+  return TLQ_OK;
+}
+
+int set_tfin(tlq_ctx* ctx, double tfin) {
+  CK(cudaMemcpyAsync(&ctx->clk->tfin, &tfin, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  return TLQ_OK;
+}
+
+int read_clock(tlq_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->clk_host, ctx->clk, sizeof(Clock), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // The current buffer follows the number of steps the device really ran.
+  ctx->cur = (int)((ctx->clk_host->it - ctx->it_base) & 1LL);
+  return TLQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void tlq_config_default(tlq_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->nx = c->ny = c->nz = 50;
+  c->xl = c->yl = c->zl = -1.0;
+  c->xr = c->yr = c->zr = 1.0;
+  c->gamma = 5.0 / 3.0;
+  c->cfl = 0.4;
+  c->eta = 0.5e-2;
+  c->mu0 = 1.0;
+  c->cooling_limit = 0.5;
+  c->limiter = TLQ_LIMITER_VANLEER;
+  c->solver = TLQ_SOLVER_HLLC;
+  for (int q = 0; q < 6; ++q) c->bc[q] = TLQ_BC_REFLECTIVE;
+  c->cooling = TLQ_COOL_NONE;
+  c->cool_max_sub = 1;
+  c->cool_sub_frac = 0.1;
+  c->precision = TLQ_PREC_FP64;
+  c->device = 0;
+}
+
+const char* tlq_status_string(int s) {
+  switch (s) {
+    case TLQ_OK: return "ok";
+    case TLQ_ERR_CUDA: return "CUDA error";
+    case TLQ_ERR_CONFIG: return "invalid configuration";
+    case TLQ_ERR_NONFINITE_DT: return "non-finite CFL time step";
+    case TLQ_ERR_NEG_DENSITY: return "non-positive density";
+    case TLQ_ERR_TIMEOUT: return "device wait timed out";
+    case TLQ_ERR_ARG: return "invalid argument";
+    case TLQ_ERR_STATE: return "call out of order";
+    case TLQ_ERR_NOMEM: return "out of memory";
+    default: return "unknown status";
+  }
+}
+
+const char* tlq_last_error(tlq_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
+  if (!cfg || !out) return TLQ_ERR_ARG;
+  *out = nullptr;
+  std::string why;
+  int rc = validate(cfg, why);
+  if (rc) return rc;
+  tlq_ctx* ctx = new tlq_ctx();
+  ctx->cfg = *cfg;
+  auto bail = [&](int code) { tlq_destroy(ctx); return code; };
+  cudaError_t e = cudaSetDevice(cfg->device);
+  if (e != cudaSuccess) { tlq_destroy(ctx); return TLQ_ERR_CUDA; }
+  fill_params(ctx);
+  ctx->A = Aos{cfg->nx, cfg->ny, cfg->nz};
+  Layout& L = ctx->L;
+  L.px = ((cfg->nx + 4) + 7) / 8 * 8;
+  L.nyg = cfg->ny + 4;
+  L.nzg = cfg->nz + 4;
+  L.plane = (long long)L.px * L.nyg * L.nzg;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(TLQ_ERR_CUDA);
+  ctx->own_stream = true;
+  const size_t soa = (size_t)L.plane * 5 * sizeof(double);
+  if (cudaMalloc(&ctx->U[0], soa) || cudaMalloc(&ctx->U[1], soa) || cudaMalloc(&ctx->UPP, soa) ||
+      cudaMalloc(&ctx->Pc, (size_t)L.plane * 8) || cudaMalloc(&ctx->phi, (size_t)L.plane * 8) ||
+      cudaMalloc(&ctx->staging, array_bytes(*cfg)))
+    return bail(TLQ_ERR_NOMEM);
+  cudaMemset(ctx->U[0], 0, soa);
+  cudaMemset(ctx->U[1], 0, soa);
+  cudaMemset(ctx->UPP, 0, soa);
+  cudaMemset(ctx->Pc, 0, (size_t)L.plane * 8);
+  cudaMemset(ctx->phi, 0, (size_t)L.plane * 8);
+  if (cudaMalloc(&ctx->clk, sizeof(Clock)) || cudaMallocHost(&ctx->clk_host, sizeof(Clock))) return bail(TLQ_ERR_NOMEM);
+  std::memset(ctx->clk_host, 0, sizeof(Clock));
+  ctx->clk_host->tfin = std::numeric_limits<double>::infinity();
+  cudaMemcpy(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice);
+  // stage grid: TX x TY column tiles, z split into chunks of zlen planes
+  const int gx = (cfg->nx + TX - 1) / TX, gy = (cfg->ny + TY - 1) / TY;
+  ctx->zlen = cfg->nz >= 128 ? 64 : (cfg->nz >= 32 ? 32 : cfg->nz);
+  const int gz = (cfg->nz + ctx->zlen - 1) / ctx->zlen;
+  ctx->grid = dim3(gx, gy, gz);
+  ctx->npartials = gx * gy * gz;
+  const int nb = init_blocks(ctx->P);
+  if (cudaMalloc(&ctx->partials, sizeof(double) * 3 * (size_t)std::max(ctx->npartials, nb)) ||
+      cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
+    return bail(TLQ_ERR_NOMEM);
+  if (prepare_stage_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
+  int r = make_map(ctx, &ctx->tm_U[0], ctx->U[0], 5);
+  if (!r) r = make_map(ctx, &ctx->tm_U[1], ctx->U[1], 5);
+  if (!r) r = make_map(ctx, &ctx->tm_UPP, ctx->UPP, 5);
+  if (!r) r = make_map(ctx, &ctx->tm_P, ctx->Pc, 1);
+  if (r) return bail(r);
+  for (int q = 0; q < 3; ++q) cudaEventCreate(&ctx->ev[q]);
+  if (cudaDeviceSynchronize() != cudaSuccess) return bail(TLQ_ERR_CUDA);
+  *out = ctx;
+  return TLQ_OK;
+}
+
+int tlq_destroy(tlq_ctx* ctx) {
+  if (!ctx) return TLQ_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  invalidate_graphs(ctx);
+  for (int q = 0; q < 3; ++q)
+    if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
+  cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
+  cudaFree(ctx->clk); cudaFree(ctx->partials); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
+  cudaFree(ctx->staging);
+  cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);
+  for (int q = 0; q < 6; ++q) cudaFree(ctx->rb[q]);
+  cudaFree(ctx->rphi); cudaFree(ctx->rclk); cudaFree(ctx->rpartials);
+  if (ctx->clk_host) cudaFreeHost(ctx->clk_host);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return TLQ_OK;
+}
+
+int tlq_set_stream(tlq_ctx* ctx, void* s) {
+  if (!ctx) return TLQ_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  if (s) {
+    ctx->stream = (cudaStream_t)s;
+    ctx->own_stream = false;
+  } else {
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    ctx->own_stream = true;
+  }
+  invalidate_graphs(ctx);
+  return TLQ_OK;
+}
+
+int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int n) {
+  if (!ctx || !T || !logL || n < 2) return TLQ_ERR_ARG;
+  for (int q = 1; q < n; ++q)
+    if (!(T[q] >= T[q - 1])) return fail(ctx, TLQ_ERR_ARG, "cooling table temperatures must be ascending");
+  std::vector<double> lt(n);
+  for (int q = 0; q < n; ++q) lt[q] = std::log10(T[q]);
+  cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC);
+  ctx->dT = ctx->dlogT = ctx->dC = nullptr;
+  CK(cudaMalloc(&ctx->dT, n * sizeof(double)));
+  CK(cudaMalloc(&ctx->dlogT, n * sizeof(double)));
+  CK(cudaMalloc(&ctx->dC, n * sizeof(double)));
+  CK(cudaMemcpy(ctx->dT, T, n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dC, logL, n * sizeof(double), cudaMemcpyHostToDevice));
+  // log10 of the table temperatures is evaluated on the device, like the
+  // reference does at each lookup (cooling.f90:135,137).
+  CK(cudaMemcpy(ctx->dlogT, T, n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(launch_log10_inplace(ctx->dlogT, n, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->P.cool = CoolTable{ctx->dT, ctx->dlogT, ctx->dC, n};
+  invalidate_graphs(ctx);
+  return TLQ_OK;
+}
+
+int tlq_set_winds(tlq_ctx* ctx, const tlq_wind* w, int n) {
+  if (!ctx || n < 0 || (n > 0 && !w)) return TLQ_ERR_ARG;
+  cudaFree(ctx->dwinds);
+  ctx->dwinds = nullptr;
+  ctx->P.nwinds = 0;
+  ctx->P.winds = nullptr;
+  if (n > 0) {
+    std::vector<Wind> hw(n);
+    const Params& p = ctx->P;
+    for (int q = 0; q < n; ++q) {
+      Wind& d = hw[q];
+      d.xc = w[q].xc; d.yc = w[q].yc; d.zc = w[q].zc;
+      d.vx = w[q].vx; d.vy = w[q].vy; d.vz = w[q].vz;
+      d.radius = w[q].radius; d.mdot = w[q].mdot; d.vinf = w[q].vinf; d.temp = w[q].temp; d.mu = w[q].mu;
+      // Index box of the cells whose centre can lie within radius (one cell
+      // of margin on each side; the exact test runs inside the box).
+      auto lo = [](double c, double r, double l, double h) { return (int)std::floor((c - r - l) / h + 0.5) - 1; };
+      auto hi = [](double c, double r, double l, double h) { return (int)std::ceil((c + r - l) / h + 0.5) + 1; };
+      d.ilo = std::max(-1, lo(d.xc, d.radius, p.xl, p.dx)); d.ihi = std::min(p.nx + 2, hi(d.xc, d.radius, p.xl, p.dx));
+      d.jlo = std::max(-1, lo(d.yc, d.radius, p.yl, p.dy)); d.jhi = std::min(p.ny + 2, hi(d.yc, d.radius, p.yl, p.dy));
+      d.klo = std::max(-1, lo(d.zc, d.radius, p.zl, p.dz)); d.khi = std::min(p.nz + 2, hi(d.zc, d.radius, p.zl, p.dz));
+    }
+    CK(cudaMalloc(&ctx->dwinds, n * sizeof(Wind)));
+    CK(cudaMemcpy(ctx->dwinds, hw.data(), n * sizeof(Wind), cudaMemcpyHostToDevice));
+    ctx->P.nwinds = n;
+    ctx->P.winds = ctx->dwinds;
+  }
+  invalidate_graphs(ctx);
+  return TLQ_OK;
+}
+
+int tlq_set_point_masses(tlq_ctx* ctx, const double* xyzm, int n) {
+  if (!ctx || n < 0 || (n > 0 && !xyzm)) return TLQ_ERR_ARG;
+  cudaFree(ctx->dmasses);
+  ctx->dmasses = nullptr;
+  ctx->nmasses = 0;
+  ctx->P.gravity = 0;
+  CK(cudaMemsetAsync(ctx->phi, 0, (size_t)ctx->L.plane * 8, ctx->stream));
+  if (n > 0) {
+    CK(cudaMalloc(&ctx->dmasses, 4 * n * sizeof(double)));
+    CK(cudaMemcpy(ctx->dmasses, xyzm, 4 * n * sizeof(double), cudaMemcpyHostToDevice));
+    ctx->nmasses = n;
+    ctx->P.gravity = 1;
+    CK(launch_point_potential_soa(ctx->P, ctx->L, ctx->dmasses, n, ctx->phi, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  invalidate_graphs(ctx);
+  return TLQ_OK;
+}
+
+int tlq_set_time(tlq_ctx* ctx, double t, int it) {
+  if (!ctx) return TLQ_ERR_ARG;
+  ctx->t0 = t;
+  ctx->it0 = it;
+  if (ctx->uploaded) {
+    CK(cudaMemcpyAsync(&ctx->clk->t, &ctx->t0, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    long long itl = it;
+    CK(cudaMemcpyAsync(&ctx->clk->it, &itl, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->it_base = it - (long long)ctx->cur;
+  }
+  return TLQ_OK;
+}
+
+int tlq_upload(tlq_ctx* ctx, const double* U) {
+  if (!ctx || !U) return TLQ_ERR_ARG;
+  if (ctx->cfg.cooling != TLQ_COOL_NONE && !ctx->dT) return fail(ctx, TLQ_ERR_STATE, "cooling on but no cooling table");
+  CK(cudaMemcpyAsync(ctx->staging, U, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_aos_to_soa(ctx->A, ctx->L, ctx->staging, ctx->U[0], ctx->stream));
+  Clock c{};
+  c.t = ctx->t0;
+  c.it = ctx->it0;
+  c.tfin = std::numeric_limits<double>::infinity();
+  *ctx->clk_host = c;
+  CK(cudaMemcpyAsync(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], ctx->cfg.cooling != TLQ_COOL_NONE ? ctx->Pc : nullptr, ctx->clk,
+                          ctx->partials, init_blocks(ctx->P), ctx->stream));
+  ctx->cur = 0;
+  ctx->it_base = ctx->it0;
+  ctx->steps = 0;
+  ctx->uploaded = true;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_download(tlq_ctx* ctx, double* U, double* W) {
+  if (!ctx) return TLQ_ERR_ARG;
+  if (!ctx->uploaded) return fail(ctx, TLQ_ERR_STATE, "tlq_download before tlq_upload");
+  int rc = read_clock(ctx);
+  if (rc) return rc;
+  if (U) {
+    CK(launch_soa_to_aos(ctx->A, ctx->L, ctx->U[ctx->cur], ctx->staging, ctx->stream));
+    CK(cudaMemcpyAsync(U, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  if (W) {
+    CK(launch_prims_soa_to_aos(ctx->P, ctx->A, ctx->L, ctx->U[ctx->cur],
+                               ctx->cfg.cooling != TLQ_COOL_NONE ? ctx->Pc : nullptr, ctx->staging, ctx->stream));
+    CK(cudaMemcpyAsync(W, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_get_time(tlq_ctx* ctx, double* t, int* it, double* dt) {
+  if (!ctx) return TLQ_ERR_ARG;
+  int rc = read_clock(ctx);
+  if (rc) return rc;
+  if (t) *t = ctx->clk_host->t;
+  if (it) *it = (int)ctx->clk_host->it;
+  if (dt) *dt = ctx->clk_host->dt_used;
+  return status_from_bits(ctx->clk_host->status);
+}
+
+int tlq_step(tlq_ctx* ctx, double* t, int* it, double* dt) {
+  if (!ctx) return TLQ_ERR_ARG;
+  if (!ctx->uploaded) return fail(ctx, TLQ_ERR_STATE, "tlq_step before tlq_upload");
+  int rc = run_steps(ctx, 1);
+  if (rc) return rc;
+  return tlq_get_time(ctx, t, it, dt);
+}
+
+int tlq_advance(tlq_ctx* ctx, int n) {
+  if (!ctx || n < 0) return TLQ_ERR_ARG;
+  if (!ctx->uploaded) return fail(ctx, TLQ_ERR_STATE, "tlq_advance before tlq_upload");
+  return run_steps(ctx, n);
+}
+
+int tlq_run_until(tlq_ctx* ctx, double tfin, int max_steps, double* t, int* it, double* dt) {
+  if (!ctx || max_steps < 0) return TLQ_ERR_ARG;
+  if (!ctx->uploaded) return fail(ctx, TLQ_ERR_STATE, "tlq_run_until before tlq_upload");
+  int rc = set_tfin(ctx, tfin);
+  if (rc) return rc;
+  int left = max_steps;
+  while (left > 0) {
+    // Steps whose start finds t >= tfin do nothing on the device; the host
+    // re-reads the clock after each batch and stops once t >= tfin.
+    const int batch = std::min(left, 64);
+    rc = run_steps(ctx, batch);
+    if (rc) break;
+    left -= batch;
+    rc = read_clock(ctx);
+    if (rc) break;
+    if (!(ctx->clk_host->t < tfin) || ctx->clk_host->status) break;
+  }
+  const double inf = std::numeric_limits<double>::infinity();
+  int rc2 = set_tfin(ctx, inf);
+  if (rc) return rc;
+  if (rc2) return rc2;
+  return tlq_get_time(ctx, t, it, dt);
+}
+
+int tlq_synchronize(tlq_ctx* ctx) {
+  if (!ctx) return TLQ_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_enable_timing(tlq_ctx* ctx, int on) {
+  if (!ctx) return TLQ_ERR_ARG;
+  ctx->timing = on != 0;
+  ctx->ms1_acc = ctx->ms2_acc = 0.0;
+  ctx->ntimed = 0;
+  return TLQ_OK;
+}
+
+int tlq_stats_get(tlq_ctx* ctx, tlq_stats* s) {
+  if (!ctx || !s) return TLQ_ERR_ARG;
+  std::memset(s, 0, sizeof(*s));
+  if (ctx->uploaded) {
+    int rc = read_clock(ctx);
+    if (rc) return rc;
+    s->t = ctx->clk_host->t;
+    s->dt = ctx->clk_host->dt_used;
+    s->status = status_from_bits(ctx->clk_host->status);
+  }
+  s->steps = ctx->steps;
+  s->graph = (ctx->graph[0] || ctx->graph[1]) ? 1 : 0;
+  s->timed = ctx->ntimed;
+  s->ms_stage1 = ctx->ntimed ? ctx->ms1_acc / ctx->ntimed : 0.0;
+  s->ms_stage2 = ctx->ntimed ? ctx->ms2_acc / ctx->ntimed : 0.0;
+  s->bytes_state = (double)ctx->L.plane * 8.0 * 17.0;
+  return TLQ_OK;
+}
+
+int tlq_conserved_sums(tlq_ctx* ctx, double out[5]) {
+  if (!ctx || !out) return TLQ_ERR_ARG;
+  if (!ctx->uploaded) return fail(ctx, TLQ_ERR_STATE, "tlq_conserved_sums before tlq_upload");
+  int rc = read_clock(ctx);
+  if (rc) return rc;
+  const int nb = init_blocks(ctx->P);
+  CK(launch_conserved_sums(ctx->P, ctx->L, ctx->U[ctx->cur], ctx->sums_partials, nb, ctx->sums_out, ctx->stream));
+  CK(cudaMemcpyAsync(out, ctx->sums_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+// ---- per-routine entry points ---------------------------------------------
+#define NEED(p) \
+  if (!(p)) return fail(ctx, TLQ_ERR_ARG, "null array argument")
+
+int tlq_calc_prims(tlq_ctx* ctx, double* W, const double* U) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(W); NEED(U);
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[0], U, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_calc_prims_aos(ctx->P, ctx->A, ctx->rb[1], ctx->rb[0], ctx->stream));
+  CK(cudaMemcpyAsync(W, ctx->rb[1], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_time_step(tlq_ctx* ctx, const double* W, double* dt) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(W); NEED(dt);
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->rb[0], W, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
+  Clock c{};
+  CK(cudaMemcpyAsync(ctx->rclk, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_time_step_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rclk, ctx->rpartials, init_blocks(ctx->P), ctx->stream));
+  CK(cudaMemcpyAsync(&c, ctx->rclk, sizeof(Clock), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *dt = c.dt;
+  return status_from_bits(c.status);
+}
+
+int tlq_fluxes(tlq_ctx* ctx, const double* U, double* F, double* G, double* H, const double* W, int choice) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(U); NEED(F); NEED(G); NEED(H); NEED(W);
+  if (choice != 1 && choice != 2) return fail(ctx, TLQ_ERR_ARG, "choice must be 1 or 2");
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[0], U, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[1], W, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[2], F, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[3], G, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[4], H, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_fluxes_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rb[1], ctx->rb[2], ctx->rb[3], ctx->rb[4], choice, ctx->stream));
+  CK(cudaMemcpyAsync(F, ctx->rb[2], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(G, ctx->rb[3], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(H, ctx->rb[4], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_godunov(tlq_ctx* ctx, double* UPPP, const double* UU, const double* F, const double* G, const double* H,
+                const double* W, double dt) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(UPPP); NEED(UU); NEED(F); NEED(G); NEED(H);
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[0], UU, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[1], F, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[2], G, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[3], H, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[4], UPPP, b, cudaMemcpyHostToDevice, ctx->stream));
+  const bool grav = ctx->nmasses > 0 && W;
+  if (grav) {
+    CK(cudaMemcpyAsync(ctx->rb[5], W, b, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(ctx->rphi, 0, phi_bytes(ctx->cfg), ctx->stream));
+    CK(launch_point_potential_ref(ctx->P, ctx->dmasses, ctx->nmasses, ctx->rphi, ctx->stream));
+  }
+  CK(launch_godunov_aos(ctx->P, ctx->A, ctx->rb[4], ctx->rb[0], ctx->rb[1], ctx->rb[2], ctx->rb[3],
+                        grav ? ctx->rb[5] : nullptr, grav ? ctx->rphi : nullptr, dt, ctx->stream));
+  CK(cudaMemcpyAsync(UPPP, ctx->rb[4], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_borders(tlq_ctx* ctx, double* U, int order) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(U);
+  if (order != 1 && order != 2) return fail(ctx, TLQ_ERR_ARG, "order must be 1 or 2");
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[0], U, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_borders_aos(ctx->P, ctx->A, ctx->rb[0], order, ctx->stream));
+  CK(cudaMemcpyAsync(U, ctx->rb[0], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_viscous_step(tlq_ctx* ctx, double* U, const double* UP, double* t, int* it, double dt) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(U); NEED(UP);
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[2], U, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[1], UP, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_viscous_step_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rb[1], ctx->rb[2], ctx->stream));
+  CK(cudaMemcpyAsync(U, ctx->rb[0], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (t) *t = *t + dt;
+  if (it) *it = *it + 1;
+  return TLQ_OK;
+}
+
+int tlq_cooling(tlq_ctx* ctx, double* W, double* U, double dt) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(W); NEED(U);
+  if (ctx->cfg.cooling == TLQ_COOL_NONE) return TLQ_OK;
+  if (!ctx->dT) return fail(ctx, TLQ_ERR_STATE, "cooling table not set");
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[0], W, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rb[1], U, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_cooling_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rb[1], dt, ctx->stream));
+  CK(cudaMemcpyAsync(W, ctx->rb[0], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(U, ctx->rb[1], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_point_potential(tlq_ctx* ctx, double* phi) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(phi);
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = phi_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rphi, phi, b, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->nmasses > 0) CK(launch_point_potential_ref(ctx->P, ctx->dmasses, ctx->nmasses, ctx->rphi, ctx->stream));
+  CK(cudaMemcpyAsync(phi, ctx->rphi, b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_gravity_source(tlq_ctx* ctx, const double* W, const double* phi, double* S) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(W); NEED(phi); NEED(S);
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const size_t b = array_bytes(ctx->cfg);
+  CK(cudaMemcpyAsync(ctx->rb[0], W, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->rphi, phi, phi_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_gravity_source_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rphi, ctx->rb[1], ctx->stream));
+  CK(cudaMemcpyAsync(S, ctx->rb[1], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+// tlq_device.cuh -- device layout, clock, TMA/mbarrier helpers and the
+// single-pass CFL grid reduction shared by the kernels of libtlq.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tlq_physics.cuh"
+
+namespace tlq {
+
+// Status bits held in Clock::status (mapped to TLQ_ERR_* on the host).
+constexpr int ST_NONFINITE_DT = 1;
+constexpr int ST_NEG_DENSITY = 2;
+constexpr int ST_TIMEOUT = 4;
+
+// Device-resident time of the run (mainHD.f90's t, dt, it) and the ticket of
+// the single-pass CFL reduction.
+struct Clock {
+  double t;          // simulated time
+  double dt;         // dt of the next step (time_step's result)
+  double dt_used;    // dt of the last completed step
+  double tfin;       // steps start only while t < tfin
+  long long it;      // iterations
+  unsigned int ticket;
+  int status;
+};
+
+// Structure-of-arrays mesh layout: 5 planes of px * nyg * nzg doubles (x
+// fastest), cell (i, j, k) with i in -1..nx+2 at x index i+1.  px is a
+// multiple of 8 so that every row starts on a 64-byte boundary.
+struct Layout {
+  int px, nyg, nzg;
+  long long plane;
+  __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
+    return (long long)(i + 1) + (long long)px * ((long long)(j + 1) + (long long)nyg * (long long)(k + 1));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// mbarrier / TMA helpers (inline PTX, sm_90+ forms valid on sm_103a).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after `limit` polls (each poll may suspend the
+// thread for a short, hardware-chosen time).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
+  for (long long n = 0; n < limit; ++n)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// 4-D tiled bulk tensor load global -> shared, completing on `bar`.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// L1-bypassing load for values another block wrote in this launch.
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+
+// ---------------------------------------------------------------------------
+// Single-pass CFL reduction (time_step, source/HydroCore.f90:138-150):
+// warp shuffles -> shared memory -> one partial per block -> a ticket; the
+// last block to arrive reduces the partials and writes dt (and advances t,
+// it when `advance` is set, as `step` does at HydroCore.f90:208-209).
+// No block ever waits for another.  `partials` holds 3 doubles per block.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_max_nan(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max_nan(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <int NTHREADS>
+__device__ __forceinline__ void block_max3(double& a, double& b, double& c, double* red /*3*32*/) {
+  a = warp_max_nan(a);
+  b = warp_max_nan(b);
+  c = warp_max_nan(c);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = NTHREADS / 32;
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = a;
+    red[32 + warp] = b;
+    red[64 + warp] = c;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < NW ? red[lane] : 0.0;
+    b = lane < NW ? red[32 + lane] : 0.0;
+    c = lane < NW ? red[64 + lane] : 0.0;
+    a = warp_max_nan(a);
+    b = warp_max_nan(b);
+    c = warp_max_nan(c);
+  }
+}
+
+template <int NTHREADS>
+__device__ void cfl_reduce_finalize(double a, double b, double c, double* partials, Clock* clk, const Params& p,
+                                    bool advance, double* red, int* s_flag) {
+  const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  block_max3<NTHREADS>(a, b, c, red);
+  if (threadIdx.x == 0) {
+    partials[3 * bid + 0] = a;
+    partials[3 * bid + 1] = b;
+    partials[3 * bid + 2] = c;
+    __threadfence();
+    const unsigned t = atomicAdd(&clk->ticket, 1u);
+    *s_flag = (t == nblocks - 1);
+  }
+  __syncthreads();
+  if (!*s_flag) return;
+  __threadfence();
+  a = b = c = 0.0;
+  for (unsigned q = threadIdx.x; q < nblocks; q += NTHREADS) {
+    a = max_nan(a, ld_cg(partials + 3 * q + 0));
+    b = max_nan(b, ld_cg(partials + 3 * q + 1));
+    c = max_nan(c, ld_cg(partials + 3 * q + 2));
+  }
+  block_max3<NTHREADS>(a, b, c, red);
+  if (threadIdx.x == 0) {
+    const double dtn = cfl_dt(p.cfl, p.dx, p.dy, p.dz, a, b, c);
+    if (advance) {
+      clk->t = clk->t + clk->dt;
+      clk->it = clk->it + 1;
+      clk->dt_used = clk->dt;
+    }
+    clk->dt = dtn;
+    if (!(dtn > 0.0) || dtn != dtn || dtn > 1.0e300) atomicOr(&clk->status, ST_NONFINITE_DT);
+    clk->ticket = 0u;
+    __threadfence();
+  }
+}
+
+}  // namespace tlq

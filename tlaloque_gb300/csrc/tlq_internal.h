@@ -1,0 +1,76 @@
+// tlq_internal.h -- launchers shared between the kernel translation units and
+// the host API (tlq_api.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "tlq_stage.cuh"
+
+namespace tlq {
+
+// Reference layout A(5, -1:nx+2, -1:ny+2, -1:nz+2), variable fastest.
+struct Aos {
+  int nx, ny, nz;
+  __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
+    return 5LL * ((long long)(i + 1) + (long long)(nx + 4) * ((long long)(j + 1) + (long long)(ny + 4) * (long long)(k + 1)));
+  }
+  __host__ __device__ __forceinline__ long long cells() const {
+    return (long long)(nx + 4) * (long long)(ny + 4) * (long long)(nz + 4);
+  }
+};
+
+// Potential phi(0:nx+1, 0:ny+1, 0:nz+1) of the reference (pointsource_gravity.f90:14).
+struct PhiLayout {
+  int nx, ny, nz;
+  __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
+    return (long long)i + (long long)(nx + 2) * ((long long)j + (long long)(ny + 2) * (long long)k);
+  }
+};
+
+constexpr int RED_THREADS = 256;  // block size of the reduction kernels
+
+// Fused step (FP64 instantiations in tlq_kernels.cu).
+cudaError_t prepare_stage_kernels();
+size_t stage_smem_bytes(int precision);
+cudaError_t launch_stage(int stage, int precision, const CUtensorMap& tm_in, const CUtensorMap& tm_p,
+                         const StageArgs& a, dim3 grid, cudaStream_t s);
+
+// Layout conversions and per-step helpers (SoA device state).
+cudaError_t launch_aos_to_soa(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_soa_to_aos(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_prims_soa_to_aos(const Params& p, const Aos& A, const Layout& L, const double* U,
+                                    const double* P, double* W, cudaStream_t s);
+// calc_prims + time_step on the uploaded state; writes P (interior pressure)
+// when P is non-null; clk->dt receives the first dt.  `grid_blocks` returns
+// the number of partials used.
+cudaError_t launch_init_prims_dt(const Params& p, const Layout& L, const double* U, double* P, Clock* clk,
+                                 double* partials, int nblocks, cudaStream_t s);
+int init_blocks(const Params& p);
+cudaError_t launch_point_potential_soa(const Params& p, const Layout& L, const double* xyzm, int n, double* phi,
+                                       cudaStream_t s);
+cudaError_t launch_conserved_sums(const Params& p, const Layout& L, const double* U, double* partials, int nblocks,
+                                  double* out5, cudaStream_t s);
+
+// log10 of a small device array in place (cooling-table temperatures).
+cudaError_t launch_log10_inplace(double* v, int n, cudaStream_t s);
+
+// Per-routine kernels on the reference layout.
+cudaError_t launch_calc_prims_aos(const Params& p, const Aos& A, double* W, const double* U, cudaStream_t s);
+cudaError_t launch_time_step_aos(const Params& p, const Aos& A, const double* W, Clock* clk, double* partials,
+                                 int nblocks, cudaStream_t s);
+cudaError_t launch_fluxes_aos(const Params& p, const Aos& A, const double* U, const double* W, double* F, double* G,
+                              double* H, int choice, cudaStream_t s);
+cudaError_t launch_godunov_aos(const Params& p, const Aos& A, double* out, const double* UU, const double* F,
+                               const double* G, const double* H, const double* W, const double* phi, double dt,
+                               cudaStream_t s);
+cudaError_t launch_borders_aos(const Params& p, const Aos& A, double* U, int order, cudaStream_t s);
+cudaError_t launch_winds_aos(const Params& p, const Aos& A, double* U, cudaStream_t s);
+cudaError_t launch_viscous_step_aos(const Params& p, const Aos& A, double* U, const double* UP, const double* Uold,
+                                    cudaStream_t s);
+cudaError_t launch_cooling_aos(const Params& p, const Aos& A, double* W, double* U, double dt, cudaStream_t s);
+cudaError_t launch_point_potential_ref(const Params& p, const double* xyzm, int n, double* phi, cudaStream_t s);
+cudaError_t launch_gravity_source_aos(const Params& p, const Aos& A, const double* W, const double* phi, double* S,
+                                      cudaStream_t s);
+
+}  // namespace tlq

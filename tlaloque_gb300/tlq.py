@@ -1,0 +1,362 @@
+"""ctypes binding of libtlq (the C ABI in include/tlq.h).
+
+This is the Python face of the drop-in: the same entry points a Fortran host
+binds through ISO_C_BINDING.  Host arrays are numpy float64 arrays in the
+reference layout ``A(1:5, -1:nx+2, -1:ny+2, -1:nz+2)`` (Fortran order).
+There is no CPU fallback: without the built library every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libtlq.so")
+
+OK, ERR_CUDA, ERR_CONFIG, ERR_NONFINITE_DT, ERR_NEG_DENSITY, ERR_TIMEOUT, ERR_ARG, ERR_STATE, ERR_NOMEM = range(9)
+BC_OUTFLOW, BC_REFLECTIVE, BC_PERIODIC, BC_INFLOW = 1, 2, 3, 4
+LIMITER_NONE, LIMITER_VANLEER, LIMITER_MINMOD, LIMITER_UMIST, LIMITER_WOODWARD, LIMITER_SUPERBEE = 1, 2, 3, 4, 5, 6
+SOLVER_HLLC, SOLVER_HLL = 0, 1
+COOL_NONE, COOL_REF, COOL_SUBCYCLE = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+
+# Every function the header declares (checked by the CPU test suite).
+EXPORTS = (
+    "tlq_config_default", "tlq_create", "tlq_destroy", "tlq_set_stream", "tlq_set_cooling_table", "tlq_set_winds",
+    "tlq_set_point_masses", "tlq_upload", "tlq_download", "tlq_set_time", "tlq_get_time", "tlq_step", "tlq_advance",
+    "tlq_run_until", "tlq_synchronize", "tlq_stats_get", "tlq_enable_timing", "tlq_last_error", "tlq_status_string",
+    "tlq_conserved_sums", "tlq_calc_prims", "tlq_time_step", "tlq_fluxes", "tlq_godunov", "tlq_borders",
+    "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source",
+)
+
+
+class TlqError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tlq error {code}: {msg}")
+        self.code = code
+
+
+class CConfig(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("xl", C.c_double), ("xr", C.c_double), ("yl", C.c_double), ("yr", C.c_double),
+        ("zl", C.c_double), ("zr", C.c_double),
+        ("gamma", C.c_double), ("cfl", C.c_double), ("eta", C.c_double), ("mu0", C.c_double),
+        ("cooling_limit", C.c_double),
+        ("limiter", C.c_int), ("solver", C.c_int), ("bc", C.c_int * 6), ("cooling", C.c_int),
+        ("cool_max_sub", C.c_int), ("cool_sub_frac", C.c_double), ("precision", C.c_int), ("device", C.c_int),
+    ]
+
+
+class CWind(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("xc", "yc", "zc", "vx", "vy", "vz", "radius", "mdot", "vinf", "temp", "mu")]
+
+
+class CStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_longlong), ("t", C.c_double), ("dt", C.c_double), ("status", C.c_int), ("graph", C.c_int),
+        ("ms_stage1", C.c_double), ("ms_stage2", C.c_double), ("timed", C.c_longlong), ("bytes_state", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libtlq.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libtlq.so is not built ({path}); run __graft_entry__.build()")
+    L = C.CDLL(path)
+    D = C.POINTER(C.c_double)
+    V = C.c_void_p
+    I = C.c_int
+    sig = {
+        "tlq_config_default": (None, [C.POINTER(CConfig)]),
+        "tlq_create": (I, [C.POINTER(CConfig), C.POINTER(V)]),
+        "tlq_destroy": (I, [V]),
+        "tlq_set_stream": (I, [V, V]),
+        "tlq_set_cooling_table": (I, [V, D, D, I]),
+        "tlq_set_winds": (I, [V, C.POINTER(CWind), I]),
+        "tlq_set_point_masses": (I, [V, D, I]),
+        "tlq_upload": (I, [V, D]),
+        "tlq_download": (I, [V, D, D]),
+        "tlq_set_time": (I, [V, C.c_double, I]),
+        "tlq_get_time": (I, [V, D, C.POINTER(I), D]),
+        "tlq_step": (I, [V, D, C.POINTER(I), D]),
+        "tlq_advance": (I, [V, I]),
+        "tlq_run_until": (I, [V, C.c_double, I, D, C.POINTER(I), D]),
+        "tlq_synchronize": (I, [V]),
+        "tlq_stats_get": (I, [V, C.POINTER(CStats)]),
+        "tlq_enable_timing": (I, [V, I]),
+        "tlq_last_error": (C.c_char_p, [V]),
+        "tlq_status_string": (C.c_char_p, [I]),
+        "tlq_conserved_sums": (I, [V, D]),
+        "tlq_calc_prims": (I, [V, D, D]),
+        "tlq_time_step": (I, [V, D, D]),
+        "tlq_fluxes": (I, [V, D, D, D, D, D, I]),
+        "tlq_godunov": (I, [V, D, D, D, D, D, D, C.c_double]),
+        "tlq_borders": (I, [V, D, I]),
+        "tlq_viscous_step": (I, [V, D, D, D, C.POINTER(I), C.c_double]),
+        "tlq_cooling": (I, [V, D, D, C.c_double]),
+        "tlq_point_potential": (I, [V, D]),
+        "tlq_gravity_source": (I, [V, D, D, D]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _dp(a):
+    if a is None:
+        return None
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and (a.flags.f_contiguous or a.flags.c_contiguous)):
+        raise TypeError("expected a contiguous float64 numpy array")
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+@dataclass
+class Wind:
+    """tlq_wind / spherical_wind_type (source/winds.f90:5-16)."""
+    xc: float = 0.0
+    yc: float = 0.0
+    zc: float = 0.0
+    vx: float = 0.0
+    vy: float = 0.0
+    vz: float = 0.0
+    radius: float = 0.0
+    mdot: float = 0.0
+    vinf: float = 0.0
+    temp: float = 1.0e4
+    mu: float = 1.0
+
+
+@dataclass
+class Config:
+    """tlq_config: the runtime image of user/parameters.f90 (its defaults)."""
+    nx: int = 50
+    ny: int = 50
+    nz: int = 50
+    xl: float = -1.0
+    xr: float = 1.0
+    yl: float = -1.0
+    yr: float = 1.0
+    zl: float = -1.0
+    zr: float = 1.0
+    gamma: float = 5.0 / 3.0
+    cfl: float = 0.4
+    eta: float = 0.5e-2
+    mu0: float = 1.0
+    cooling_limit: float = 0.5
+    limiter: int = LIMITER_VANLEER
+    solver: int = SOLVER_HLLC
+    bc: tuple = (BC_REFLECTIVE,) * 6
+    cooling: int = COOL_NONE
+    cool_max_sub: int = 1
+    cool_sub_frac: float = 0.1
+    precision: int = PREC_FP64
+    device: int = 0
+    # run-time tables (not part of tlq_config; set through their own calls)
+    cool_T: np.ndarray | None = None
+    cool_logL: np.ndarray | None = None
+    winds: list = field(default_factory=list)
+    masses: np.ndarray | None = None  # (n, 4): x, y, z, M
+
+    @property
+    def shape(self):
+        return (5, self.nx + 4, self.ny + 4, self.nz + 4)
+
+    @property
+    def phi_shape(self):
+        return (self.nx + 2, self.ny + 2, self.nz + 2)
+
+    @property
+    def dx(self):
+        return (self.xr - self.xl) / self.nx
+
+    @property
+    def dy(self):
+        return (self.yr - self.yl) / self.ny
+
+    @property
+    def dz(self):
+        return (self.zr - self.zl) / self.nz
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def zeros(self) -> np.ndarray:
+        return np.zeros(self.shape, dtype=np.float64, order="F")
+
+    def to_c(self) -> CConfig:
+        c = CConfig()
+        for n in ("nx", "ny", "nz", "limiter", "solver", "cooling", "cool_max_sub", "precision", "device"):
+            setattr(c, n, int(getattr(self, n)))
+        for n in ("xl", "xr", "yl", "yr", "zl", "zr", "gamma", "cfl", "eta", "mu0", "cooling_limit", "cool_sub_frac"):
+            setattr(c, n, float(getattr(self, n)))
+        for q in range(6):
+            c.bc[q] = int(self.bc[q])
+        return c
+
+
+class Context:
+    """One tlq_ctx: the whole mesh resident on one GPU."""
+
+    def __init__(self, cfg: Config):
+        self.L = load_library()
+        self.cfg = cfg
+        h = C.c_void_p()
+        cc = cfg.to_c()
+        rc = self.L.tlq_create(C.byref(cc), C.byref(h))
+        if rc != OK:
+            raise TlqError(rc, f"tlq_create: {self.L.tlq_status_string(rc).decode()}")
+        self.h = h
+        if cfg.cool_T is not None:
+            T = np.ascontiguousarray(cfg.cool_T, dtype=np.float64)
+            Lm = np.ascontiguousarray(cfg.cool_logL, dtype=np.float64)
+            self._check(self.L.tlq_set_cooling_table(self.h, _dp(T), _dp(Lm), len(T)), "set_cooling_table")
+        if cfg.winds:
+            arr = (CWind * len(cfg.winds))()
+            for q, w in enumerate(cfg.winds):
+                for n, _ in CWind._fields_:
+                    setattr(arr[q], n, float(getattr(w, n)))
+            self._check(self.L.tlq_set_winds(self.h, arr, len(cfg.winds)), "set_winds")
+        if cfg.masses is not None and len(cfg.masses):
+            m = np.ascontiguousarray(cfg.masses, dtype=np.float64).reshape(-1, 4)
+            self._check(self.L.tlq_set_point_masses(self.h, _dp(m), m.shape[0]), "set_point_masses")
+
+    # -- plumbing ------------------------------------------------------------
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            msg = self.L.tlq_last_error(self.h).decode() if self.h else ""
+            raise TlqError(rc, f"{what}: {self.L.tlq_status_string(rc).decode()} {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tlq_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- run -----------------------------------------------------------------
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.L.tlq_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
+
+    def upload(self, U: np.ndarray):
+        assert U.shape == self.cfg.shape
+        self._check(self.L.tlq_upload(self.h, _dp(U)), "upload")
+
+    def download(self, U: np.ndarray | None = None, W: np.ndarray | None = None):
+        self._check(self.L.tlq_download(self.h, _dp(U), _dp(W)), "download")
+        return U, W
+
+    def state(self):
+        U = self.cfg.zeros()
+        W = self.cfg.zeros()
+        self.download(U, W)
+        return U, W
+
+    def set_time(self, t: float, it: int = 0):
+        self._check(self.L.tlq_set_time(self.h, float(t), int(it)), "set_time")
+
+    def time(self):
+        t, dt, it = C.c_double(), C.c_double(), C.c_int()
+        rc = self.L.tlq_get_time(self.h, C.byref(t), C.byref(it), C.byref(dt))
+        return t.value, it.value, dt.value, rc
+
+    def step(self, check: bool = True):
+        t, dt, it = C.c_double(), C.c_double(), C.c_int()
+        rc = self.L.tlq_step(self.h, C.byref(t), C.byref(it), C.byref(dt))
+        if check:
+            self._check(rc, "step")
+        return t.value, it.value, dt.value
+
+    def advance(self, n: int):
+        self._check(self.L.tlq_advance(self.h, int(n)), "advance")
+
+    def run_until(self, tfin: float, max_steps: int = 1 << 30):
+        t, dt, it = C.c_double(), C.c_double(), C.c_int()
+        self._check(self.L.tlq_run_until(self.h, float(tfin), int(max_steps), C.byref(t), C.byref(it), C.byref(dt)),
+                    "run_until")
+        return t.value, it.value, dt.value
+
+    def synchronize(self):
+        self._check(self.L.tlq_synchronize(self.h), "synchronize")
+
+    def enable_timing(self, on: bool = True):
+        self._check(self.L.tlq_enable_timing(self.h, int(bool(on))), "enable_timing")
+
+    def stats(self) -> CStats:
+        s = CStats()
+        self._check(self.L.tlq_stats_get(self.h, C.byref(s)), "stats")
+        return s
+
+    def conserved_sums(self) -> np.ndarray:
+        out = np.zeros(5)
+        self._check(self.L.tlq_conserved_sums(self.h, _dp(out)), "conserved_sums")
+        return out
+
+    # -- per-routine entry points ----------------------------------------------
+    def calc_prims(self, U):
+        W = self.cfg.zeros()
+        self._check(self.L.tlq_calc_prims(self.h, _dp(W), _dp(U)), "calc_prims")
+        return W
+
+    def time_step(self, W) -> float:
+        dt = C.c_double()
+        self._check(self.L.tlq_time_step(self.h, _dp(W), C.byref(dt)), "time_step")
+        return dt.value
+
+    def fluxes(self, U, W, choice, F=None, G=None, H=None):
+        F = self.cfg.zeros() if F is None else F
+        G = self.cfg.zeros() if G is None else G
+        H = self.cfg.zeros() if H is None else H
+        self._check(self.L.tlq_fluxes(self.h, _dp(U), _dp(F), _dp(G), _dp(H), _dp(W), int(choice)), "fluxes")
+        return F, G, H
+
+    def godunov(self, UU, F, G, H, dt, W=None, out=None):
+        out = self.cfg.zeros() if out is None else out
+        self._check(self.L.tlq_godunov(self.h, _dp(out), _dp(UU), _dp(F), _dp(G), _dp(H), _dp(W), float(dt)), "godunov")
+        return out
+
+    def borders(self, U, order):
+        self._check(self.L.tlq_borders(self.h, _dp(U), int(order)), "borders")
+        return U
+
+    def viscous_step(self, U, UP, t, it, dt):
+        tt, ii = C.c_double(t), C.c_int(it)
+        self._check(self.L.tlq_viscous_step(self.h, _dp(U), _dp(UP), C.byref(tt), C.byref(ii), float(dt)),
+                    "viscous_step")
+        return tt.value, ii.value
+
+    def cooling(self, W, U, dt):
+        self._check(self.L.tlq_cooling(self.h, _dp(W), _dp(U), float(dt)), "cooling")
+
+    def point_potential(self, phi=None):
+        phi = np.zeros(self.cfg.phi_shape, order="F") if phi is None else phi
+        self._check(self.L.tlq_point_potential(self.h, _dp(phi)), "point_potential")
+        return phi
+
+    def gravity_source(self, W, phi):
+        S = self.cfg.zeros()
+        self._check(self.L.tlq_gravity_source(self.h, _dp(W), _dp(phi), _dp(S)), "gravity_source")
+        return S
