@@ -1,0 +1,334 @@
+"""Benchmark of tlaloque's hydrodynamic step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tlq|reference]
+                    [--workload wind256|sedov128|sod] [--precision fp64]
+
+A "step" is one full iteration of the reference's main loop
+(source/mainHD.f90:74-99: CFL dt, two HLLC stages, ghost fill, winds, point
+gravity, artificial viscosity, cooling) over the whole mesh.  The metric is
+zone-updates/s = interior cells x steps / time.
+
+* value      device-resident: K steps through the C ABI (tlq_advance with
+             per-kernel CUDA events) with the state already in HBM, timed
+             with CUDA events on the library's stream;
+* e2e        the same metric end to end through the C ABI with host
+             buffers: per step tlq_upload (pinned host -> device + layout
+             conversion + calc_prims/dt), tlq_step, tlq_download;
+* roofline   the dominant kernel's algorithmic bytes per launch / its
+             average CUDA-event duration, against the measured HBM peak;
+* cpu_baseline  the oracle restatement on the host cores (bounded sample).
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement: the Fortran reference has no compiler on this pool) on
+all host cores, same workload and metric.  With N > 1 ranks (torchrun) each
+rank advances an independent replica of the workload (the step has no data
+path shared between meshes); value = all ranks' zone-updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "zone-updates/s on 1 GB300 at 256³ (mixed+surrogate vs plain FP64 at ≤1% L1 err); HBM GB/s"
+UNIT = "zone-updates/s"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def make_workload(name: str):
+    from tlaloque_gb300 import problems, tlq
+    if name == "wind256":
+        cfg, U0 = problems.wind_bubble(256)
+        desc = ("radiative wind-blown bubble 256^3, (8 pc)^3 box, HLLC + van Leer, spherical wind (R = 4 dx, "
+                "1e-6 Msun/yr, 2000 km/s), 10 Msun point mass, sub-cycled tabulated cooling, outflow")
+    elif name == "wind128":
+        cfg, U0 = problems.wind_bubble(128)
+        desc = "radiative wind-blown bubble 128^3 (the 256^3 workload at half resolution)"
+    elif name == "sedov128":
+        cfg, U0 = problems.sedov(128)
+        desc = "3-D Sedov-Taylor blast 128^3, HLLC + van Leer, outflow"
+    elif name == "sod":
+        cfg, U0 = problems.sod_tube()
+        desc = "Sod shock tube 256x4x4, HLL, gamma 1.4, outflow"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return cfg, U0, desc
+
+
+def bytes_per_zone(cfg) -> dict:
+    """Algorithmic HBM bytes per zone-update of each stage kernel (FP64 state:
+    5 conserved variables x 8 B; cooling carries the cooled interior pressure
+    (8 B written by stage 2, read by stage 1); point gravity reads phi once
+    per stage)."""
+    from tlaloque_gb300 import tlq
+    cool = cfg.cooling != tlq.COOL_NONE
+    grav = cfg.masses is not None and len(cfg.masses) > 0
+    s1 = 40 + 40 + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
+    s2 = 40 + 40 + 40 + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
+    return {"stage1": s1, "stage2": s2, "step": s1 + s2}
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for s in self.samples for q in range(4) if s[5 + q].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_oracle_rate(cfg, U0, budget_s: float, nthreads: int, min_steps: int = 2, max_steps: int = 10 ** 6):
+    """Time the oracle restatement on the host: zone-updates/s over a bounded
+    number of steps of the same workload (steps until budget_s elapses)."""
+    from oracle.oracle import Run
+    from tests.helpers import oracle_params
+    run = Run(oracle_params(cfg, nthreads=nthreads), U0)
+    run.run(1)  # first touch of the arrays
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps:
+        run.run(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if steps >= min_steps and el >= budget_s:
+            break
+    el = time.perf_counter() - t0
+    return cfg.cells * steps / el, steps, el
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local, dist
+
+
+def allmax(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_reference(args, world, rank, dist):
+    """The reference algorithm on the host cores (oracle restatement)."""
+    if rank != 0:
+        return
+    cfg, U0, desc = make_workload(args.workload)
+    ncores = os.cpu_count() or 1
+    from oracle.oracle import Run
+    from tests.helpers import oracle_params
+    run = Run(oracle_params(cfg, nthreads=ncores), U0)
+    run.run(args.warmup)
+    t0 = time.perf_counter()
+    run.run(args.steps)
+    el = time.perf_counter() - t0
+    value = cfg.cells * args.steps / el
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "mesh": [cfg.nx, cfg.ny, cfg.nz], "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                         "sample": f"{args.steps} full steps of the workload after {args.warmup} warm-up steps "
+                                   f"(oracle restatement, OpenMP over {ncores} host threads; the Fortran reference "
+                                   "cannot be compiled on this pool: no Fortran compiler)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tlq", choices=["tlq", "reference"])
+    ap.add_argument("--workload", default="wind256")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        barrier(dist)
+        return
+
+    import torch
+    from tlaloque_gb300 import build as tbuild
+    from tlaloque_gb300 import tlq
+    tbuild.build()
+    torch.cuda.set_device(local)
+    cfg, U0, desc = make_workload(args.workload)
+    cfg.device = local
+    peak, peak_kind = load_peaks()
+    bpz = bytes_per_zone(cfg)
+
+    stream = torch.cuda.Stream()
+    ctx = tlq.Context(cfg)
+    ctx.set_stream(stream.cuda_stream)
+    U1 = U0.copy(order="F")
+    ctx.borders(U1, 1)          # mainHD.f90:38
+    ctx.upload(U1)
+    ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
+    ctx.synchronize()
+
+    # ---- device-resident timed region -------------------------------------
+    sampler = ClockSampler(local)
+    sampler.start()
+    ctx.enable_timing(True)
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        ctx.advance(args.steps)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    st = ctx.stats()
+    ctx.enable_timing(False)
+    t_sim, it_sim, dt_sim, status = ctx.time()
+    ms_max = allmax(dist, ms)
+    value = world * cfg.cells * args.steps / (ms_max / 1e3)
+
+    k1, k2 = st.ms_stage1, st.ms_stage2
+    dom = "stage2" if k2 >= k1 else "stage1"
+    kms = max(k1, k2)
+    achieved = bpz[dom] * cfg.cells / (kms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": f"stage_kernel<{2 if dom == 'stage2' else 1}, double>",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "traffic": None, "bytes_per_zone": bpz, "ms_stage1": k1, "ms_stage2": k2,
+                "note": "plain FP64 is FP64-pipe bound on GB300 (see fp64 block), not HBM bound"}
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tr = json.load(f).get(args.workload, {}).get(dom)
+            if tr:
+                roofline["traffic"] = tr["bytes_per_launch"] * cfg.cells / tr["cells"]
+    except Exception:
+        pass
+
+    # ---- end to end through the C ABI with pinned host buffers -------------
+    host = torch.empty((cfg.nz + 4, cfg.ny + 4, cfg.nx + 4, 5), dtype=torch.float64, pin_memory=True)
+    Uh = host.numpy().transpose(3, 2, 1, 0)
+    ctx.download(Uh, None)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        ctx.upload(Uh)
+        ctx.step()
+        ctx.download(Uh, None)
+    el = time.perf_counter() - t0
+    barrier(dist)
+    el = allmax(dist, el)
+    e2e = {"value": world * cfg.cells * args.e2e_steps / el, "unit": UNIT,
+           "h2d_bytes_per_step": int(Uh.nbytes), "d2h_bytes_per_step": int(Uh.nbytes),
+           "ms_per_step": 1e3 * el / args.e2e_steps,
+           "path": "tlq_upload(pinned host U) + tlq_step + tlq_download(U) per step"}
+    ctx.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "mesh": [cfg.nx, cfg.ny, cfg.nz], "form": "plain FP64 (bit-identical to the "
+                   "reference arithmetic)", "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (each state array 0.7 GB; 3 arrays touched per step)",
+                   "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status}},
+        "e2e": e2e, "roofline": roofline, "clocks": clocks, "gpu_launches": 2 * args.steps,
+        "hbm_gbs_step": bpz["step"] * cfg.cells * args.steps / (ms_max / 1e3) / 1e9,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        ncores = os.cpu_count() or 1
+        rate, steps, secs = cpu_oracle_rate(cfg, U0, args.cpu_budget, ncores)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port",
+                                "sample": f"{steps} full steps of the same workload ({secs:.1f} s) on the oracle "
+                                          f"restatement, OpenMP over {ncores} host threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
