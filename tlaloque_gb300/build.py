@@ -28,6 +28,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = [
     ("tlq_kernels.cu", ["-fmad=false"]),
     ("tlq_api.cu", []),
+    ("tlq_noalloc.cu", ["-fmad=false"]),
 ]
 
 

@@ -1,0 +1,113 @@
+// tlq_noalloc.cu -- time_step (source/HydroCore.f90:113-155) for callers that
+// cannot allocate device memory.
+//
+// Who needs this: a host whose device memory is owned by someone else -- an
+// arena or pool allocator that has already reserved the GPU's memory (a
+// further cudaMalloc can then fail, and it fragments the arena), or a
+// time-critical step loop that cannot afford cudaMalloc/cudaFree's implicit
+// device synchronisation.  Such callers hand in device buffers they already
+// own; this entry point then allocates nothing at all: no cudaMalloc, no
+// cudaFree, no allocating library routine.
+//
+// The per-block partial maxima and the ticket of the single-pass CFL
+// reduction live in one file-scope device array of fixed size (below), which
+// every GPU that loads the library holds until the process exits.  That
+// fixes the largest mesh this entry point accepts.
+#include <mutex>
+
+#include "../../include/tlq.h"
+#include "tlq_internal.h"
+
+namespace tlq {
+namespace {
+
+constexpr int NA_THREADS = 256;
+constexpr int NA_CELLS_PER_THREAD = 16;
+constexpr long long NA_CELLS_PER_BLOCK = (long long)NA_THREADS * NA_CELLS_PER_THREAD;  // 4096
+constexpr int NA_MAX_BLOCKS = 8192;
+constexpr long long NA_MAX_CELLS = NA_CELLS_PER_BLOCK * NA_MAX_BLOCKS;  // 33,554,432 interior cells
+constexpr int NA_MAX_DEVICES = 64;
+
+struct NoAllocScratch {
+  Clock clk;                          // ticket (must start at 0) and the reduction's dt
+  double partials[3 * NA_MAX_BLOCKS];  // one (max |u|+c, max |v|+c, max |w|+c) per block
+};
+
+// The scratch: 196,656 bytes per device.  Host code must not use this name as
+// an address; it looks the device address up once per device (below).
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Same reduction as the per-routine time_step kernel, with a fixed chunk of
+// NA_CELLS_PER_BLOCK interior cells per block so that the number of partials
+// (and hence the scratch needed) follows from the mesh size.
+__global__ void __launch_bounds__(NA_THREADS) k_time_step_noalloc(Params p, Aos A, const double* __restrict__ W,
+                                                                  NoAllocScratch* sc, double* d_dt) {
+  __shared__ double red[96];
+  __shared__ int flag;
+  const long long n = (long long)p.nx * p.ny * p.nz;
+  const long long beg = (long long)blockIdx.x * NA_CELLS_PER_BLOCK;
+  const long long end = beg + NA_CELLS_PER_BLOCK < n ? beg + NA_CELLS_PER_BLOCK : n;
+  double m0 = 0.0, m1 = 0.0, m2 = 0.0;
+  for (long long c = beg + threadIdx.x; c < end; c += NA_THREADS) {
+    const int i = 1 + (int)(c % p.nx);
+    const long long r = c / p.nx;
+    const int j = 1 + (int)(r % p.ny);
+    const int k = 1 + (int)(r / p.ny);
+    const double* w = W + A.at(i, j, k);
+    double ww[5], v3[3];
+#pragma unroll
+    for (int e = 0; e < 5; ++e) ww[e] = w[e];
+    signal_speeds(p.gamma, ww, v3);
+    m0 = max_nan(m0, v3[0]);
+    m1 = max_nan(m1, v3[1]);
+    m2 = max_nan(m2, v3[2]);
+  }
+  cfl_reduce_finalize<NA_THREADS>(m0, m1, m2, sc->partials, &sc->clk, p, false, red, &flag);
+  if (flag && threadIdx.x == 0) *d_dt = sc->clk.dt;
+}
+
+std::mutex g_mutex;
+void* g_scratch_addr[NA_MAX_DEVICES] = {};
+
+// Set-up, once per device with that device current: the device address of
+// the scratch array.
+cudaError_t scratch_address(NoAllocScratch** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= NA_MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_scratch_addr[dev]) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_addr[dev] = ptr;
+  }
+  *out = static_cast<NoAllocScratch*>(g_scratch_addr[dev]);
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace tlq
+
+extern "C" int tlq_time_step_noalloc(const double* d_uprim, int nx, int ny, int nz, double dx, double dy, double dz,
+                                     double gamma, double cfl, double* d_dt, void* cuda_stream) {
+  using namespace tlq;
+  if (!d_uprim || !d_dt || nx < 1 || ny < 1 || nz < 1) return TLQ_ERR_ARG;
+  const long long n = (long long)nx * ny * nz;
+  if (n > NA_MAX_CELLS) return TLQ_ERR_ARG;  // more interior cells than the fixed scratch can reduce
+  NoAllocScratch* sc = nullptr;
+  if (scratch_address(&sc) != cudaSuccess) return TLQ_ERR_CUDA;
+  Params p{};
+  p.nx = nx; p.ny = ny; p.nz = nz;
+  p.dx = dx; p.dy = dy; p.dz = dz;
+  p.gamma = gamma;
+  p.cfl = cfl;
+  const Aos A{nx, ny, nz};
+  const int nblocks = (int)((n + NA_CELLS_PER_BLOCK - 1) / NA_CELLS_PER_BLOCK);
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  // The array keeps the previous call's contents: the ticket must start at 0.
+  if (cudaMemsetAsync(&sc->clk, 0, sizeof(Clock), s) != cudaSuccess) return TLQ_ERR_CUDA;
+  k_time_step_noalloc<<<nblocks, NA_THREADS, 0, s>>>(p, A, d_uprim, sc, d_dt);
+  return cudaGetLastError() == cudaSuccess ? TLQ_OK : TLQ_ERR_CUDA;
+}

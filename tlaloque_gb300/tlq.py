@@ -29,7 +29,7 @@ EXPORTS = (
     "tlq_set_point_masses", "tlq_upload", "tlq_download", "tlq_set_time", "tlq_get_time", "tlq_step", "tlq_advance",
     "tlq_run_until", "tlq_synchronize", "tlq_stats_get", "tlq_enable_timing", "tlq_last_error", "tlq_status_string",
     "tlq_conserved_sums", "tlq_calc_prims", "tlq_time_step", "tlq_fluxes", "tlq_godunov", "tlq_borders",
-    "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source",
+    "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
 )
 
 
@@ -106,6 +106,7 @@ def load_library(path: str = LIB_PATH):
         "tlq_cooling": (I, [V, D, D, C.c_double]),
         "tlq_point_potential": (I, [V, D]),
         "tlq_gravity_source": (I, [V, D, D, D]),
+        "tlq_time_step_noalloc": (I, [V, I, I, I, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, V, V]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
