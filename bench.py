@@ -8,9 +8,12 @@ A "step" is one full iteration of the reference's main loop
 gravity, artificial viscosity, cooling) over the whole mesh.  The metric is
 zone-updates/s = interior cells x steps / time.
 
-* value      device-resident: K steps through the C ABI (tlq_advance with
-             per-kernel CUDA events) with the state already in HBM, timed
-             with CUDA events on the library's stream;
+* value      device-resident, headline (mixed-precision) form: K steps
+             through the C ABI (tlq_advance with per-kernel CUDA events) with
+             the state already in HBM, timed with CUDA events on the
+             library's stream; `forms` holds the plain FP64 form measured the
+             same way, the speed-up, and the mixed form's relative L1 density
+             error and total-energy drift against FP64 after W+K steps;
 * e2e        the same metric end to end through the C ABI with host
              buffers: per step tlq_upload (pinned host -> device + layout
              conversion + calc_prims/dt), tlq_step, tlq_download;
@@ -75,13 +78,13 @@ def make_workload(name: str):
     return cfg, U0, desc
 
 
-def bytes_per_zone(cfg) -> dict:
+def bytes_per_zone(cfg, mixed: bool = False) -> dict:
     """Algorithmic HBM bytes per zone-update of each stage kernel (FP64 state:
-    5 conserved variables x 8 B; cooling carries the cooled interior pressure
-    (8 B written by stage 2, read by stage 1); point gravity reads phi once
-    per stage)."""
+    5 conserved variables x 8 B; the plain form carries the cooled interior
+    pressure (8 B written by stage 2, read by stage 1; the mixed form
+    recomputes it); point gravity reads phi once per stage)."""
     from tlaloque_gb300 import tlq
-    cool = cfg.cooling != tlq.COOL_NONE
+    cool = cfg.cooling != tlq.COOL_NONE and not mixed
     grav = cfg.masses is not None and len(cfg.masses) > 0
     s1 = 40 + 40 + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
     s2 = 40 + 40 + 40 + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
@@ -238,55 +241,80 @@ def main():
     cfg.device = local
     peak, peak_kind = load_peaks()
     bpz = bytes_per_zone(cfg)
-
     stream = torch.cuda.Stream()
-    ctx = tlq.Context(cfg)
-    ctx.set_stream(stream.cuda_stream)
-    U1 = U0.copy(order="F")
-    ctx.borders(U1, 1)          # mainHD.f90:38
-    ctx.upload(U1)
-    ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
-    ctx.synchronize()
+    forms = {}
 
-    # ---- device-resident timed region -------------------------------------
-    sampler = ClockSampler(local)
-    sampler.start()
-    ctx.enable_timing(True)
-    barrier(dist)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        ctx.advance(args.steps)
-        e1.record(stream)
-    torch.cuda.synchronize()
-    barrier(dist)
-    ms = e0.elapsed_time(e1)
-    clocks = sampler.stop()
-    st = ctx.stats()
-    ctx.enable_timing(False)
-    t_sim, it_sim, dt_sim, status = ctx.time()
-    ms_max = allmax(dist, ms)
-    value = world * cfg.cells * args.steps / (ms_max / 1e3)
+    def measure(precision, steps, sample_clocks):
+        """W warm-up + K timed steps of one form from the initial state."""
+        c = tlq.Config(**{**cfg.__dict__, "precision": precision})
+        ctx = tlq.Context(c)
+        ctx.set_stream(stream.cuda_stream)
+        U1 = U0.copy(order="F")
+        ctx.borders(U1, 1)          # mainHD.f90:38
+        ctx.upload(U1)
+        ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
+        ctx.synchronize()
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.start()
+        ctx.enable_timing(True)
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            ctx.advance(steps)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(dist)
+        ms = e0.elapsed_time(e1)
+        clocks = sampler.stop() if sampler else None
+        st = ctx.stats()
+        ctx.enable_timing(False)
+        t_sim, it_sim, dt_sim, status = ctx.time()
+        W = cfg.zeros()
+        ctx.download(None, W)
+        sums = ctx.conserved_sums()
+        ms_max = allmax(dist, ms)
+        return {"ctx": ctx, "ms": ms_max, "value": world * cfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
+                "k2": st.ms_stage2, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
+                "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks}
 
-    k1, k2 = st.ms_stage1, st.ms_stage2
+    f64 = measure(tlq.PREC_FP64, args.steps, False)
+    f64["ctx"].close()
+    mix = measure(tlq.PREC_MIXED, args.steps, True)
+    nst = args.warmup + args.steps
+    l1 = float(np.sum(np.abs(mix["rho"] - f64["rho"])) / np.sum(np.abs(f64["rho"])))
+    drift = abs(mix["E"] - f64["E"]) / abs(f64["E"]) * (100.0 / nst)
+    forms = {"fp64": {"value": f64["value"], "ms_per_step": f64["ms"] / args.steps, "ms_stage1": f64["k1"],
+                      "ms_stage2": f64["k2"]},
+             "mixed": {"value": mix["value"], "ms_per_step": mix["ms"] / args.steps, "ms_stage1": mix["k1"],
+                       "ms_stage2": mix["k2"]},
+             "speedup_mixed_vs_fp64": mix["value"] / f64["value"],
+             "mixed_vs_fp64_after_steps": nst, "l1_rho_rel": l1, "energy_drift_rel_per_100_steps": drift}
+    value = mix["value"]
+    ms_max = mix["ms"]
+
+    k1, k2 = mix["k1"], mix["k2"]
     dom = "stage2" if k2 >= k1 else "stage1"
     kms = max(k1, k2)
-    achieved = bpz[dom] * cfg.cells / (kms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": f"stage_kernel<{2 if dom == 'stage2' else 1}, double>",
+    bpz_m = bytes_per_zone(cfg, mixed=True)
+    achieved = bpz_m[dom] * cfg.cells / (kms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": f"stage_kernel_mixed<{2 if dom == 'stage2' else 1}>",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                "traffic": None, "bytes_per_zone": bpz, "ms_stage1": k1, "ms_stage2": k2,
-                "note": "plain FP64 is FP64-pipe bound on GB300 (see fp64 block), not HBM bound"}
+                "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if peak_kind == "measured"
+                else peak_kind,
+                "traffic": None, "bytes_per_zone": bpz_m, "ms_stage1": k1, "ms_stage2": k2}
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            tr = json.load(f).get(args.workload, {}).get(dom)
+            tr = json.load(f).get(args.workload, {}).get("mixed_" + dom)
             if tr:
                 roofline["traffic"] = tr["bytes_per_launch"] * cfg.cells / tr["cells"]
     except Exception:
         pass
 
     # ---- end to end through the C ABI with pinned host buffers -------------
+    ctx = mix["ctx"]
     host = torch.empty((cfg.nz + 4, cfg.ny + 4, cfg.nx + 4, 5), dtype=torch.float64, pin_memory=True)
     Uh = host.numpy().transpose(3, 2, 1, 0)
     ctx.download(Uh, None)
@@ -303,19 +331,21 @@ def main():
     e2e = {"value": world * cfg.cells * args.e2e_steps / el, "unit": UNIT,
            "h2d_bytes_per_step": int(Uh.nbytes), "d2h_bytes_per_step": int(Uh.nbytes),
            "ms_per_step": 1e3 * el / args.e2e_steps,
-           "path": "tlq_upload(pinned host U) + tlq_step + tlq_download(U) per step"}
+           "path": "tlq_upload(pinned host U) + tlq_step + tlq_download(U) per step, mixed form"}
     ctx.close()
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "mesh": [cfg.nx, cfg.ny, cfg.nz], "form": "plain FP64 (bit-identical to the "
-                   "reference arithmetic)", "parallelism": "replicas" if world > 1 else "single GPU",
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": desc, "mesh": [cfg.nx, cfg.ny, cfg.nz],
+                   "form": "mixed: FP32 reconstruction, Riemann fluxes, sources and cooling; FP64 state, "
+                           "accumulation, high-Mach pressure recovery and dt",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (each state array 0.7 GB; 3 arrays touched per step)",
-                   "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status}},
-        "e2e": e2e, "roofline": roofline, "clocks": clocks, "gpu_launches": 2 * args.steps,
-        "hbm_gbs_step": bpz["step"] * cfg.cells * args.steps / (ms_max / 1e3) / 1e9,
+                   "sim": mix["sim"]},
+        "forms": forms, "e2e": e2e, "roofline": roofline, "clocks": mix["clocks"], "gpu_launches": 2 * args.steps,
+        "hbm_gbs_step": bpz_m["step"] * cfg.cells * args.steps / (ms_max / 1e3) / 1e9,
     }
     if rank == 0 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1

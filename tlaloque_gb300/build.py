@@ -29,6 +29,7 @@ UNITS = [
     ("tlq_kernels.cu", ["-fmad=false"]),
     ("tlq_api.cu", []),
     ("tlq_noalloc.cu", ["-fmad=false"]),
+    ("tlq_mixed.cu", ["--use_fast_math"]),
 ]
 
 

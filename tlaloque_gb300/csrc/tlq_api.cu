@@ -39,6 +39,7 @@ struct tlq_ctx {
   double* staging = nullptr;  // one reference-layout array
   // tables
   double *dT = nullptr, *dlogT = nullptr, *dC = nullptr;
+  float *dTf = nullptr, *dlogTf = nullptr, *dCf = nullptr;
   Wind* dwinds = nullptr;
   double* dmasses = nullptr;
   int nmasses = 0;
@@ -129,7 +130,9 @@ int validate(const tlq_config* c, std::string& why) {
     why = "sub-cycled cooling needs cool_max_sub >= 1 and cool_sub_frac > 0";
     return TLQ_ERR_CONFIG;
   }
-  if (c->precision != TLQ_PREC_FP64) { why = "precision mode not available in this build"; return TLQ_ERR_CONFIG; }
+  if (c->precision != TLQ_PREC_FP64 && c->precision != TLQ_PREC_MIXED) { why = "unknown precision"; return TLQ_ERR_CONFIG; }
+  for (int q = 0; q < 6; ++q)
+    if (c->bc[q] == TLQ_BC_INFLOW) { why = "inflow boundaries are an empty stub in the reference"; return TLQ_ERR_CONFIG; }
   return TLQ_OK;
 }
 
@@ -167,6 +170,12 @@ int ensure_routine_scratch(tlq_ctx* ctx) {
   return TLQ_OK;
 }
 
+// The plain FP64 form carries apply_cooling's UPrim(5) exactly (a plane of
+// interior pressures); the mixed form recomputes the pressure from U.
+bool carries_pressure(const tlq_ctx* c) {
+  return c->cfg.cooling != TLQ_COOL_NONE && c->cfg.precision == TLQ_PREC_FP64;
+}
+
 int status_from_bits(int bits) {
   if (bits & ST_TIMEOUT) return TLQ_ERR_TIMEOUT;
   if (bits & ST_NONFINITE_DT) return TLQ_ERR_NONFINITE_DT;
@@ -187,15 +196,22 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.uold = ctx->U[par];
   a.out = ctx->UPP;
   a.pout = nullptr;
-  a.use_p = ctx->cfg.cooling != TLQ_COOL_NONE;
+  const bool mixed = ctx->cfg.precision == TLQ_PREC_MIXED;
+  a.use_p = (!mixed && ctx->cfg.cooling != TLQ_COOL_NONE) ? 1 : 0;
   if (timed) CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-  CK(launch_stage(1, ctx->cfg.precision, ctx->tm_U[par], ctx->tm_P, a, ctx->grid, ctx->stream));
+  if (mixed)
+    CK(launch_stage_mixed(1, ctx->tm_U[par], a, ctx->grid, ctx->stream));
+  else
+    CK(launch_stage(1, ctx->cfg.precision, ctx->tm_U[par], ctx->tm_P, a, ctx->grid, ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
   // stage 2: UPP (+ U[par]) -> U[par^1]
   a.out = ctx->U[par ^ 1];
   a.pout = ctx->Pc;
   a.use_p = 0;
-  CK(launch_stage(2, ctx->cfg.precision, ctx->tm_UPP, ctx->tm_P, a, ctx->grid, ctx->stream));
+  if (mixed)
+    CK(launch_stage_mixed(2, ctx->tm_UPP, a, ctx->grid, ctx->stream));
+  else
+    CK(launch_stage(2, ctx->cfg.precision, ctx->tm_UPP, ctx->tm_P, a, ctx->grid, ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
   return TLQ_OK;
 }
@@ -339,6 +355,7 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
       cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
     return bail(TLQ_ERR_NOMEM);
   if (prepare_stage_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
+  if (cfg->precision == TLQ_PREC_MIXED && prepare_mixed_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
   int r = make_map(ctx, &ctx->tm_U[0], ctx->U[0], 5);
   if (!r) r = make_map(ctx, &ctx->tm_U[1], ctx->U[1], 5);
   if (!r) r = make_map(ctx, &ctx->tm_UPP, ctx->UPP, 5);
@@ -360,6 +377,7 @@ int tlq_destroy(tlq_ctx* ctx) {
   cudaFree(ctx->clk); cudaFree(ctx->partials); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);
+  cudaFree(ctx->dTf); cudaFree(ctx->dlogTf); cudaFree(ctx->dCf);
   for (int q = 0; q < 6; ++q) cudaFree(ctx->rb[q]);
   cudaFree(ctx->rphi); cudaFree(ctx->rclk); cudaFree(ctx->rpartials);
   if (ctx->clk_host) cudaFreeHost(ctx->clk_host);
@@ -401,7 +419,20 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int
   CK(cudaMemcpy(ctx->dlogT, T, n * sizeof(double), cudaMemcpyHostToDevice));
   CK(launch_log10_inplace(ctx->dlogT, n, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  ctx->P.cool = CoolTable{ctx->dT, ctx->dlogT, ctx->dC, n};
+  // FP32 copies for the mixed-precision step
+  std::vector<double> hlt(n);
+  CK(cudaMemcpy(hlt.data(), ctx->dlogT, n * sizeof(double), cudaMemcpyDeviceToHost));
+  std::vector<float> fT(n), flt(n), fC(n);
+  for (int q = 0; q < n; ++q) { fT[q] = (float)T[q]; flt[q] = (float)hlt[q]; fC[q] = (float)logL[q]; }
+  cudaFree(ctx->dTf); cudaFree(ctx->dlogTf); cudaFree(ctx->dCf);
+  ctx->dTf = ctx->dlogTf = ctx->dCf = nullptr;
+  CK(cudaMalloc(&ctx->dTf, n * sizeof(float)));
+  CK(cudaMalloc(&ctx->dlogTf, n * sizeof(float)));
+  CK(cudaMalloc(&ctx->dCf, n * sizeof(float)));
+  CK(cudaMemcpy(ctx->dTf, fT.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dlogTf, flt.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dCf, fC.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  ctx->P.cool = CoolTable{ctx->dT, ctx->dlogT, ctx->dC, n, ctx->dTf, ctx->dlogTf, ctx->dCf};
   invalidate_graphs(ctx);
   return TLQ_OK;
 }
@@ -481,7 +512,7 @@ int tlq_upload(tlq_ctx* ctx, const double* U) {
   c.tfin = std::numeric_limits<double>::infinity();
   *ctx->clk_host = c;
   CK(cudaMemcpyAsync(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], ctx->cfg.cooling != TLQ_COOL_NONE ? ctx->Pc : nullptr, ctx->clk,
+  CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], carries_pressure(ctx) ? ctx->Pc : nullptr, ctx->clk,
                           ctx->partials, init_blocks(ctx->P), ctx->stream));
   ctx->cur = 0;
   ctx->it_base = ctx->it0;
@@ -501,8 +532,8 @@ int tlq_download(tlq_ctx* ctx, double* U, double* W) {
     CK(cudaMemcpyAsync(U, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
   }
   if (W) {
-    CK(launch_prims_soa_to_aos(ctx->P, ctx->A, ctx->L, ctx->U[ctx->cur],
-                               ctx->cfg.cooling != TLQ_COOL_NONE ? ctx->Pc : nullptr, ctx->staging, ctx->stream));
+    CK(launch_prims_soa_to_aos(ctx->P, ctx->A, ctx->L, ctx->U[ctx->cur], carries_pressure(ctx) ? ctx->Pc : nullptr,
+                               ctx->staging, ctx->stream));
     CK(cudaMemcpyAsync(W, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
   }
   CK(cudaStreamSynchronize(ctx->stream));

@@ -36,6 +36,11 @@ size_t stage_smem_bytes(int precision);
 cudaError_t launch_stage(int stage, int precision, const CUtensorMap& tm_in, const CUtensorMap& tm_p,
                          const StageArgs& a, dim3 grid, cudaStream_t s);
 
+// Mixed-precision stage kernels (tlq_mixed.cu).
+cudaError_t prepare_mixed_kernels();
+size_t mixed_smem_bytes();
+cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageArgs& a, dim3 grid, cudaStream_t s);
+
 // Layout conversions and per-step helpers (SoA device state).
 cudaError_t launch_aos_to_soa(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);

@@ -40,12 +40,16 @@ struct Wind {
   int ilo, ihi, jlo, jhi, klo, khi;
 };
 
-// Cooling table on the device: T (ascending), log10 T, log10 Lambda.
+// Cooling table on the device: T (ascending), log10 T, log10 Lambda, and
+// FP32 copies of the three columns for the mixed-precision step.
 struct CoolTable {
   const double* T;
   const double* logT;
   const double* C;
   int n;
+  const float* Tf;
+  const float* logTf;
+  const float* Cf;
 };
 
 // Static description of the mesh and the physics switches, passed by value.

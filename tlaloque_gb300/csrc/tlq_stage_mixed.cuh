@@ -1,0 +1,379 @@
+// tlq_stage_mixed.cuh -- the mixed-precision form of the two stage kernels.
+//
+// Same step and same fusion as tlq_stage.cuh, with a different split of the
+// arithmetic, chosen for GB300 (FP64 at 1/64 of the FP32 rate):
+//   FP32  primitives, limiter reconstruction, HLL/HLLC fluxes, flux
+//         divergence, gravity source, viscosity Laplacian, cooling, signal
+//         speeds;
+//   FP64  the state in HBM, the conserved-variable accumulation
+//         U + dU, the pressure of cells with kinetic/total energy > 0.99,
+//         winds and ghost images, the CFL reduction across blocks and dt.
+// Conversions between the two go through the integer pipe (tlq_convert.cuh).
+// The state stays FP64 in HBM (same layout, same tensor maps), so the two
+// forms share every other kernel and the host code.
+#pragma once
+
+#include "tlq_convert.cuh"
+#include "tlq_stage.cuh"
+
+namespace tlq {
+
+constexpr int MRAW = 3;  // TMA landing slots (raw FP64 planes)
+
+struct MixedSmem {
+  double raw[MRAW][5 * PLANE_BOX];  // TMA landing zone
+  float cu[NRING][5][HY][HX];       // conserved state of the ring planes (FP32)
+  float prm[NRING][5][HY][HX];      // primitives of the ring planes (FP32)
+  float fx[5][TY][TX + 1];
+  float fy[5][TY + 1][TX];
+  float fz[2][5][TY][TX];
+  uint64_t bar[MRAW];
+  double red[96];
+  int flag;
+  int abort;
+};
+
+// One cell: FP64 conserved (stride vs) -> FP32 conserved and primitives.
+// The pressure of a cell whose kinetic energy exceeds 0.99 of its total
+// energy is recovered in FP64 (FP32 would lose it to cancellation).
+__device__ __forceinline__ void mixed_cell(float gm1, const double* u, long long vs, float* cf, float* w) {
+#pragma unroll
+  for (int e = 0; e < 5; ++e) cf[e] = d2f(u[e * vs]);
+  const float inv = 1.0f / cf[0];
+  w[0] = cf[0];
+  w[1] = cf[1] * inv;
+  w[2] = cf[2] * inv;
+  w[3] = cf[3] * inv;
+  const float ek = 0.5f * (cf[1] * w[1] + cf[2] * w[2] + cf[3] * w[3]);
+  float p;
+  if (ek > 0.99f * cf[4]) {
+    const double r = u[0], m1 = u[vs], m2 = u[2 * vs], m3 = u[3 * vs], E = u[4 * vs];
+    p = d2f((double)gm1 * (E - 0.5 * ((m1 * m1 + m2 * m2) + m3 * m3) / r));
+  } else {
+    p = gm1 * (cf[4] - ek);
+  }
+  w[4] = fmaxf(p, 1e-20f);
+}
+
+// Cooling in FP32 (the mixed form's cooling source; same algorithm as
+// cool_cell: the reference's exponential factor, its limiter and floor,
+// sub-cycled when asked).  The total energy changes by the thermal energy
+// removed, accumulated in FP64.
+__device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
+  int lo = 1, hi = t.n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (t.Tf[mid] > temp) hi = mid; else lo = mid + 1;
+  }
+  if (lo >= t.n) return exp10f(t.Cf[t.n - 1]);
+  const float T0 = t.logTf[lo - 1], C0 = t.Cf[lo - 1];
+  const float T1 = t.logTf[lo], C1 = t.Cf[lo];
+  return exp10f((C1 - C0) / (T1 - T0) * (log10f(temp) - T0) + C0);
+}
+
+__device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv_muamu, float gm1, float* w,
+                                            double& u4, float dt) {
+  const CoolTable& t = p.cool;
+  float temp = (w[4] / w[0]) * cT;
+  if (!(temp >= t.Tf[0])) return;
+  const float p0 = w[4];
+  float ETH = w[4] / gm1;
+  float aloss = cool_coef_f(t, temp);
+  const float n = w[0] * inv_muamu;
+  float ce = (aloss * n) * (n / ETH);
+  int nsub = 1;
+  const float frac = (float)p.cool_sub_frac;
+  if (p.cooling == COOL_SUBCYCLE && ce * dt > frac) {
+    const float q = ceilf(ce * dt / frac);
+    nsub = (q > (float)p.cool_max_sub) ? p.cool_max_sub : (int)q;
+    if (nsub < 1) nsub = 1;
+  }
+  const float h = dt / (float)nsub;
+  const float fmin = 1.0f - (float)p.cooling_limit;
+  for (int s = 0; s < nsub; ++s) {
+    if (s > 0) {
+      temp = (w[4] / w[0]) * cT;
+      if (!(temp >= t.Tf[0])) break;
+      ETH = w[4] / gm1;
+      aloss = cool_coef_f(t, temp);
+      ce = (aloss * n) * (n / ETH);
+    }
+    float f = __expf(-ce * h);
+    if (f < fmin) f = fmin;
+    bool floored = false;
+    if (temp * f < (float)T_FLOOR) {
+      f = (float)T_FLOOR / temp;
+      floored = true;
+    }
+    w[4] = w[4] * f;
+    if (floored) break;
+  }
+  u4 = u4 + f2d((w[4] - p0) / gm1);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(NT, 2)
+    stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, StageArgs a) {
+  constexpr int H = STAGE;
+  extern __shared__ __align__(128) unsigned char smem_bytes[];
+  MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
+  const Params& p = a.p;
+  const Layout& L = a.L;
+  const int tid = threadIdx.x;
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
+  const int k0 = 1 + (int)blockIdx.z * a.zlen;
+  const int k1 = min(p.nz, k0 + a.zlen - 1);
+  Clock* clk = a.clk;
+
+  if (!(clk->t < clk->tfin)) return;  // the loop condition of mainHD.f90:61 (uniform)
+  const double dtstep = clk->dt;
+  const double dt = (STAGE == 1) ? dtstep / 2.0 : dtstep;
+  const float gf = (float)p.gamma, gm1 = gf - 1.0f, g1f = (float)p.g1;
+  const float dtdx = (float)(dt / p.dx), dtdy = (float)(dt / p.dy), dtdz = (float)(dt / p.dz);
+  const float dtf = (float)dt;
+  const int last_plane = k1 + H;
+  const long long pxy = (long long)L.px * L.nyg;
+
+  if (tid == 0) {
+    for (int q = 0; q < MRAW; ++q) mbar_init(&s.bar[q], 1);
+    s.abort = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int issued = k0 - H - 1;
+  auto issue = [&](int q) {
+    const int slot = q % MRAW;
+    fence_proxy_async();
+    mbar_arrive_expect_tx(&s.bar[slot], 5u * PLANE_BOX * 8u);
+    tma_load_4d(s.raw[slot], &tm_in, &s.bar[slot], bx * TX, by * TY, q + 1, 0);
+    issued = q;
+  };
+  uint32_t phase = 0;
+  int waited = k0 - H - 1;
+  bool failed = false;
+  auto wait_plane = [&](int q) {
+    if (failed) return;
+    const int slot = q % MRAW;
+    if (!mbar_wait_bounded(&s.bar[slot], (phase >> slot) & 1u, WAIT_LIMIT)) {
+      failed = true;
+      s.abort = 1;
+      return;
+    }
+    phase ^= 1u << slot;
+    waited = q;
+  };
+
+  auto convert = [&](int q) {
+    const double* r0 = s.raw[q % MRAW];
+    const int sl = q & 3;
+    constexpr int RW = TX + 2 * H;
+    constexpr int NROW = RW * TY, NCOL = TX * 2 * H;
+    for (int t = tid; t < NROW + NCOL; t += NT) {
+      int lx, ly;
+      if (t < NROW) {
+        lx = 2 - H + t % RW;
+        ly = 2 + t / RW;
+      } else {
+        const int u = t - NROW, r2 = u / TX;
+        lx = 2 + u % TX;
+        ly = (r2 < H) ? (2 - H + r2) : (TY + 2 + r2 - H);
+      }
+      float cf[5], w[5];
+      mixed_cell(gm1, r0 + ly * HX + lx, PLANE_BOX, cf, w);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        s.cu[sl][e][ly][lx] = cf[e];
+        s.prm[sl][e][ly][lx] = w[e];
+      }
+    }
+  };
+
+  auto faces = [&](int k, bool xy) {
+    constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1), NZF = TX * TY;
+    const int tbeg = xy ? 0 : NXF + NYF;
+    const int sk = k & 3;
+    constexpr int VS = PLANE_BOX;
+    for (int t = tbeg + tid; t < NXF + NYF + NZF; t += NT) {
+      int d, fxl, fyl;
+      const float *w0, *w1, *w2, *w3, *uL, *uR;
+      bool valid;
+      if (t < NXF) {
+        d = 1;
+        fxl = t % (TX + 1);
+        fyl = t / (TX + 1);
+        const int ly = fyl + 2;
+        w0 = &s.prm[sk][0][ly][fxl];
+        w1 = w0 + 1; w2 = w0 + 2; w3 = w0 + 3;
+        uL = &s.cu[sk][0][ly][fxl + 1];
+        uR = uL + 1;
+        valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
+      } else if (t < NXF + NYF) {
+        d = 2;
+        const int u = t - NXF;
+        fxl = u % TX;
+        fyl = u / TX;
+        const int lx = fxl + 2;
+        w0 = &s.prm[sk][0][fyl][lx];
+        w1 = w0 + HX; w2 = w0 + 2 * HX; w3 = w0 + 3 * HX;
+        uL = &s.cu[sk][0][fyl + 1][lx];
+        uR = uL + HX;
+        valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
+      } else {
+        d = 3;
+        const int u = t - NXF - NYF;
+        fxl = u % TX;
+        fyl = u / TX;
+        const int lx = fxl + 2, ly = fyl + 2;
+        w0 = &s.prm[(k - 1) & 3][0][ly][lx];
+        w1 = &s.prm[k & 3][0][ly][lx];
+        w2 = &s.prm[(k + 1) & 3][0][ly][lx];
+        w3 = &s.prm[(k + 2) & 3][0][ly][lx];
+        uL = &s.cu[k & 3][0][ly][lx];
+        uR = &s.cu[(k + 1) & 3][0][ly][lx];
+        valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
+      }
+      if (!valid) continue;
+      float wll[5], wl[5], wr[5], wrr[5], UL[5], UR[5], ff[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        wl[e] = w1[e * VS];
+        wr[e] = w2[e * VS];
+        UL[e] = uL[e * VS];
+        UR[e] = uR[e * VS];
+      }
+      if (STAGE == 2) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) {
+          wll[e] = w0[e * VS];
+          wrr[e] = w3[e * VS];
+        }
+        limiter(wll, wl, wr, wrr, p.limiter);
+      }
+      if (!riemann(p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) ff[e] = NAN;
+      }
+      if (d == 1) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
+      } else if (d == 2) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
+      } else {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
+      }
+    }
+  };
+
+  // ---- prologue: planes k0-H .. k0+H-1, then the z face k0-1/2 ------------
+  if (tid == 0)
+    for (int q = k0 - H; q <= min(k0 - H + MRAW - 1, last_plane); ++q) issue(q);
+  bool aborted = false;
+  for (int q = k0 - H; q <= k0 + H - 1; ++q) {
+    wait_plane(q);
+    convert(q);
+    __syncthreads();
+    if (s.abort) { aborted = true; break; }
+    if (tid == 0 && q + MRAW <= last_plane && q + MRAW > issued) issue(q + MRAW);
+  }
+  if (!aborted) faces(k0 - 1, false);
+  __syncthreads();
+
+  const int tx = tid % TX, ty = tid / TX;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool cell_ok = (i <= p.nx) && (j <= p.ny);
+  float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
+  const float cT = (float)(p.mu0 * AMU / KB);
+  const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
+  const float etaf = (float)p.eta;
+
+  for (int k = k0; k <= k1 && !aborted; ++k) {
+    wait_plane(k + H);
+    convert(k + H);
+    __syncthreads();  // S1
+    if (s.abort) { aborted = true; break; }
+    if (tid == 0 && k + H + MRAW <= last_plane && k + H + MRAW > issued) issue(k + H + MRAW);
+    faces(k, true);
+    __syncthreads();  // S2
+
+    if (cell_ok) {
+      const int cur = (k + 1) & 1, prv = k & 1;
+      const long long c = L.at(i, j, k);
+      float dU[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e)
+        dU[e] = dtdx * (s.fx[e][ty][tx + 1] - s.fx[e][ty][tx]) + dtdy * (s.fy[e][ty + 1][tx] - s.fy[e][ty][tx]) +
+                dtdz * (s.fz[cur][e][ty][tx] - s.fz[prv][e][ty][tx]);
+      if (p.gravity) {
+        const double* ph = a.phi;
+        float w[5], sv[5];
+#pragma unroll
+        for (int e = 0; e < 5; ++e) w[e] = s.prm[k & 3][e][ty + 2][tx + 2];
+        const float fg1 = (d2f(ph[c + 1]) - d2f(ph[c - 1])) * (float)(0.5 / p.dx);
+        const float fg2 = (d2f(ph[c + L.px]) - d2f(ph[c - L.px])) * (float)(0.5 / p.dy);
+        const float fg3 = (d2f(ph[c + pxy]) - d2f(ph[c - pxy])) * (float)(0.5 / p.dz);
+        sv[0] = 0.0f;
+        sv[1] = -w[0] * fg1;
+        sv[2] = -w[0] * fg2;
+        sv[3] = -w[0] * fg3;
+        sv[4] = -w[0] * (w[1] * fg1 + w[2] * fg2 + w[3] * fg3);
+#pragma unroll
+        for (int e = 0; e < 5; ++e) dU[e] -= dtf * sv[e];
+      }
+      // FP64 accumulation: U' = U - dU (Godunov's centre value is U in both
+      // stages; `uold` is the stage-1 input and the stage-2 old state)
+      double uc[5], up[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        uc[e] = a.uold[e * L.plane + c];
+        up[e] = uc[e] - f2d(dU[e]);
+      }
+      write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
+      winds_cell(p, i, j, k, up);
+      if (STAGE == 1) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = up[e];
+      } else {
+        // step: U = UP + eta * (Laplacian of the old U), Laplacian in FP32
+        double un[5];
+#pragma unroll
+        for (int e = 0; e < 5; ++e) {
+          const double* q = a.uold + e * L.plane + c;
+          const float lap = ((d2f(q[1]) + d2f(q[-1])) + (d2f(q[L.px]) + d2f(q[-L.px]))) +
+                            ((d2f(q[pxy]) + d2f(q[-pxy])) - 6.0f * d2f(uc[e]));
+          un[e] = up[e] + f2d(etaf * lap);
+        }
+        float cf[5], w[5];
+        mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
+        if (p.cooling != COOL_NONE) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], (float)dtstep);
+        if (!(un[0] > 0.0)) atomicOr(&clk->status, ST_NEG_DENSITY);
+#pragma unroll
+        for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
+        const float cs = sqrtf(gf * w[4] / w[0]);
+        const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
+        m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
+        m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
+        m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
+      }
+    }
+  }
+
+  double d0 = f2d(m0), d1 = f2d(m1), d2 = f2d(m2);
+  if (aborted) {
+    if (tid == 0) {
+      atomicOr(&clk->status, ST_TIMEOUT);
+      for (int q = waited + 1; q <= issued; ++q) {
+        const int slot = q % MRAW;
+        mbar_wait_bounded(&s.bar[slot], (phase >> slot) & 1u, WAIT_LIMIT);
+        phase ^= 1u << slot;
+      }
+    }
+    d0 = d1 = d2 = NAN;
+  }
+  if (STAGE == 2) cfl_reduce_finalize<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag);
+}
+
+}  // namespace tlq
