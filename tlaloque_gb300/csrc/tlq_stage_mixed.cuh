@@ -20,6 +20,10 @@ namespace tlq {
 
 constexpr int MRAW = 3;  // TMA landing slots (raw FP64 planes)
 
+// Landing slot of plane q.  Planes start at k0 - 2 >= -1, so q can be
+// negative; C++ '%' keeps the sign of q, hence the offset.
+__device__ __forceinline__ int raw_slot(int q) { return (q + 2 * MRAW) % MRAW; }
+
 struct MixedSmem {
   double raw[MRAW][5 * PLANE_BOX];  // TMA landing zone
   float cu[NRING][5][HY][HX];       // conserved state of the ring planes (FP32)
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(NT, 2)
 
   int issued = k0 - H - 1;
   auto issue = [&](int q) {
-    const int slot = q % MRAW;
+    const int slot = raw_slot(q);
     fence_proxy_async();
     mbar_arrive_expect_tx(&s.bar[slot], 5u * PLANE_BOX * 8u);
     tma_load_4d(s.raw[slot], &tm_in, &s.bar[slot], bx * TX, by * TY, q + 1, 0);
@@ -155,7 +159,7 @@ __global__ void __launch_bounds__(NT, 2)
   bool failed = false;
   auto wait_plane = [&](int q) {
     if (failed) return;
-    const int slot = q % MRAW;
+    const int slot = raw_slot(q);
     if (!mbar_wait_bounded(&s.bar[slot], (phase >> slot) & 1u, WAIT_LIMIT)) {
       failed = true;
       s.abort = 1;
@@ -166,7 +170,7 @@ __global__ void __launch_bounds__(NT, 2)
   };
 
   auto convert = [&](int q) {
-    const double* r0 = s.raw[q % MRAW];
+    const double* r0 = s.raw[raw_slot(q)];
     const int sl = q & 3;
     constexpr int RW = TX + 2 * H;
     constexpr int NROW = RW * TY, NCOL = TX * 2 * H;
@@ -366,7 +370,7 @@ __global__ void __launch_bounds__(NT, 2)
     if (tid == 0) {
       atomicOr(&clk->status, ST_TIMEOUT);
       for (int q = waited + 1; q <= issued; ++q) {
-        const int slot = q % MRAW;
+        const int slot = raw_slot(q);
         mbar_wait_bounded(&s.bar[slot], (phase >> slot) & 1u, WAIT_LIMIT);
         phase ^= 1u << slot;
       }
