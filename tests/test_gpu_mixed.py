@@ -47,8 +47,9 @@ def test_mixed_short_run_against_oracle(gpu_lib, limiter):
     run.run(10)
     U, W, (t, it, dt, rc), _ = run_gpu(cfg, U0, 10, precision=tlq.PREC_MIXED)
     assert rc == tlq.OK and it == run.it
-    for e in range(5):
-        assert rel_l1(interior(U)[e], interior(run.U)[e]) < 1e-5, e
+    err = [rel_l1(interior(U)[e], interior(run.U)[e]) for e in range(5)]
+    # FP32 round-off on a Mach ~1 random field, 10 steps (the bar is 1 %)
+    assert max(err) < 2e-4, err
     assert abs(t - run.t) < 1e-5 * run.t
 
 

@@ -18,15 +18,17 @@
 
 namespace tlq {
 
-constexpr int MRAW = 3;  // TMA landing slots (raw FP64 planes)
+constexpr int MRAW = 2;  // TMA landing slots (raw FP64 planes); a plane is requested two planes ahead
+constexpr int MCU = 3;   // FP32 conserved-state ring (the faces need planes k and k+1)
 
-// Landing slot of plane q.  Planes start at k0 - 2 >= -1, so q can be
+// Ring slots of plane q.  Planes start at k0 - 2 >= -1, so q can be
 // negative; C++ '%' keeps the sign of q, hence the offset.
-__device__ __forceinline__ int raw_slot(int q) { return (q + 2 * MRAW) % MRAW; }
+__device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
+__device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
 
 struct MixedSmem {
   double raw[MRAW][5 * PLANE_BOX];  // TMA landing zone
-  float cu[NRING][5][HY][HX];       // conserved state of the ring planes (FP32)
+  float cu[MCU][5][HY][HX];         // conserved state of the ring planes (FP32)
   float prm[NRING][5][HY][HX];      // primitives of the ring planes (FP32)
   float fx[5][TY][TX + 1];
   float fy[5][TY + 1][TX];
@@ -75,11 +77,27 @@ __device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
   return exp10f((C1 - C0) / (T1 - T0) * (log10f(temp) - T0) + C0);
 }
 
+// Whether cooling applies (temp >= the table's first temperature,
+// cooling.f90:71).  The switch is a jump in the source term; a cell whose
+// FP32 temperature falls within 1e-6 of the edge (e.g. a medium initialised
+// at exactly the table's lower edge) decides it from the FP64 state with the
+// plain step's arithmetic (uncontracted intrinsics), so both forms agree.
+__device__ __forceinline__ bool cools_at(const Params& p, float temp, const double* u) {
+  const float Tmin = p.cool.Tf[0];
+  if (fabsf(temp - Tmin) > 1e-6f * Tmin) return temp >= Tmin;
+  const double r = u[0];
+  const double k2 = __dadd_rn(__dadd_rn(__dmul_rn(u[1], u[1]), __dmul_rn(u[2], u[2])), __dmul_rn(u[3], u[3]));
+  double pr = __dmul_rn(__dsub_rn(p.gamma, 1.0), __dsub_rn(u[4], __ddiv_rn(__dmul_rn(0.5, k2), r)));
+  pr = pr > 1e-20 ? pr : 1e-20;
+  const double T = __ddiv_rn(__dmul_rn(__dmul_rn(pr, p.mu0), AMU), __dmul_rn(r, KB));
+  return T >= p.cool.T[0];
+}
+
 __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv_muamu, float gm1, float* w,
-                                            double& u4, float dt) {
+                                            double& u4, float dt, const double* u) {
   const CoolTable& t = p.cool;
   float temp = (w[4] / w[0]) * cT;
-  if (!(temp >= t.Tf[0])) return;
+  if (!cools_at(p, temp, u)) return;
   const float p0 = w[4];
   float ETH = w[4] / gm1;
   float aloss = cool_coef_f(t, temp);
@@ -97,7 +115,7 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   for (int s = 0; s < nsub; ++s) {
     if (s > 0) {
       temp = (w[4] / w[0]) * cT;
-      if (!(temp >= t.Tf[0])) break;
+      if (!(temp >= t.Tf[0])) break;  // (after a sub-step the state is no longer the stored one)
       ETH = w[4] / gm1;
       aloss = cool_coef_f(t, temp);
       ce = (aloss * n) * (n / ETH);
@@ -116,7 +134,7 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(NT, 2)
+__global__ void __launch_bounds__(NT, 3)
     stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, StageArgs a) {
   constexpr int H = STAGE;
   extern __shared__ __align__(128) unsigned char smem_bytes[];
@@ -171,7 +189,7 @@ __global__ void __launch_bounds__(NT, 2)
 
   auto convert = [&](int q) {
     const double* r0 = s.raw[raw_slot(q)];
-    const int sl = q & 3;
+    const int sl = q & 3, sc = cu_slot(q);
     constexpr int RW = TX + 2 * H;
     constexpr int NROW = RW * TY, NCOL = TX * 2 * H;
     for (int t = tid; t < NROW + NCOL; t += NT) {
@@ -188,7 +206,7 @@ __global__ void __launch_bounds__(NT, 2)
       mixed_cell(gm1, r0 + ly * HX + lx, PLANE_BOX, cf, w);
 #pragma unroll
       for (int e = 0; e < 5; ++e) {
-        s.cu[sl][e][ly][lx] = cf[e];
+        s.cu[sc][e][ly][lx] = cf[e];
         s.prm[sl][e][ly][lx] = w[e];
       }
     }
@@ -210,7 +228,7 @@ __global__ void __launch_bounds__(NT, 2)
         const int ly = fyl + 2;
         w0 = &s.prm[sk][0][ly][fxl];
         w1 = w0 + 1; w2 = w0 + 2; w3 = w0 + 3;
-        uL = &s.cu[sk][0][ly][fxl + 1];
+        uL = &s.cu[cu_slot(k)][0][ly][fxl + 1];
         uR = uL + 1;
         valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
       } else if (t < NXF + NYF) {
@@ -221,7 +239,7 @@ __global__ void __launch_bounds__(NT, 2)
         const int lx = fxl + 2;
         w0 = &s.prm[sk][0][fyl][lx];
         w1 = w0 + HX; w2 = w0 + 2 * HX; w3 = w0 + 3 * HX;
-        uL = &s.cu[sk][0][fyl + 1][lx];
+        uL = &s.cu[cu_slot(k)][0][fyl + 1][lx];
         uR = uL + HX;
         valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
       } else {
@@ -234,8 +252,8 @@ __global__ void __launch_bounds__(NT, 2)
         w1 = &s.prm[k & 3][0][ly][lx];
         w2 = &s.prm[(k + 1) & 3][0][ly][lx];
         w3 = &s.prm[(k + 2) & 3][0][ly][lx];
-        uL = &s.cu[k & 3][0][ly][lx];
-        uR = &s.cu[(k + 1) & 3][0][ly][lx];
+        uL = &s.cu[cu_slot(k)][0][ly][lx];
+        uR = &s.cu[cu_slot(k + 1)][0][ly][lx];
         valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
       }
       if (!valid) continue;
@@ -293,6 +311,8 @@ __global__ void __launch_bounds__(NT, 2)
   const float cT = (float)(p.mu0 * AMU / KB);
   const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
   const float etaf = (float)p.eta;
+  const float hdx = (float)(0.5 / p.dx), hdy = (float)(0.5 / p.dy), hdz = (float)(0.5 / p.dz);
+  const float dtstep_f = (float)dtstep;
 
   for (int k = k0; k <= k1 && !aborted; ++k) {
     wait_plane(k + H);
@@ -316,9 +336,9 @@ __global__ void __launch_bounds__(NT, 2)
         float w[5], sv[5];
 #pragma unroll
         for (int e = 0; e < 5; ++e) w[e] = s.prm[k & 3][e][ty + 2][tx + 2];
-        const float fg1 = (d2f(ph[c + 1]) - d2f(ph[c - 1])) * (float)(0.5 / p.dx);
-        const float fg2 = (d2f(ph[c + L.px]) - d2f(ph[c - L.px])) * (float)(0.5 / p.dy);
-        const float fg3 = (d2f(ph[c + pxy]) - d2f(ph[c - pxy])) * (float)(0.5 / p.dz);
+        const float fg1 = (d2f(ph[c + 1]) - d2f(ph[c - 1])) * hdx;
+        const float fg2 = (d2f(ph[c + L.px]) - d2f(ph[c - L.px])) * hdy;
+        const float fg3 = (d2f(ph[c + pxy]) - d2f(ph[c - pxy])) * hdz;
         sv[0] = 0.0f;
         sv[1] = -w[0] * fg1;
         sv[2] = -w[0] * fg2;
@@ -352,7 +372,7 @@ __global__ void __launch_bounds__(NT, 2)
         }
         float cf[5], w[5];
         mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
-        if (p.cooling != COOL_NONE) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], (float)dtstep);
+        if (p.cooling != COOL_NONE) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
         if (!(un[0] > 0.0)) atomicOr(&clk->status, ST_NEG_DENSITY);
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
