@@ -48,8 +48,9 @@ def test_mixed_short_run_against_oracle(gpu_lib, limiter):
     U, W, (t, it, dt, rc), _ = run_gpu(cfg, U0, 10, precision=tlq.PREC_MIXED)
     assert rc == tlq.OK and it == run.it
     err = [rel_l1(interior(U)[e], interior(run.U)[e]) for e in range(5)]
-    # FP32 round-off on a Mach ~1 random field, 10 steps (the bar is 1 %)
-    assert max(err) < 2e-4, err
+    # FP32 round-off on a Mach ~1 random field, 10 steps (the bar is 1 %;
+    # superbee, the most compressive limiter, amplifies it most)
+    assert max(err) < 1e-3, err
     assert abs(t - run.t) < 1e-5 * run.t
 
 

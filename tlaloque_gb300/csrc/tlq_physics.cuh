@@ -99,8 +99,20 @@ __device__ __forceinline__ R average(R a, R b, int opt) {
     case LIM_NONE:
       return R(0.5) * (a + b);
     case LIM_VANLEER:
-      if (a * b <= R(0.0)) return R(0.0);
-      return a * b * (a + b) / (a * a + b * b);
+      if constexpr (sizeof(R) == 4) {
+        // FP32 (mixed form): the same limiter without products of two
+        // differences, which underflow FP32 for cgs-scale densities
+        // (|drho| ~ 1e-25 g/cm^3 squared is below FLT_MIN):
+        // a b (a+b)/(a^2+b^2) = m r (1+r)/(1+r^2), m the larger, r = ratio <= 1.
+        if (!((a > R(0) && b > R(0)) || (a < R(0) && b < R(0)))) return R(0.0);
+        const bool ab = fabs(a) >= fabs(b);
+        const R m = ab ? a : b;
+        const R r = ab ? b / a : a / b;
+        return m * r * (R(1) + r) / (R(1) + r * r);
+      } else {
+        if (a * b <= R(0.0)) return R(0.0);
+        return a * b * (a + b) / (a * a + b * b);
+      }
     case LIM_MINMOD:
       s = sgn1(a);
       return s * mx(R(0.0), mn(fabs(a), s * b));

@@ -140,7 +140,11 @@ def wind_bubble(n: int = 256, cooling: int = COOL_SUBCYCLE, T_wind: float = 1.0e
                       vinf=vw_kms * KMS, temp=T_wind, mu=mu)]
     cfg.masses = np.array([[0.0, 0.0, 0.0, mass_msun * MSUN]])
     rho = n_amb * mu * AMU
-    p = n_amb * KB * 1.0e4
+    # T = 1e4 K is the cooling table's first entry: cooling.f90:71 cools a
+    # cell when temp >= cool_Tmin, so a medium at exactly 1e4 K is decided by
+    # the last bit of its pressure.  1e-9 above the edge gives the
+    # exact-arithmetic decision (cooled) robustly in every precision.
+    p = n_amb * KB * 1.0e4 * (1.0 + 1e-9)
     return cfg, conserved(cfg, rho, 0.0, 0.0, 0.0, p)
 
 
