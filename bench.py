@@ -82,12 +82,14 @@ def bytes_per_zone(cfg, mixed: bool = False) -> dict:
     """Algorithmic HBM bytes per zone-update of each stage kernel (FP64 state:
     5 conserved variables x 8 B; the plain form carries the cooled interior
     pressure (8 B written by stage 2, read by stage 1; the mixed form
-    recomputes it); point gravity reads phi once per stage)."""
+    recomputes it, and moves the viscosity Laplacian into stage 1 as an FP32
+    plane); point gravity reads phi once per stage)."""
     from tlaloque_gb300 import tlq
     cool = cfg.cooling != tlq.COOL_NONE and not mixed
     grav = cfg.masses is not None and len(cfg.masses) > 0
-    s1 = 40 + 40 + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
-    s2 = 40 + 40 + 40 + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
+    lap = 20 if mixed else 0  # mixed: stage 1 writes eta*Lap(U) in FP32, stage 2 reads it
+    s1 = 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
+    s2 = 40 + 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
     return {"stage1": s1, "stage2": s2, "step": s1 + s2}
 
 

@@ -30,6 +30,7 @@ struct tlq_ctx {
   double* UPP = nullptr;
   double* Pc = nullptr;   // carried pressure plane (cooling)
   double* phi = nullptr;  // point-mass potential plane
+  float* lapf = nullptr;  // mixed form: eta * Laplacian of U between the stages
   Clock* clk = nullptr;
   Clock* clk_host = nullptr;  // pinned mirror
   double* partials = nullptr;
@@ -192,6 +193,7 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.partials = ctx->partials;
   a.zlen = ctx->zlen;
   a.phi = ctx->phi;
+  a.lapf = ctx->lapf;
   // stage 1: U[par] -> UPP
   a.uold = ctx->U[par];
   a.out = ctx->UPP;
@@ -340,6 +342,10 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   cudaMemset(ctx->UPP, 0, soa);
   cudaMemset(ctx->Pc, 0, (size_t)L.plane * 8);
   cudaMemset(ctx->phi, 0, (size_t)L.plane * 8);
+  if (cfg->precision == TLQ_PREC_MIXED) {
+    if (cudaMalloc(&ctx->lapf, (size_t)L.plane * 5 * sizeof(float))) return bail(TLQ_ERR_NOMEM);
+    cudaMemset(ctx->lapf, 0, (size_t)L.plane * 5 * sizeof(float));
+  }
   if (cudaMalloc(&ctx->clk, sizeof(Clock)) || cudaMallocHost(&ctx->clk_host, sizeof(Clock))) return bail(TLQ_ERR_NOMEM);
   std::memset(ctx->clk_host, 0, sizeof(Clock));
   ctx->clk_host->tfin = std::numeric_limits<double>::infinity();
@@ -374,6 +380,7 @@ int tlq_destroy(tlq_ctx* ctx) {
   for (int q = 0; q < 3; ++q)
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
+  cudaFree(ctx->lapf);
   cudaFree(ctx->clk); cudaFree(ctx->partials); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);

@@ -36,6 +36,7 @@ struct StageArgs {
   double* partials;    // 3 doubles per block (CFL reduction scratch)
   int zlen;            // planes per block
   int use_p;           // STAGE 1 with cooling: interior pressure from the P plane
+  float* lapf;         // mixed form: eta * Laplacian of U (FP32, written by stage 1, read by stage 2)
 };
 
 template <class R>

@@ -19,12 +19,11 @@
 namespace tlq {
 
 constexpr int MRAW = 2;  // TMA landing slots (raw FP64 planes); a plane is requested two planes ahead
-constexpr int MCU = 3;   // FP32 conserved-state ring (the faces need planes k and k+1)
+constexpr int MCU = 4;   // FP32 conserved-state ring (faces: planes k, k+1; stage-1 Laplacian: k-1..k+1)
 
 // Ring slots of plane q.  Planes start at k0 - 2 >= -1, so q can be
 // negative; C++ '%' keeps the sign of q, hence the offset.
 __device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
-__device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
 
 struct MixedSmem {
   double raw[MRAW][5 * PLANE_BOX];  // TMA landing zone
@@ -189,7 +188,7 @@ __global__ void __launch_bounds__(NT, 3)
 
   auto convert = [&](int q) {
     const double* r0 = s.raw[raw_slot(q)];
-    const int sl = q & 3, sc = cu_slot(q);
+    const int sl = q & 3, sc = q & 3;
     constexpr int RW = TX + 2 * H;
     constexpr int NROW = RW * TY, NCOL = TX * 2 * H;
     for (int t = tid; t < NROW + NCOL; t += NT) {
@@ -228,7 +227,7 @@ __global__ void __launch_bounds__(NT, 3)
         const int ly = fyl + 2;
         w0 = &s.prm[sk][0][ly][fxl];
         w1 = w0 + 1; w2 = w0 + 2; w3 = w0 + 3;
-        uL = &s.cu[cu_slot(k)][0][ly][fxl + 1];
+        uL = &s.cu[k & 3][0][ly][fxl + 1];
         uR = uL + 1;
         valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
       } else if (t < NXF + NYF) {
@@ -239,7 +238,7 @@ __global__ void __launch_bounds__(NT, 3)
         const int lx = fxl + 2;
         w0 = &s.prm[sk][0][fyl][lx];
         w1 = w0 + HX; w2 = w0 + 2 * HX; w3 = w0 + 3 * HX;
-        uL = &s.cu[cu_slot(k)][0][fyl + 1][lx];
+        uL = &s.cu[k & 3][0][fyl + 1][lx];
         uR = uL + HX;
         valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
       } else {
@@ -252,8 +251,8 @@ __global__ void __launch_bounds__(NT, 3)
         w1 = &s.prm[k & 3][0][ly][lx];
         w2 = &s.prm[(k + 1) & 3][0][ly][lx];
         w3 = &s.prm[(k + 2) & 3][0][ly][lx];
-        uL = &s.cu[cu_slot(k)][0][ly][lx];
-        uR = &s.cu[cu_slot(k + 1)][0][ly][lx];
+        uL = &s.cu[k & 3][0][ly][lx];
+        uR = &s.cu[(k + 1) & 3][0][ly][lx];
         valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
       }
       if (!valid) continue;
@@ -315,6 +314,25 @@ __global__ void __launch_bounds__(NT, 3)
   const float dtstep_f = (float)dtstep;
 
   for (int k = k0; k <= k1 && !aborted; ++k) {
+    // Global operands of this cell's update, requested now so that their
+    // latency hides behind the conversion and face phases.
+    const long long c = L.at(i, j, k);
+    double uc[5];
+    float lv[5];
+    double ph[6];
+    if (cell_ok) {
+#pragma unroll
+      for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
+      if (STAGE == 2) {
+#pragma unroll
+        for (int e = 0; e < 5; ++e) lv[e] = a.lapf[e * L.plane + c];
+      }
+      if (p.gravity) {
+        ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
+        ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
+        ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
+      }
+    }
     wait_plane(k + H);
     convert(k + H);
     __syncthreads();  // S1
@@ -325,20 +343,18 @@ __global__ void __launch_bounds__(NT, 3)
 
     if (cell_ok) {
       const int cur = (k + 1) & 1, prv = k & 1;
-      const long long c = L.at(i, j, k);
       float dU[5];
 #pragma unroll
       for (int e = 0; e < 5; ++e)
         dU[e] = dtdx * (s.fx[e][ty][tx + 1] - s.fx[e][ty][tx]) + dtdy * (s.fy[e][ty + 1][tx] - s.fy[e][ty][tx]) +
                 dtdz * (s.fz[cur][e][ty][tx] - s.fz[prv][e][ty][tx]);
       if (p.gravity) {
-        const double* ph = a.phi;
         float w[5], sv[5];
 #pragma unroll
         for (int e = 0; e < 5; ++e) w[e] = s.prm[k & 3][e][ty + 2][tx + 2];
-        const float fg1 = (d2f(ph[c + 1]) - d2f(ph[c - 1])) * hdx;
-        const float fg2 = (d2f(ph[c + L.px]) - d2f(ph[c - L.px])) * hdy;
-        const float fg3 = (d2f(ph[c + pxy]) - d2f(ph[c - pxy])) * hdz;
+        const float fg1 = (d2f(ph[0]) - d2f(ph[1])) * hdx;
+        const float fg2 = (d2f(ph[2]) - d2f(ph[3])) * hdy;
+        const float fg3 = (d2f(ph[4]) - d2f(ph[5])) * hdz;
         sv[0] = 0.0f;
         sv[1] = -w[0] * fg1;
         sv[2] = -w[0] * fg2;
@@ -349,11 +365,21 @@ __global__ void __launch_bounds__(NT, 3)
       }
       // FP64 accumulation: U' = U - dU (Godunov's centre value is U in both
       // stages; `uold` is the stage-1 input and the stage-2 old state)
-      double uc[5], up[5];
+      double up[5];
 #pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        uc[e] = a.uold[e * L.plane + c];
-        up[e] = uc[e] - f2d(dU[e]);
+      for (int e = 0; e < 5; ++e) up[e] = uc[e] - f2d(dU[e]);
+      if (STAGE == 1) {
+        // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U
+        // this stage streams (= the old U of stage 2), in FP32 from the ring
+        const int a0 = (k - 1) & 3, a1 = k & 3, a2 = (k + 1) & 3;
+        const int lx = tx + 2, ly = ty + 2;
+#pragma unroll
+        for (int e = 0; e < 5; ++e) {
+          const float lap = ((s.cu[a1][e][ly][lx + 1] + s.cu[a1][e][ly][lx - 1]) +
+                             (s.cu[a1][e][ly + 1][lx] + s.cu[a1][e][ly - 1][lx])) +
+                            ((s.cu[a2][e][ly][lx] + s.cu[a0][e][ly][lx]) - 6.0f * s.cu[a1][e][ly][lx]);
+          a.lapf[e * L.plane + c] = etaf * lap;
+        }
       }
       write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
       winds_cell(p, i, j, k, up);
@@ -361,15 +387,10 @@ __global__ void __launch_bounds__(NT, 3)
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = up[e];
       } else {
-        // step: U = UP + eta * (Laplacian of the old U), Laplacian in FP32
+        // step: U = UP + eta * (Laplacian of the old U), from stage 1
         double un[5];
 #pragma unroll
-        for (int e = 0; e < 5; ++e) {
-          const double* q = a.uold + e * L.plane + c;
-          const float lap = ((d2f(q[1]) + d2f(q[-1])) + (d2f(q[L.px]) + d2f(q[-L.px]))) +
-                            ((d2f(q[pxy]) + d2f(q[-pxy])) - 6.0f * d2f(uc[e]));
-          un[e] = up[e] + f2d(etaf * lap);
-        }
+        for (int e = 0; e < 5; ++e) un[e] = up[e] + f2d(lv[e]);
         float cf[5], w[5];
         mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
         if (p.cooling != COOL_NONE) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
