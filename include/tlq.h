@@ -45,7 +45,8 @@ enum { TLQ_SOLVER_HLLC = 0, TLQ_SOLVER_HLL = 1 };
 /* Radiative cooling: off; the reference's single exponential step
  * (source/cooling.f90:47-119); its sub-cycled extension (nsub = 1 is the
  * reference formula exactly). */
-enum { TLQ_COOL_NONE = 0, TLQ_COOL_REF = 1, TLQ_COOL_SUBCYCLE = 2 };
+enum { TLQ_COOL_NONE = 0, TLQ_COOL_REF = 1, TLQ_COOL_SUBCYCLE = 2,
+       TLQ_COOL_MLP = 3 /* learned surrogate with the sub-cycled integrator as fallback (mixed form only) */ };
 /* Arithmetic of the fused step: plain FP64 (matches the reference), or
  * mixed (FP32 reconstruction and Riemann fluxes, FP64 accumulation). */
 enum { TLQ_PREC_FP64 = 0, TLQ_PREC_MIXED = 1 };
@@ -80,6 +81,46 @@ typedef struct tlq_wind {
   double mu;          /* wind mean particle mass [AMU] */
 } tlq_wind;
 
+/* Learned cooling surrogate (build-defined; the reference has none).  A
+ * 3-64-64-64-1 SiLU network maps (log10 n, log10 T, log10 tau), tau =
+ * Lambda(T) n^2 dt / E_th the step's cooling number, to r with
+ * ln(T/T_new) = tau (1 + tau r) (exact to first order in tau whatever r is).  It is trained on the GPU on pairs from the
+ * sub-cycled integrator (the "exact" one: sub-steps of sub_frac and
+ * sub_frac/2, Richardson-extrapolated in ln T); in the step a cell
+ * falls back to that integrator (the context's cool_sub_frac/cool_max_sub)
+ * when it lies outside the training box or when the a-posteriori energy
+ * residual |T_pred - T_int|/T > 1e-3, T_int from the closed-form cooling-time
+ * integral of the piecewise power-law table (Townsend 2009), and when that
+ * integral says the cooling reaches the table's first temperature T_0 within
+ * the step (there the integrator's last sub-step decides how far below T_0
+ * the cell ends).  T_pred = max(T exp(-tau (1 + tau r)), T_0); training
+ * ignores the pairs that reach T_0 and weighs pairs with tau < 1e-5 by
+ * (tau/1e-5)^2 (their r is lost to FP64 round-off). */
+#define TLQ_MLP_NPARAM 8641
+typedef struct tlq_surrogate_opts {
+  long long nsamples;      /* training pairs (default 2e7; 1 % held out) */
+  int epochs;              /* passes over the pairs (default 30) */
+  int batch;               /* minibatch (default 4096) */
+  float lr;                /* Adam learning rate, cosine-decayed to lr/20 (default 3e-3) */
+  unsigned long long seed;
+  double box[6];           /* training box: log10 n, log10 T, log10 tau (lo, hi pairs;
+                              default -4 4, 4 8.5, -8 1) */
+  double sub_frac;         /* exact integrator: max tau per sub-step (default 2e-3) */
+  int max_sub;             /* exact integrator: max sub-steps (default 20000) */
+} tlq_surrogate_opts;
+
+typedef struct tlq_surrogate_report {
+  double loss_first, loss_last;  /* minibatch MSE of y at the first and last step */
+  double val_rmse_y;             /* RMSE of y = 1 + tau r on the held-out pairs that do not reach T_0
+                                    (the other metrics too) */
+  double val_max_rel_T;          /* max |T_pred - T_exact| / T on the held-out pairs (T_pred
+                                    clamped at the table's first temperature, as in the step) */
+  double val_p99_rel_T;          /* 99th percentile of the same */
+  double val_accept;             /* fraction of held-out pairs within the step's 1e-3 check */
+  double ms_generate, ms_train;  /* wall time of pair generation and training */
+  long long steps;               /* optimiser steps */
+} tlq_surrogate_report;
+
 typedef struct tlq_stats {
   long long steps;      /* tlq_step/tlq_advance iterations since tlq_upload */
   double t, dt;         /* simulated time and the dt of the last step */
@@ -89,6 +130,8 @@ typedef struct tlq_stats {
   double ms_stage2;     /* average device time of the last timed stage-2 launches */
   long long timed;      /* number of timed steps behind the averages */
   double bytes_state;   /* device bytes held for the mesh state */
+  long long cool_mlp;      /* TLQ_COOL_MLP: cell-steps cooled by the network (since upload) */
+  long long cool_fallback; /* TLQ_COOL_MLP: cell-steps handed to the exact integrator */
 } tlq_stats;
 
 typedef struct tlq_ctx tlq_ctx;
@@ -140,6 +183,25 @@ const char* tlq_last_error(tlq_ctx* ctx);
 const char* tlq_status_string(int status);
 /* Global sums over the interior: mass, x/y/z momentum, total energy. */
 int tlq_conserved_sums(tlq_ctx* ctx, double out[5]);
+
+/* Cooling surrogate: train on the GPU with the context's cooling table and
+ * physics (stores the network in the context), read or install a network. */
+void tlq_surrogate_opts_default(tlq_surrogate_opts* opts);
+int tlq_train_cooling_surrogate(tlq_ctx* ctx, const tlq_surrogate_opts* opts, tlq_surrogate_report* report);
+int tlq_get_cooling_surrogate(tlq_ctx* ctx, float* params, float* norm6, double* box6);
+int tlq_set_cooling_surrogate(tlq_ctx* ctx, const float* params, const float* norm6, const double* box6);
+/* Training pairs from the exact integrator (context's table and physics,
+ * sub-steps sub_frac/max_sub): X = raw features (3 per pair), Y = targets,
+ * raw = (n, T, T_new, dt) per pair (may be NULL).  Host arrays. */
+int tlq_cooling_pairs(tlq_ctx* ctx, long long n, unsigned long long seed, const double* box6, double sub_frac,
+                      int max_sub, float* X, float* Y, double* raw);
+/* Context-free network pieces on host arrays (normalised features): loss
+ * sum_i w_i (y_i - t_i)^2 / n (w_i = Wt[i], or 1 when Wt is NULL) and its
+ * gradient w.r.t. the 8641 FP32 parameters, and inference.  Training weighs
+ * each pair by max(tau exp(-t tau), 1e-2)^2, the sensitivity of T_new/T to y. */
+int tlq_mlp_loss_grad(const float* params, const float* X, const float* Y, const float* Wt, int n, float* grad,
+                      float* loss);
+int tlq_mlp_infer(const float* params, const float* X, int n, float* Y);
 
 /* ---- Per-routine entry points (unit parity; host arrays in the reference
  * layout; each replaces the external subroutine cited). ------------------- */

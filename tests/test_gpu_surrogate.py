@@ -1,0 +1,236 @@
+"""Learned cooling surrogate: the GPU training and inference kernels against
+the CPU oracle of the network (oracle/mlp_oracle.py), the training pairs
+against the C oracle's sub-cycled integrator, training itself, and the
+surrogate inside the mixed step (fallback, accuracy bars, and what it gains
+over the sub-cycled integrator it replaces)."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+from oracle.oracle import COOL_SUBCYCLE as O_SUBCYCLE, Oracle
+from tests.helpers import interior, oracle_params
+from tlaloque_gb300 import problems, tlq
+
+pytestmark = pytest.mark.gpu
+
+TRAIN = dict(nsamples=1 << 22, epochs=120, batch=4096, seed=7)
+
+
+def rel_l1(a, b):
+    return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
+
+
+def mixed_cfg(cfg, cooling, **kw):
+    return tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_MIXED, "cooling": cooling, **kw})
+
+
+@pytest.fixture(scope="module")
+def trained(gpu_lib):
+    """One network for the synthetic cooling curve (mu 1.3, gamma 5/3), the
+    physics both the wind bubble and the clumpy medium use."""
+    cfg, _ = problems.wind_bubble(16)
+    with tlq.Context(cfg) as ctx:
+        rep = ctx.train_cooling_surrogate(**TRAIN)
+        net = ctx.get_cooling_surrogate()
+    print("training report:", rep)
+    return rep, net
+
+
+# ---------------------------------------------------------------------------
+# kernels against the oracle
+# ---------------------------------------------------------------------------
+def test_gradient_matches_oracle(gpu_lib):
+    rng = np.random.default_rng(0)
+    P = mo.init_params(5)
+    P[mo.OFF_B1:mo.OFF_W2] = 0.2 * rng.standard_normal(mo.HID)
+    P[mo.OFF_B2:mo.OFF_W3] = 0.2 * rng.standard_normal(mo.HID)
+    n = 1000  # not a multiple of the 16-sample tile
+    X = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    Y = rng.uniform(0, 2, n).astype(np.float32)
+    wt = np.where(rng.uniform(size=n) < 0.3, -1.0, 1.0).astype(np.float32)  # 30 % one-sided targets
+    loss, g = tlq.mlp_loss_grad(P, X, Y, wt)
+    loss_o, g_o = mo.loss_grad(P, X, Y, bf16_round=True, wt=wt)
+    assert abs(loss - loss_o) <= 1e-4 * loss_o, (loss, loss_o)
+    # per parameter block: FP32 accumulation order and rare BF16 rounding
+    # flips of intermediate values are all that separate the two
+    blocks = {"W1": (mo.OFF_W1, mo.OFF_B1), "b1": (mo.OFF_B1, mo.OFF_W2), "W2": (mo.OFF_W2, mo.OFF_B2),
+              "b2": (mo.OFF_B2, mo.OFF_W3), "W3": (mo.OFF_W3, mo.OFF_B3), "b3": (mo.OFF_B3, mo.OFF_W4),
+              "W4": (mo.OFF_W4, mo.OFF_B4), "b4": (mo.OFF_B4, mo.NPARAM)}
+    for name, (a, b) in blocks.items():
+        err = np.linalg.norm(g[a:b] - g_o[a:b]) / np.linalg.norm(g_o[a:b])
+        assert err < 1e-2, (name, err)
+    # and the unrounded FP64 gradient is close (BF16 is the only approximation)
+    _, g64 = mo.loss_grad(P, X, Y, bf16_round=False, wt=wt)
+    assert np.linalg.norm(g - g64) / np.linalg.norm(g64) < 0.05
+
+
+def test_inference_matches_oracle(gpu_lib):
+    rng = np.random.default_rng(1)
+    P = mo.init_params(6)
+    X = rng.uniform(-1, 1, (777, 3)).astype(np.float32)
+    y = tlq.mlp_infer(P, X)
+    y_o, _ = mo.forward(P, X, bf16_round=True)
+    assert np.max(np.abs(y - y_o)) <= 2e-3 * np.max(np.abs(y_o))
+
+
+def test_pairs_match_oracle_integrator(gpu_lib):
+    """y of each training pair against the C oracle's sub-cycled cooling
+    (the reference algorithm, source/cooling.f90:64-112) at sub-steps frac
+    and frac/2, extrapolated the same way."""
+    cfg, _ = problems.wind_bubble(16)
+    box = (-4.0, 4.0, 4.0, 8.5, -8.0, 1.0)
+    frac, msub = 2e-3, 20000
+    with tlq.Context(cfg) as ctx:
+        X, Y, R = ctx.cooling_pairs(96, 11, box, frac, msub)
+    assert np.all(np.isfinite(Y))
+    # stratified tau covers the box
+    assert X[:, 2].min() < -7.5 and X[:, 2].max() > 0.5
+    ocfg = tlq.Config(**{**cfg.__dict__, "nx": 2, "ny": 2, "nz": 2, "winds": [], "masses": None})
+    for q in range(0, 96, 3):
+        nd, T, Tn_gpu, dt = R[q]
+        Tn = []
+        for f in (frac, 0.5 * frac):
+            p = oracle_params(ocfg)
+            p.cooling, p.cool_sub_frac, p.cool_max_sub = O_SUBCYCLE, f, msub
+            o = Oracle(p)
+            W = o.p.zeros()
+            W[0] = nd * cfg.mu0 * problems.AMU
+            W[4] = W[0] * problems.KB * T / (cfg.mu0 * problems.AMU)
+            U = W.copy()
+            U[1:4] = 0.0
+            U[4] = W[4] / (cfg.gamma - 1.0)
+            o.cooling(W, U, dt)
+            Tn.append(W[4, 2, 2, 2] * cfg.mu0 * problems.AMU / (W[0, 2, 2, 2] * problems.KB))
+        Tex = np.exp(2 * np.log(Tn[1]) - np.log(Tn[0]))
+        Tmin = cfg.cool_T[0]
+        if Tn[1] < Tmin or Tex < Tmin:  # cooling completes: the pair lands on the table's first temperature
+            Tex = Tmin
+        assert abs(Tn_gpu - Tex) <= 1e-9 * Tex, (q, Tn_gpu, Tex)
+
+
+# ---------------------------------------------------------------------------
+# training
+# ---------------------------------------------------------------------------
+def test_training_converges(trained):
+    rep, (P, norm, box) = trained
+    assert rep["loss_last"] < 0.5 * rep["loss_first"], rep
+    # most held-out pairs pass the step's residual check (|dT|/T <= 1e-3);
+    # the rest (runaway cooling above the curve's peak) fall back
+    assert rep["val_accept"] > 0.85, rep
+    assert rep["val_p99_rel_T"] < 0.1, rep
+    assert np.all(np.isfinite(P)) and tuple(box) == (-4.0, 4.0, 4.0, 8.5, -8.0, 1.0)
+
+
+def test_trained_network_matches_oracle_forward(trained):
+    _, (P, norm, box) = trained
+    rng = np.random.default_rng(2)
+    X = rng.uniform(-1, 1, (512, 3)).astype(np.float32)
+    y = tlq.mlp_infer(P, X)
+    y_o, _ = mo.forward(P, X, bf16_round=True)
+    assert np.max(np.abs(y - y_o)) <= 2e-3 * max(1.0, np.max(np.abs(y_o)))
+
+
+# ---------------------------------------------------------------------------
+# in the step
+# ---------------------------------------------------------------------------
+def run(cfg, U0, nsteps, net=None, timing=False):
+    """nsteps steps from U0; with timing, the average device time of nsteps
+    more steps (after 2 warm-up steps) from U0 in a second context."""
+    U1 = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        if net is not None:
+            ctx.set_cooling_surrogate(*net)
+        ctx.borders(U1, 1)
+        ctx.upload(U1)
+        ctx.advance(nsteps)
+        t, it, dt, rc = ctx.time()
+        st = ctx.stats()
+        U, W = ctx.state()
+        sums = ctx.conserved_sums()
+    ms = None
+    if timing:
+        with tlq.Context(cfg) as ctx:
+            if net is not None:
+                ctx.set_cooling_surrogate(*net)
+            ctx.upload(U1)
+            ctx.advance(2)
+            ctx.enable_timing(True)
+            ctx.advance(nsteps)
+            s2 = ctx.stats()
+            ms = s2.ms_stage1 + s2.ms_stage2
+    return dict(U=U, W=W, t=t, it=it, rc=rc, sums=sums, mlp=st.cool_mlp, fb=st.cool_fallback, ms=ms)
+
+
+def test_no_network_is_an_error(gpu_lib):
+    cfg, U0 = problems.wind_bubble(16)
+    c = mixed_cfg(cfg, tlq.COOL_MLP)
+    with tlq.Context(c) as ctx:
+        ctx.upload(U0.copy(order="F"))
+        with pytest.raises(tlq.TlqError):
+            ctx.advance(1)
+    with pytest.raises(tlq.TlqError):  # the surrogate runs in the mixed step only
+        tlq.Context(tlq.Config(**{**cfg.__dict__, "cooling": tlq.COOL_MLP}))
+
+
+def test_all_fallback_is_the_sub_cycled_step(trained):
+    """A training box no cell lies in: every cooling cell falls back, and the
+    step is bit for bit the mixed step with sub-cycled cooling."""
+    _, (P, norm, box) = trained
+    cfg, U0 = problems.clumpy(32, seed=3)
+    ref = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE), U0, 5)
+    empty = np.array([9.0, 9.5, 9.0, 9.5, 9.0, 9.5])
+    got = run(mixed_cfg(cfg, tlq.COOL_MLP), U0, 5, net=(P, norm, empty))
+    assert got["rc"] == tlq.OK and got["it"] == ref["it"] == 5
+    assert got["mlp"] == 0 and got["fb"] > 0
+    np.testing.assert_array_equal(interior(got["U"]), interior(ref["U"]))
+    assert got["t"] == ref["t"]
+
+
+EXACT = dict(cool_sub_frac=2e-3, cool_max_sub=20000)  # the exact integrator: fine sub-cycling
+
+
+def test_wind_bubble_bars_with_surrogate(trained):
+    """Mixed + surrogate against the plain FP64 step, 100 steps of the 64^3
+    wind bubble: L1 density <= 1 %, total-energy drift <= 1e-6.  Both cool
+    with the exact integrator (the surrogate's fallback; the FP64 step's
+    cooling): the network reproduces that integrator, not a coarse one
+    (16 sub-steps of 0.1 tau differ from it by ~tau^2 per step)."""
+    _, net = trained
+    cfg, U0 = problems.wind_bubble(64)
+    ref = run(tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, **EXACT}), U0, 100)
+    got = run(mixed_cfg(cfg, tlq.COOL_MLP, **EXACT), U0, 100, net=net)
+    assert got["rc"] == tlq.OK and got["it"] == 100
+    err = rel_l1(interior(got["W"])[0], interior(ref["W"])[0])
+    drift = abs(got["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4])
+    frac_fb = got["fb"] / max(1, got["fb"] + got["mlp"])
+    print(f"wind64 surrogate: L1 rho {err:.3e} drift {drift:.3e} fallback {frac_fb:.4f} "
+          f"(mlp {got['mlp']}, fallback {got['fb']})")
+    assert err <= 1e-2 and drift <= 1e-6
+    assert got["mlp"] > 0
+
+
+def test_surrogate_gain_over_sub_cycling(trained):
+    """What the network gains, on a clumpy medium where cooling is stiff: the
+    step's cooling against the exact integrator (FP64 step, sub-steps of
+    2e-3 tau).  The surrogate, with the exact integrator as its fallback, is
+    more accurate than the sub-cycled integrator at a coarse setting (16
+    sub-steps of at most 0.1 tau) and faster than the sub-cycled integrator
+    made exact (2e-3 tau, up to 20000 sub-steps) everywhere."""
+    _, net = trained
+    cfg, U0 = problems.clumpy(48, seed=1)
+    n = 3
+    fine_kw = EXACT
+    exact = run(tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, **fine_kw}), U0, n)
+    coarse = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE), U0, n, timing=True)
+    fine = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE, **fine_kw), U0, n, timing=True)
+    mlp = run(mixed_cfg(cfg, tlq.COOL_MLP, **fine_kw), U0, n, net=net, timing=True)
+    # thermal energy of the cells: the cooling's footprint
+    eth = lambda r: interior(r["W"])[4]
+    e_coarse = rel_l1(eth(coarse), eth(exact))
+    e_fine = rel_l1(eth(fine), eth(exact))
+    e_mlp = rel_l1(eth(mlp), eth(exact))
+    frac_fb = mlp["fb"] / max(1, mlp["fb"] + mlp["mlp"])
+    print(f"clumpy48: L1 p err coarse {e_coarse:.3e} fine {e_fine:.3e} mlp {e_mlp:.3e}; "
+          f"ms/step coarse {coarse['ms']:.3f} fine {fine['ms']:.3f} mlp {mlp['ms']:.3f}; fallback {frac_fb:.4f}")
+    assert e_mlp < 0.5 * e_coarse
+    assert mlp["ms"] < 0.5 * fine["ms"]

@@ -30,6 +30,8 @@ UNITS = [
     ("tlq_api.cu", []),
     ("tlq_noalloc.cu", ["-fmad=false"]),
     ("tlq_mixed.cu", ["--use_fast_math"]),
+    ("tlq_mlp.cu", []),
+    ("tlq_surrogate.cu", ["--use_fast_math"]),
 ]
 
 

@@ -14,60 +14,11 @@
 #include <vector>
 
 #include "../../include/tlq.h"
-#include "tlq_internal.h"
+#include "tlq_ctx.h"
 
 using namespace tlq;
 
-struct tlq_ctx {
-  tlq_config cfg{};
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  Params P{};
-  Layout L{};
-  Aos A{};
-  // device state
-  double* U[2] = {nullptr, nullptr};
-  double* UPP = nullptr;
-  double* Pc = nullptr;   // carried pressure plane (cooling)
-  double* phi = nullptr;  // point-mass potential plane
-  float* lapf = nullptr;  // mixed form: eta * Laplacian of U between the stages
-  Clock* clk = nullptr;
-  Clock* clk_host = nullptr;  // pinned mirror
-  double* partials = nullptr;
-  int npartials = 0;
-  double* sums_partials = nullptr;
-  double* sums_out = nullptr;
-  double* staging = nullptr;  // one reference-layout array
-  // tables
-  double *dT = nullptr, *dlogT = nullptr, *dC = nullptr;
-  float *dTf = nullptr, *dlogTf = nullptr, *dCf = nullptr;
-  Wind* dwinds = nullptr;
-  double* dmasses = nullptr;
-  int nmasses = 0;
-  std::vector<double> masses_host;
-  // per-routine scratch (reference layout), allocated on first use
-  double* rb[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  double* rphi = nullptr;
-  Clock* rclk = nullptr;
-  double* rpartials = nullptr;
-  // stage launch geometry and tensor maps
-  dim3 grid{};
-  int zlen = 0;
-  CUtensorMap tm_U[2]{}, tm_UPP{}, tm_P{};
-  // run state
-  int cur = 0;  // U[cur] holds the current state
-  long long it_base = 0;
-  bool uploaded = false;
-  double t0 = 0.0;
-  int it0 = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  bool timing = false;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  double ms1_acc = 0.0, ms2_acc = 0.0;
-  long long ntimed = 0;
-  long long steps = 0;
-  std::string err;
-};
+
 
 namespace {
 
@@ -126,12 +77,17 @@ int validate(const tlq_config* c, std::string& why) {
   if (c->solver != TLQ_SOLVER_HLLC && c->solver != TLQ_SOLVER_HLL) { why = "unknown solver"; return TLQ_ERR_CONFIG; }
   for (int q = 0; q < 6; ++q)
     if (c->bc[q] < TLQ_BC_OUTFLOW || c->bc[q] > TLQ_BC_INFLOW) { why = "unknown boundary kind"; return TLQ_ERR_CONFIG; }
-  if (c->cooling < TLQ_COOL_NONE || c->cooling > TLQ_COOL_SUBCYCLE) { why = "unknown cooling mode"; return TLQ_ERR_CONFIG; }
-  if (c->cooling == TLQ_COOL_SUBCYCLE && (c->cool_max_sub < 1 || !(c->cool_sub_frac > 0.0))) {
-    why = "sub-cycled cooling needs cool_max_sub >= 1 and cool_sub_frac > 0";
+  if (c->cooling < TLQ_COOL_NONE || c->cooling > TLQ_COOL_MLP) { why = "unknown cooling mode"; return TLQ_ERR_CONFIG; }
+  if ((c->cooling == TLQ_COOL_SUBCYCLE || c->cooling == TLQ_COOL_MLP) &&
+      (c->cool_max_sub < 1 || !(c->cool_sub_frac > 0.0))) {
+    why = "sub-cycled cooling (and the surrogate's fallback) needs cool_max_sub >= 1 and cool_sub_frac > 0";
     return TLQ_ERR_CONFIG;
   }
   if (c->precision != TLQ_PREC_FP64 && c->precision != TLQ_PREC_MIXED) { why = "unknown precision"; return TLQ_ERR_CONFIG; }
+  if (c->cooling == TLQ_COOL_MLP && c->precision != TLQ_PREC_MIXED) {
+    why = "the cooling surrogate runs in the mixed-precision step";
+    return TLQ_ERR_CONFIG;
+  }
   for (int q = 0; q < 6; ++q)
     if (c->bc[q] == TLQ_BC_INFLOW) { why = "inflow boundaries are an empty stub in the reference"; return TLQ_ERR_CONFIG; }
   return TLQ_OK;
@@ -214,6 +170,11 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
     CK(launch_stage_mixed(2, ctx->tm_UPP, a, ctx->grid, ctx->stream));
   else
     CK(launch_stage(2, ctx->cfg.precision, ctx->tm_UPP, ctx->tm_P, a, ctx->grid, ctx->stream));
+  // surrogate cooling + the dt reduction (stage 2 leaves both to it)
+  if (ctx->cfg.cooling == TLQ_COOL_MLP)
+    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[par ^ 1], ctx->clk, ctx->partials, ctx->mlp_params, ctx->mlp_norm,
+                          ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts, ctx->mlp_queue, ctx->mlp_qcount,
+                          ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
   return TLQ_OK;
 }
@@ -232,6 +193,8 @@ int build_graph(tlq_ctx* ctx, int par) {
 }
 
 int run_steps(tlq_ctx* ctx, int n) {
+  if (ctx->cfg.cooling == TLQ_COOL_MLP && !ctx->mlp_ready)
+    return fail(ctx, TLQ_ERR_STATE, "surrogate cooling on but no network (train or set one first)");
   for (int q = 0; q < n; ++q) {
     const int par = ctx->cur;
     if (ctx->timing) {
@@ -346,6 +309,12 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
     if (cudaMalloc(&ctx->lapf, (size_t)L.plane * 5 * sizeof(float))) return bail(TLQ_ERR_NOMEM);
     cudaMemset(ctx->lapf, 0, (size_t)L.plane * 5 * sizeof(float));
   }
+  if (cfg->cooling == TLQ_COOL_MLP) {
+    const size_t ncell = (size_t)cfg->nx * cfg->ny * cfg->nz;
+    if (cudaMalloc(&ctx->mlp_queue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_qcount, sizeof(unsigned)))
+      return bail(TLQ_ERR_NOMEM);
+    cudaMemset(ctx->mlp_qcount, 0, sizeof(unsigned));
+  }
   if (cudaMalloc(&ctx->clk, sizeof(Clock)) || cudaMallocHost(&ctx->clk_host, sizeof(Clock))) return bail(TLQ_ERR_NOMEM);
   std::memset(ctx->clk_host, 0, sizeof(Clock));
   ctx->clk_host->tfin = std::numeric_limits<double>::infinity();
@@ -357,7 +326,8 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   ctx->grid = dim3(gx, gy, gz);
   ctx->npartials = gx * gy * gz;
   const int nb = init_blocks(ctx->P);
-  if (cudaMalloc(&ctx->partials, sizeof(double) * 3 * (size_t)std::max(ctx->npartials, nb)) ||
+  const int npart = std::max(std::max(ctx->npartials, nb), cool_mlp_blocks(ctx->P));
+  if (cudaMalloc(&ctx->partials, sizeof(double) * 3 * (size_t)npart) ||
       cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
     return bail(TLQ_ERR_NOMEM);
   if (prepare_stage_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
@@ -381,6 +351,8 @@ int tlq_destroy(tlq_ctx* ctx) {
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
+  cudaFree(ctx->mlp_params); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
+  cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_qcount);
   cudaFree(ctx->clk); cudaFree(ctx->partials); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);
@@ -440,6 +412,8 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int
   CK(cudaMemcpy(ctx->dlogTf, flt.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->dCf, fC.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   ctx->P.cool = CoolTable{ctx->dT, ctx->dlogT, ctx->dC, n, ctx->dTf, ctx->dlogTf, ctx->dCf};
+  const int rs = tlq_surrogate_prepare_table(ctx, T, logL, n);
+  if (rs != TLQ_OK) return rs;
   invalidate_graphs(ctx);
   return TLQ_OK;
 }
@@ -511,6 +485,7 @@ int tlq_set_time(tlq_ctx* ctx, double t, int it) {
 int tlq_upload(tlq_ctx* ctx, const double* U) {
   if (!ctx || !U) return TLQ_ERR_ARG;
   if (ctx->cfg.cooling != TLQ_COOL_NONE && !ctx->dT) return fail(ctx, TLQ_ERR_STATE, "cooling on but no cooling table");
+  if (ctx->cool_counts) CK(cudaMemsetAsync(ctx->cool_counts, 0, 2 * sizeof(unsigned long long), ctx->stream));
   CK(cudaMemcpyAsync(ctx->staging, U, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
   CK(launch_aos_to_soa(ctx->A, ctx->L, ctx->staging, ctx->U[0], ctx->stream));
   Clock c{};
@@ -625,6 +600,13 @@ int tlq_stats_get(tlq_ctx* ctx, tlq_stats* s) {
   s->ms_stage1 = ctx->ntimed ? ctx->ms1_acc / ctx->ntimed : 0.0;
   s->ms_stage2 = ctx->ntimed ? ctx->ms2_acc / ctx->ntimed : 0.0;
   s->bytes_state = (double)ctx->L.plane * 8.0 * 17.0;
+  if (ctx->cool_counts) {
+    unsigned long long cc[2] = {0, 0};
+    CK(cudaMemcpyAsync(cc, ctx->cool_counts, sizeof(cc), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    s->cool_mlp = (long long)cc[0];
+    s->cool_fallback = (long long)cc[1];
+  }
   return TLQ_OK;
 }
 

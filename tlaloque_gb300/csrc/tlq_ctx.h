@@ -1,0 +1,76 @@
+// tlq_ctx.h -- the context behind tlq_ctx* (private to libtlq's host code).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/tlq.h"
+#include "tlq_internal.h"
+
+using namespace tlq;
+
+struct tlq_ctx {
+  tlq_config cfg{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Params P{};
+  Layout L{};
+  Aos A{};
+  // device state
+  double* U[2] = {nullptr, nullptr};
+  double* UPP = nullptr;
+  double* Pc = nullptr;   // carried pressure plane (cooling)
+  double* phi = nullptr;  // point-mass potential plane
+  float* lapf = nullptr;  // mixed form: eta * Laplacian of U between the stages
+  Clock* clk = nullptr;
+  Clock* clk_host = nullptr;  // pinned mirror
+  double* partials = nullptr;
+  int npartials = 0;
+  double* sums_partials = nullptr;
+  double* sums_out = nullptr;
+  double* staging = nullptr;  // one reference-layout array
+  // tables
+  double *dT = nullptr, *dlogT = nullptr, *dC = nullptr;
+  float *dTf = nullptr, *dlogTf = nullptr, *dCf = nullptr;
+  Wind* dwinds = nullptr;
+  double* dmasses = nullptr;
+  int nmasses = 0;
+  std::vector<double> masses_host;
+  // per-routine scratch (reference layout), allocated on first use
+  double* rb[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double* rphi = nullptr;
+  Clock* rclk = nullptr;
+  double* rpartials = nullptr;
+  // stage launch geometry and tensor maps
+  dim3 grid{};
+  int zlen = 0;
+  CUtensorMap tm_U[2]{}, tm_UPP{}, tm_P{};
+  // run state
+  int cur = 0;  // U[cur] holds the current state
+  long long it_base = 0;
+  bool uploaded = false;
+  double t0 = 0.0;
+  int it0 = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  double ms1_acc = 0.0, ms2_acc = 0.0;
+  long long ntimed = 0;
+  long long steps = 0;
+  // learned cooling surrogate (TLQ_COOL_MLP)
+  float* mlp_params = nullptr;             // FP32 master parameters (device)
+  float mlp_norm[6] = {0, 1, 0, 1, 0, 1};  // feature centres and half-widths
+  double mlp_box[6] = {0, 0, 0, 0, 0, 0};  // training box of the features (the hull)
+  bool mlp_ready = false;
+  float* gcum = nullptr;                   // closed-form cooling-time integral at the table nodes
+  float* gslope = nullptr;                 // per-segment power-law slopes
+  unsigned long long* cool_counts = nullptr;  // device: cells cooled by the network / by the fallback
+  double cool_tmin = 0.0;                  // the table's first temperature
+  unsigned* mlp_queue = nullptr;           // cells handed to the exact integrator (capacity nx ny nz)
+  unsigned* mlp_qcount = nullptr;          // their number (zero between steps)
+  std::string err;
+};
+
+// Closed-form cooling-time integral of the table for the surrogate's
+// residual check (tlq_surrogate.cu); called by tlq_set_cooling_table.
+int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* logL, int n);

@@ -122,16 +122,19 @@ __device__ __forceinline__ void block_max3(double& a, double& b, double& c, doub
   }
 }
 
+// nprev: block maxima an earlier kernel of the same step left in
+// partials[0 .. 3 nprev); this grid's go after them and the last block
+// reduces both.
 template <int NTHREADS>
 __device__ void cfl_reduce_finalize(double a, double b, double c, double* partials, Clock* clk, const Params& p,
-                                    bool advance, double* red, int* s_flag) {
+                                    bool advance, double* red, int* s_flag, unsigned nprev = 0) {
   const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
   const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   block_max3<NTHREADS>(a, b, c, red);
   if (threadIdx.x == 0) {
-    partials[3 * bid + 0] = a;
-    partials[3 * bid + 1] = b;
-    partials[3 * bid + 2] = c;
+    partials[3 * (nprev + bid) + 0] = a;
+    partials[3 * (nprev + bid) + 1] = b;
+    partials[3 * (nprev + bid) + 2] = c;
     __threadfence();
     const unsigned t = atomicAdd(&clk->ticket, 1u);
     *s_flag = (t == nblocks - 1);
@@ -140,7 +143,7 @@ __device__ void cfl_reduce_finalize(double a, double b, double c, double* partia
   if (!*s_flag) return;
   __threadfence();
   a = b = c = 0.0;
-  for (unsigned q = threadIdx.x; q < nblocks; q += NTHREADS) {
+  for (unsigned q = threadIdx.x; q < nprev + nblocks; q += NTHREADS) {
     a = max_nan(a, ld_cg(partials + 3 * q + 0));
     b = max_nan(b, ld_cg(partials + 3 * q + 1));
     c = max_nan(c, ld_cg(partials + 3 * q + 2));

@@ -57,6 +57,28 @@ cudaError_t launch_point_potential_soa(const Params& p, const Layout& L, const d
 cudaError_t launch_conserved_sums(const Params& p, const Layout& L, const double* U, double* partials, int nblocks,
                                   double* out5, cudaStream_t s);
 
+// Cooling surrogate (tlq_mlp.cu).
+size_t mlp_train_smem();
+cudaError_t launch_mlp_grad(const float* P, const float* X, const float* Y, const float* Wt, int nb, float* grad,
+                            float* loss, int nblocks, cudaStream_t s);
+cudaError_t launch_adam(float* P, float* m, float* v, const float* grad, int n, float lr, float b1, float b2,
+                        float eps, int t, cudaStream_t s);
+cudaError_t launch_mlp_infer(const float* P, const float* X, int n, float* Y, cudaStream_t s);
+cudaError_t launch_cool_pairs(const Params& p, long long N, unsigned long long seed, const double box[6], float* X,
+                              float* Y, float* Wt, double* raw, cudaStream_t s);
+cudaError_t launch_gather_pairs(const float* X, const float* Y, const float* Wt, const long long* perm, long long N,
+                                float* X2, float* Y2, float* Wt2, cudaStream_t s);
+cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStream_t s);
+// Surrogate cooling + dt reduction of the mixed step (tlq_surrogate.cu).
+// The network's pass queues the cells it hands to the exact integrator
+// (queue: capacity nx ny nz; qcount: zero between steps); the fallback pass
+// cools them and finishes the dt reduction over both passes' block maxima.
+cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Clock* clk, double* partials,
+                               const float* P, const float norm[6], const double box[6], const float* gcum,
+                               const float* gslope, unsigned long long* counts, unsigned* queue, unsigned* qcount,
+                               cudaStream_t s);
+int cool_mlp_blocks(const Params& p);  // block maxima both passes leave in partials
+
 // log10 of a small device array in place (cooling-table temperatures).
 cudaError_t launch_log10_inplace(double* v, int n, cudaStream_t s);
 

@@ -24,7 +24,7 @@ constexpr int BC_OUTFLOW = 1, BC_REFLECTIVE = 2, BC_PERIODIC = 3, BC_INFLOW = 4;
 constexpr int LIM_NONE = 1, LIM_VANLEER = 2, LIM_MINMOD = 3, LIM_UMIST = 4, LIM_WOODWARD = 5,
               LIM_SUPERBEE = 6;
 constexpr int SOLVER_HLLC = 0, SOLVER_HLL = 1;
-constexpr int COOL_NONE = 0, COOL_REF = 1, COOL_SUBCYCLE = 2;
+constexpr int COOL_NONE = 0, COOL_REF = 1, COOL_SUBCYCLE = 2, COOL_MLP = 3;
 
 // Fortran MIN/MAX of two reals (no NaN or signed-zero tie matters for valid
 // states); SIGN(1.0, a) with gfortran's default signed-zero semantics.

@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(NT, 3)
         for (int e = 0; e < 5; ++e) un[e] = up[e] + f2d(lv[e]);
         float cf[5], w[5];
         mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
-        if (p.cooling != COOL_NONE) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
+        if (p.cooling != COOL_NONE && p.cooling != COOL_MLP) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
         if (!(un[0] > 0.0)) atomicOr(&clk->status, ST_NEG_DENSITY);
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
@@ -418,7 +418,8 @@ __global__ void __launch_bounds__(NT, 3)
     }
     d0 = d1 = d2 = NAN;
   }
-  if (STAGE == 2) cfl_reduce_finalize<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag);
+  // with the surrogate, cooling and the dt reduction follow in their own kernel
+  if (STAGE == 2 && p.cooling != COOL_MLP) cfl_reduce_finalize<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag);
 }
 
 }  // namespace tlq

@@ -1,0 +1,594 @@
+// tlq_surrogate.cu -- the learned cooling surrogate in the step (mixed form,
+// TLQ_COOL_MLP) and its training driver.
+//
+// In the step, stage 2 leaves cooling and the CFL reduction to
+// k_cool_mlp_dt: for each interior cell that cools (temp >= the table's
+// first temperature, cooling.f90:71), the network predicts
+// y = -ln(T_new/T)/tau from (log10 n, log10 T, log10 tau); the prediction is
+// accepted when the cell lies inside the training box and
+// |T_pred - T_int| <= 1e-3 T, T_int the closed-form solution of
+// dT/dt = -(gamma-1) n Lambda(T)/k_B for the piecewise power-law table
+// (Townsend 2009, ApJS 181, 391: exact integration of a power-law cooling
+// function); otherwise the cell is cooled by the sub-cycled integrator.
+// Built with --use_fast_math (FP32 part of the mixed form).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+
+#include "tlq_ctx.h"
+#include "tlq_mlp.cuh"
+#include "tlq_stage_mixed.cuh"
+
+namespace tlq {
+namespace {
+
+struct SurrogateArgs {
+  const float* P;       // FP32 network parameters
+  float norm[6];        // centre, half-width per feature
+  float box[6];         // training box (lo, hi per feature)
+  const float* gcum;    // closed-form integral at the table nodes
+  const float* gslope;  // per-segment power-law slope
+  unsigned long long* counts;
+};
+
+// Table segment of T >= T_0: i with T_i <= T < T_{i+1}, n-1 above the last node.
+__device__ __forceinline__ int seg_of(const CoolTable& t, float T) {
+  int lo = 1, hi = t.n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (t.Tf[mid] > T) hi = mid; else lo = mid + 1;
+  }
+  return lo - 1;
+}
+
+// G(T) = int_{T_0}^{T} dT'/Lambda(T') for the log-linear table.
+__device__ __forceinline__ float g_of(const CoolTable& t, const SurrogateArgs& sa, float T) {
+  const int i = seg_of(t, T);
+  const float Ti = t.Tf[i], Li = exp10f(t.Cf[i]);
+  if (i >= t.n - 1) return sa.gcum[t.n - 1] + (T - Ti) / Li;
+  const float a = 1.0f - sa.gslope[i];
+  const float r = T / Ti;
+  const float part = fabsf(a) < 1e-4f ? (Ti / Li) * __logf(r) : (Ti / Li) * (__powf(r, a) - 1.0f) / a;
+  return sa.gcum[i] + part;
+}
+
+// Inverse of G for G >= 0.
+__device__ __forceinline__ float g_inv(const CoolTable& t, const SurrogateArgs& sa, float G) {
+  int lo = 1, hi = t.n;  // first node with gcum > G
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (sa.gcum[mid] > G) hi = mid; else lo = mid + 1;
+  }
+  const int j = lo - 1;
+  const float Tj = t.Tf[j], Lj = exp10f(t.Cf[j]);
+  if (j >= t.n - 1) return Tj + (G - sa.gcum[t.n - 1]) * Lj;
+  const float a = 1.0f - sa.gslope[j];
+  const float q = (G - sa.gcum[j]) * Lj / Tj;
+  return fabsf(a) < 1e-4f ? Tj * __expf(q) : Tj * __powf(fmaxf(1.0f + a * q, 0.0f), 1.0f / a);
+}
+
+constexpr int CT = 128;   // threads per block of the network pass
+constexpr int FT = 128;   // threads per block of the fallback pass
+constexpr int FB = 152 * 4;  // blocks of the fallback pass
+
+__device__ __forceinline__ void speeds_max(const float* w, float gf, float& m0, float& m1, float& m2) {
+  const float cs = sqrtf(gf * w[4] / w[0]);
+  const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
+  m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
+  m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
+  m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
+}
+
+__device__ __forceinline__ long long interior_offset(const Params& p, const Layout& L, long long cidx) {
+  const int i = 1 + (int)(cidx % p.nx);
+  const long long r = cidx / p.nx;
+  const int j = 1 + (int)(r % p.ny);
+  const int k = 1 + (int)(r / p.ny);
+  return L.at(i, j, k);
+}
+
+// Pass 1: for every interior cell, the network's prediction where the cell
+// cools and lies in the training box, accepted when the residual check
+// passes; the other cooling cells are queued for the exact integrator, and
+// so are the cells whose cooling reaches the table's first temperature
+// within the step (closed form: G_t <= 0): there the reference integrator's
+// last sub-step decides how far below that temperature the cell ends.  The
+// block maxima of the signal speeds of all cells not queued go to
+// partials[0 .. 3 gridDim.x).
+__global__ void __launch_bounds__(CT) k_cool_mlp(Params p, Layout L, double* __restrict__ U, const Clock* clk,
+                                                 double* partials, SurrogateArgs sa, unsigned* __restrict__ queue,
+                                                 unsigned* qcount) {
+  __shared__ mlp::SmemWeights W;
+  __shared__ double red[96];
+  if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
+  mlp::load_weights(sa.P, W, nullptr);
+  __syncthreads();
+  const CoolTable& tab = p.cool;
+  const float gm1 = (float)p.gamma - 1.0f, gf = (float)p.gamma;
+  const float cT = (float)(p.mu0 * AMU / KB);
+  const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
+  const float dtf = (float)clk->dt;
+  const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+  const long long n = (long long)p.nx * p.ny * p.nz;
+  float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+  unsigned long long used = 0, fell = 0;
+  for (long long base = (long long)blockIdx.x * CT; base < n; base += (long long)gridDim.x * CT) {
+    const long long cidx = base + threadIdx.x;
+    const bool valid = cidx < n;
+    long long o = 0;
+    double u[5] = {1.0, 0.0, 0.0, 0.0, 1.0};
+    if (valid) {
+      o = interior_offset(p, L, cidx);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
+    }
+    float cf[5], w[5];
+    mixed_cell(gm1, u, 1, cf, w);
+    const float T = (w[4] / w[0]) * cT;
+    const bool need = valid && cools_at(p, T, u);
+    float feat[3] = {0.f, 0.f, 0.f}, tau = 0.f;
+    bool inbox = false;
+    if (need) {
+      const float nd = w[0] * inv_muamu;
+      const float eth = w[4] / gm1;
+      const float lam = cool_coef_f(tab, T);
+      tau = (lam * nd) * (nd / eth) * dtf;
+      const float f0 = log10f(nd), f1 = log10f(T), f2 = log10f(tau);
+      // inclusive, with 1e-4 dex of slack for the FP32 logarithms of cells on
+      // a face of the box (e.g. a medium at the table's first temperature)
+      constexpr float SL = 1e-4f;
+      inbox = f0 >= sa.box[0] - SL && f0 <= sa.box[1] + SL && f1 >= sa.box[2] - SL && f1 <= sa.box[3] + SL &&
+              f2 >= sa.box[4] - SL && f2 <= sa.box[5] + SL;
+      feat[0] = (f0 - sa.norm[0]) / sa.norm[1];
+      feat[1] = (f1 - sa.norm[2]) / sa.norm[3];
+      feat[2] = (f2 - sa.norm[4]) / sa.norm[5];
+    }
+    const bool run = need && inbox;
+    float y = 0.f;
+    if (__ballot_sync(0xffffffffu, run)) {
+      // the warp's 32 cells as two m16 tiles (rows = lanes 0-15, 16-31)
+      float yt[2][2];
+#pragma unroll 1
+      for (int tsel = 0; tsel < 2; ++tsel) {
+        float xg[3], xg8[3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          xg[f] = __shfl_sync(0xffffffffu, feat[f], 16 * tsel + g);
+          xg8[f] = __shfl_sync(0xffffffffu, feat[f], 16 * tsel + g + 8);
+        }
+        mlp::forward_tile(W, xg, xg8, g, tig, yt[tsel]);
+      }
+      const int row = lane & 15, src = 4 * (row & 7);
+      const float a0 = __shfl_sync(0xffffffffu, yt[0][0], src), a1 = __shfl_sync(0xffffffffu, yt[0][1], src);
+      const float b0 = __shfl_sync(0xffffffffu, yt[1][0], src), b1 = __shfl_sync(0xffffffffu, yt[1][1], src);
+      y = (lane < 16) ? (row < 8 ? a0 : a1) : (row < 8 ? b0 : b1);
+    }
+    bool ok = false;
+    if (run) {
+      const float lam = cool_coef_f(tab, T);
+      const float Gt = g_of(tab, sa, T) - tau * T / lam;  // budget (gamma-1) n dt / k_B = tau T / Lambda(T)
+      if (Gt > 0.0f) {
+        const float Tint = g_inv(tab, sa, Gt);
+        // the network's r: ln(T_new/T) = -(tau + tau^2 r); q = T_new/T - 1
+        // without cancellation, clamped at the table's first temperature
+        const float q = fmaxf(expm1f(-(1.0f + tau * y) * tau), tab.Tf[0] / T - 1.0f);
+        ok = fabsf(T * q - (Tint - T)) <= 1e-3f * T;
+        if (ok) {
+          const float dp = w[4] * q;
+          w[4] = w[4] + dp;
+          U[4 * L.plane + o] = u[4] + f2d(dp / gm1);
+        }
+      }
+    }
+    const bool queued = need && !ok;
+    // warp-aggregated append to the fallback queue
+    const unsigned qm = __ballot_sync(0xffffffffu, queued);
+    if (qm) {
+      unsigned basei = 0;
+      if (lane == 0) basei = atomicAdd(qcount, (unsigned)__popc(qm));
+      basei = __shfl_sync(0xffffffffu, basei, 0);
+      if (queued) queue[basei + __popc(qm & ((1u << lane) - 1u))] = (unsigned)cidx;
+    }
+    used += ok ? 1 : 0;
+    fell += queued ? 1 : 0;
+    if (valid && !queued) speeds_max(w, gf, m0, m1, m2);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    used += __shfl_xor_sync(0xffffffffu, used, off);
+    fell += __shfl_xor_sync(0xffffffffu, fell, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&sa.counts[0], used);
+    atomicAdd(&sa.counts[1], fell);
+  }
+  double a = f2d(m0), b = f2d(m1), c = f2d(m2);
+  block_max3<CT>(a, b, c, red);
+  if (threadIdx.x == 0) {
+    partials[3 * blockIdx.x + 0] = a;
+    partials[3 * blockIdx.x + 1] = b;
+    partials[3 * blockIdx.x + 2] = c;
+  }
+}
+
+// Pass 2: the queued cells through the exact integrator (the sub-cycled
+// cooling with the run's sub-step settings), then the dt reduction over the
+// block maxima of both passes; the last block empties the queue.
+__global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, double* __restrict__ U, Clock* clk,
+                                                         double* partials, unsigned npass1,
+                                                         const unsigned* __restrict__ queue, unsigned* qcount) {
+  __shared__ double red[96];
+  __shared__ int flag;
+  if (!(clk->t < clk->tfin)) return;
+  const unsigned nq = *qcount;
+  const float gm1 = (float)p.gamma - 1.0f, gf = (float)p.gamma;
+  const float cT = (float)(p.mu0 * AMU / KB);
+  const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
+  const float dtf = (float)clk->dt;
+  float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+  for (unsigned q = blockIdx.x * FT + threadIdx.x; q < nq; q += gridDim.x * FT) {
+    const long long o = interior_offset(p, L, (long long)queue[q]);
+    double u[5];
+#pragma unroll
+    for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
+    float cf[5], w[5];
+    mixed_cell(gm1, u, 1, cf, w);
+    cool_cell_f(p, cT, inv_muamu, gm1, w, u[4], dtf, u);
+    U[4 * L.plane + o] = u[4];
+    speeds_max(w, gf, m0, m1, m2);
+  }
+  cfl_reduce_finalize<FT>(f2d(m0), f2d(m1), f2d(m2), partials, clk, p, true, red, &flag, npass1);
+  if (flag && threadIdx.x == 0) *qcount = 0u;
+}
+
+int cool_blocks(const Params& p) {
+  const long long n = (long long)p.nx * p.ny * p.nz;
+  return (int)std::max<long long>(1, std::min<long long>((n + CT - 1) / CT, 152LL * 8));
+}
+
+}  // namespace
+
+cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Clock* clk, double* partials,
+                               const float* P, const float norm[6], const double box[6], const float* gcum,
+                               const float* gslope, unsigned long long* counts, unsigned* queue, unsigned* qcount,
+                               cudaStream_t s) {
+  // the fallback is the sub-cycled integrator with the run's sub-step settings
+  Params pf = p;
+  pf.cooling = COOL_SUBCYCLE;
+  SurrogateArgs sa{};
+  sa.P = P;
+  for (int q = 0; q < 6; ++q) {
+    sa.norm[q] = norm[q];
+    sa.box[q] = (float)box[q];
+  }
+  sa.gcum = gcum;
+  sa.gslope = gslope;
+  sa.counts = counts;
+  const int nb1 = cool_blocks(p);
+  k_cool_mlp<<<nb1, CT, 0, s>>>(pf, L, U, clk, partials, sa, queue, qcount);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cool_fallback_dt<<<FB, FT, 0, s>>>(pf, L, U, clk, partials, (unsigned)nb1, queue, qcount);
+  return cudaGetLastError();
+}
+
+int cool_mlp_blocks(const Params& p) { return cool_blocks(p) + FB; }
+
+}  // namespace tlq
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+namespace {
+
+int sfail(tlq_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+
+#define SCK(call)                                                                                  \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return sfail(ctx, TLQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Parameters of the exact integrator (the context's physics and table,
+// sub-cycled with the given sub-steps).
+Params exact_params(const tlq_ctx* ctx, double sub_frac, int max_sub) {
+  Params p = ctx->P;
+  p.cooling = COOL_SUBCYCLE;
+  p.cool_sub_frac = sub_frac;
+  p.cool_max_sub = max_sub;
+  return p;
+}
+
+// Initial parameters: uniform(-a, a) with a = sqrt(6/(fan_in + fan_out)).
+void init_params(std::vector<float>& P, unsigned long long seed) {
+  using namespace tlq::mlp;
+  std::mt19937_64 rng(seed ^ 0x5eedULL);
+  auto fill = [&](int off, int fo, int fi) {
+    const float a = std::sqrt(6.0f / (float)(fi + fo));
+    std::uniform_real_distribution<float> d(-a, a);
+    for (int q = 0; q < fo * fi; ++q) P[off + q] = d(rng);
+  };
+  std::fill(P.begin(), P.end(), 0.0f);
+  fill(OFF_W1, HID, IN);
+  fill(OFF_W2, HID, HID);
+  fill(OFF_W3, HID, HID);
+  fill(OFF_W4, 1, HID);
+  P[OFF_B4] = 0.0f;
+}
+
+}  // namespace
+
+// Closed-form integral of 1/Lambda over the table (FP64), for the residual check.
+int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* logL, int n) {
+  ctx->cool_tmin = T[0];
+  std::vector<float> gc(n), sl(n);
+  double acc = 0.0;
+  for (int i = 0; i < n; ++i) {
+    gc[i] = (float)acc;
+    if (i + 1 < n) {
+      const double s = (logL[i + 1] - logL[i]) / (std::log10(T[i + 1]) - std::log10(T[i]));
+      sl[i] = (float)s;
+      const double Li = std::pow(10.0, logL[i]), a = 1.0 - s, r = T[i + 1] / T[i];
+      acc += std::fabs(a) < 1e-12 ? (T[i] / Li) * std::log(r) : (T[i] / Li) * (std::pow(r, a) - 1.0) / a;
+    } else {
+      sl[i] = 0.0f;
+    }
+  }
+  cudaFree(ctx->gcum);
+  cudaFree(ctx->gslope);
+  ctx->gcum = ctx->gslope = nullptr;
+  SCK(cudaMalloc(&ctx->gcum, n * sizeof(float)));
+  SCK(cudaMalloc(&ctx->gslope, n * sizeof(float)));
+  SCK(cudaMemcpy(ctx->gcum, gc.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  SCK(cudaMemcpy(ctx->gslope, sl.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  if (!ctx->cool_counts) {
+    SCK(cudaMalloc(&ctx->cool_counts, 2 * sizeof(unsigned long long)));
+    SCK(cudaMemset(ctx->cool_counts, 0, 2 * sizeof(unsigned long long)));
+  }
+  return TLQ_OK;
+}
+
+extern "C" {
+
+void tlq_surrogate_opts_default(tlq_surrogate_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->nsamples = 20000000LL;
+  o->epochs = 30;
+  o->batch = 4096;
+  o->lr = 3e-3f;
+  o->seed = 12345ULL;
+  const double box[6] = {-4.0, 4.0, 4.0, 8.5, -8.0, 1.0};
+  for (int q = 0; q < 6; ++q) o->box[q] = box[q];
+  o->sub_frac = 2e-3;
+  o->max_sub = 20000;
+}
+
+int tlq_cooling_pairs(tlq_ctx* ctx, long long n, unsigned long long seed, const double* box6, double sub_frac,
+                      int max_sub, float* X, float* Y, double* raw) {
+  if (!ctx || n <= 0 || !box6 || !X || !Y || !(sub_frac > 0.0) || max_sub < 1) return TLQ_ERR_ARG;
+  if (!ctx->dT) return sfail(ctx, TLQ_ERR_STATE, "cooling table not set");
+  float *dX = nullptr, *dY = nullptr;
+  double* dR = nullptr;
+  SCK(cudaMalloc(&dX, 3 * n * sizeof(float)));
+  SCK(cudaMalloc(&dY, n * sizeof(float)));
+  if (raw) SCK(cudaMalloc(&dR, 4 * n * sizeof(double)));
+  const Params p = exact_params(ctx, sub_frac, max_sub);
+  cudaError_t e = launch_cool_pairs(p, n, seed, box6, dX, dY, nullptr, dR, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(X, dX, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Y, dY, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess && raw) e = cudaMemcpyAsync(raw, dR, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dX);
+  cudaFree(dY);
+  cudaFree(dR);
+  if (e != cudaSuccess) return sfail(ctx, TLQ_ERR_CUDA, std::string("cooling pairs: ") + cudaGetErrorString(e));
+  return TLQ_OK;
+}
+
+int tlq_train_cooling_surrogate(tlq_ctx* ctx, const tlq_surrogate_opts* opts, tlq_surrogate_report* rep) {
+  using namespace tlq::mlp;
+  if (!ctx) return TLQ_ERR_ARG;
+  tlq_surrogate_opts o;
+  if (opts) o = *opts; else tlq_surrogate_opts_default(&o);
+  if (o.nsamples < 2 * o.batch || o.batch < 16 || o.epochs < 1) return sfail(ctx, TLQ_ERR_ARG, "bad training options");
+  if (!ctx->dT) return sfail(ctx, TLQ_ERR_STATE, "cooling table not set");
+  const long long N = o.nsamples;
+  const long long Nval = std::max<long long>(o.batch, N / 100);
+  const long long Ntr = N - Nval;
+  float norm[6];
+  for (int q = 0; q < 3; ++q) {
+    norm[2 * q] = (float)(0.5 * (o.box[2 * q] + o.box[2 * q + 1]));
+    norm[2 * q + 1] = (float)(0.5 * (o.box[2 * q + 1] - o.box[2 * q]));
+  }
+  cudaStream_t s = ctx->stream;
+  float *X = nullptr, *Y = nullptr, *X2 = nullptr, *Y2 = nullptr, *P = nullptr, *m = nullptr, *v = nullptr,
+        *grad = nullptr, *loss = nullptr, *Yp = nullptr, *Wt = nullptr, *Wt2 = nullptr;
+  long long* perm = nullptr;
+  int rc = TLQ_OK;
+  auto t0 = std::chrono::steady_clock::now();
+  auto cleanup = [&]() {
+    cudaFree(X); cudaFree(Y); cudaFree(X2); cudaFree(Y2); cudaFree(m); cudaFree(v); cudaFree(grad);
+    cudaFree(Wt); cudaFree(Wt2);
+    cudaFree(loss); cudaFree(Yp); cudaFree(perm);
+  };
+#define TCK(call)                                                                              \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      cleanup();                                                                               \
+      cudaFree(P);                                                                             \
+      return sfail(ctx, TLQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+    }                                                                                          \
+  } while (0)
+  TCK(cudaMalloc(&X, 3 * N * sizeof(float)));
+  TCK(cudaMalloc(&Y, N * sizeof(float)));
+  TCK(cudaMalloc(&X2, 3 * N * sizeof(float)));
+  TCK(cudaMalloc(&Y2, N * sizeof(float)));
+  TCK(cudaMalloc(&Wt, N * sizeof(float)));
+  TCK(cudaMalloc(&Wt2, N * sizeof(float)));
+  TCK(cudaMalloc(&perm, N * sizeof(long long)));
+  TCK(cudaMalloc(&P, NPARAM * sizeof(float)));
+  TCK(cudaMalloc(&m, NPARAM * sizeof(float)));
+  TCK(cudaMalloc(&v, NPARAM * sizeof(float)));
+  TCK(cudaMalloc(&grad, NPARAM * sizeof(float)));
+  TCK(cudaMalloc(&loss, sizeof(float)));
+  TCK(cudaMalloc(&Yp, Nval * sizeof(float)));
+  // pairs (stratified in tau), shuffled, normalised
+  const Params pe = exact_params(ctx, o.sub_frac, o.max_sub);
+  TCK(launch_cool_pairs(pe, N, o.seed, o.box, X, Y, Wt, nullptr, s));
+  {
+    std::vector<long long> hp(N);
+    std::iota(hp.begin(), hp.end(), 0LL);
+    std::mt19937_64 rng(o.seed * 2654435761ULL + 7);
+    std::shuffle(hp.begin(), hp.end(), rng);
+    TCK(cudaMemcpyAsync(perm, hp.data(), N * sizeof(long long), cudaMemcpyHostToDevice, s));
+    TCK(launch_gather_pairs(X, Y, Wt, perm, N, X2, Y2, Wt2, s));
+    TCK(cudaStreamSynchronize(s));
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  TCK(launch_normalise(X2, N, norm, s));
+  std::vector<float> hP(NPARAM);
+  init_params(hP, o.seed);
+  TCK(cudaMemcpyAsync(P, hP.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice, s));
+  TCK(cudaMemsetAsync(m, 0, NPARAM * sizeof(float), s));
+  TCK(cudaMemsetAsync(v, 0, NPARAM * sizeof(float), s));
+  const long long steps_per_epoch = Ntr / o.batch;
+  const long long total = steps_per_epoch * o.epochs;
+  const int gblocks = std::max(1, std::min(152 * 2, (o.batch / 16 + 3) / 4));  // 16-sample tiles, 4 warps a block
+  float lfirst = 0.f, llast = 0.f;
+  long long t = 0;
+  for (int ep = 0; ep < o.epochs; ++ep) {
+    for (long long b = 0; b < steps_per_epoch; ++b) {
+      ++t;
+      const float lr = o.lr * (0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * (float)(t - 1) / (float)total)));
+      TCK(cudaMemsetAsync(grad, 0, NPARAM * sizeof(float), s));
+      TCK(cudaMemsetAsync(loss, 0, sizeof(float), s));
+      TCK(launch_mlp_grad(P, X2 + 3 * b * o.batch, Y2 + b * o.batch, Wt2 + b * o.batch, o.batch, grad, loss,
+                          gblocks, s));
+      TCK(launch_adam(P, m, v, grad, NPARAM, lr, 0.9f, 0.999f, 1e-8f, (int)t, s));
+      if (t == 1) {
+        TCK(cudaMemcpyAsync(&lfirst, loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+      }
+    }
+  }
+  TCK(cudaMemcpyAsync(&llast, loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+  // held-out pairs
+  TCK(launch_mlp_infer(P, X2 + 3 * Ntr, (int)Nval, Yp, s));
+  std::vector<float> hx(3 * Nval), hy(Nval), hyp(Nval), hw(Nval);
+  TCK(cudaMemcpyAsync(hw.data(), Wt2 + Ntr, Nval * sizeof(float), cudaMemcpyDeviceToHost, s));
+  TCK(cudaMemcpyAsync(hx.data(), X2 + 3 * Ntr, 3 * Nval * sizeof(float), cudaMemcpyDeviceToHost, s));
+  TCK(cudaMemcpyAsync(hy.data(), Y2 + Ntr, Nval * sizeof(float), cudaMemcpyDeviceToHost, s));
+  TCK(cudaMemcpyAsync(hyp.data(), Yp, Nval * sizeof(float), cudaMemcpyDeviceToHost, s));
+  TCK(cudaStreamSynchronize(s));
+  auto t2 = std::chrono::steady_clock::now();
+  // held-out pairs that do not complete (the step's network cells): T_new/T
+  // as the step forms it (clamped at the table's first temperature)
+  double se = 0.0, mx = 0.0;
+  std::vector<double> rel;
+  rel.reserve(Nval);
+  for (long long q = 0; q < Nval; ++q) {
+    if (!(hw[q] > 0.0f)) continue;
+    const double T = std::pow(10.0, (double)hx[3 * q + 1] * norm[3] + norm[2]);
+    const double tau = std::pow(10.0, (double)hx[3 * q + 2] * norm[5] + norm[4]);
+    const double d = tau * ((double)hyp[q] - (double)hy[q]);  // error of y = 1 + tau r
+    se += d * d;
+    // network output r: T_new/T = exp(-(tau + tau^2 r))
+    const double pred = std::max(std::exp(-(tau + tau * tau * (double)hyp[q])), ctx->cool_tmin / T);
+    rel.push_back(std::fabs(pred - std::exp(-(tau + tau * tau * (double)hy[q]))));  // |dT|/T
+    mx = std::max(mx, rel.back());
+  }
+  if (rel.empty()) rel.push_back(0.0);
+  std::sort(rel.begin(), rel.end());
+  cudaFree(ctx->mlp_params);
+  ctx->mlp_params = P;
+  for (int q = 0; q < 6; ++q) {
+    ctx->mlp_norm[q] = norm[q];
+    ctx->mlp_box[q] = o.box[q];
+  }
+  ctx->mlp_ready = true;
+  for (int q = 0; q < 2; ++q)
+    if (ctx->graph[q]) { cudaGraphExecDestroy(ctx->graph[q]); ctx->graph[q] = nullptr; }
+  if (rep) {
+    rep->loss_first = lfirst;
+    rep->loss_last = llast;
+    rep->val_rmse_y = std::sqrt(se / (double)rel.size());
+    rep->val_max_rel_T = mx;
+    rep->val_p99_rel_T = rel[(size_t)(0.99 * (double)(rel.size() - 1))];
+    rep->val_accept = (double)(std::upper_bound(rel.begin(), rel.end(), 1e-3) - rel.begin()) / (double)rel.size();
+    rep->ms_generate = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    rep->ms_train = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    rep->steps = t;
+  }
+  cleanup();
+#undef TCK
+  return rc;
+}
+
+int tlq_get_cooling_surrogate(tlq_ctx* ctx, float* params, float* norm6, double* box6) {
+  if (!ctx) return TLQ_ERR_ARG;
+  if (!ctx->mlp_ready) return sfail(ctx, TLQ_ERR_STATE, "no cooling surrogate");
+  if (params) SCK(cudaMemcpy(params, ctx->mlp_params, tlq::mlp::NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+  if (norm6) std::memcpy(norm6, ctx->mlp_norm, 6 * sizeof(float));
+  if (box6) std::memcpy(box6, ctx->mlp_box, 6 * sizeof(double));
+  return TLQ_OK;
+}
+
+int tlq_set_cooling_surrogate(tlq_ctx* ctx, const float* params, const float* norm6, const double* box6) {
+  if (!ctx || !params || !norm6 || !box6) return TLQ_ERR_ARG;
+  if (!ctx->mlp_params) SCK(cudaMalloc(&ctx->mlp_params, tlq::mlp::NPARAM * sizeof(float)));
+  SCK(cudaMemcpy(ctx->mlp_params, params, tlq::mlp::NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+  std::memcpy(ctx->mlp_norm, norm6, 6 * sizeof(float));
+  std::memcpy(ctx->mlp_box, box6, 6 * sizeof(double));
+  ctx->mlp_ready = true;
+  for (int q = 0; q < 2; ++q)
+    if (ctx->graph[q]) { cudaGraphExecDestroy(ctx->graph[q]); ctx->graph[q] = nullptr; }
+  return TLQ_OK;
+}
+
+int tlq_mlp_loss_grad(const float* params, const float* X, const float* Y, const float* Wt, int n, float* grad,
+                      float* loss) {
+  if (!params || !X || !Y || n < 1 || !grad || !loss) return TLQ_ERR_ARG;
+  float *dP = nullptr, *dX = nullptr, *dY = nullptr, *dW = nullptr, *dg = nullptr, *dl = nullptr;
+  cudaError_t e = cudaMalloc(&dP, tlq::mlp::NPARAM * sizeof(float));
+  if (e == cudaSuccess && Wt) e = cudaMalloc(&dW, (size_t)n * sizeof(float));
+  if (e == cudaSuccess && Wt) e = cudaMemcpy(dW, Wt, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&dX, 3 * (size_t)n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dY, (size_t)n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dg, tlq::mlp::NPARAM * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dl, sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(dP, params, tlq::mlp::NPARAM * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dX, X, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dY, Y, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dg, 0, tlq::mlp::NPARAM * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(dl, 0, sizeof(float));
+  if (e == cudaSuccess)
+    e = launch_mlp_grad(dP, dX, dY, dW, n, dg, dl, std::max(1, std::min(152 * 2, (n / 16 + 3) / 4)), 0);
+  if (e == cudaSuccess) e = cudaMemcpy(grad, dg, tlq::mlp::NPARAM * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(loss, dl, sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(dP); cudaFree(dX); cudaFree(dY); cudaFree(dW); cudaFree(dg); cudaFree(dl);
+  return e == cudaSuccess ? TLQ_OK : TLQ_ERR_CUDA;
+}
+
+int tlq_mlp_infer(const float* params, const float* X, int n, float* Yout) {
+  if (!params || !X || n < 1 || !Yout) return TLQ_ERR_ARG;
+  float *dP = nullptr, *dX = nullptr, *dY = nullptr;
+  cudaError_t e = cudaMalloc(&dP, tlq::mlp::NPARAM * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dX, 3 * (size_t)n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dY, (size_t)n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(dP, params, tlq::mlp::NPARAM * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dX, X, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_mlp_infer(dP, dX, n, dY, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(Yout, dY, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(dP); cudaFree(dX); cudaFree(dY);
+  return e == cudaSuccess ? TLQ_OK : TLQ_ERR_CUDA;
+}
+
+}  // extern "C"

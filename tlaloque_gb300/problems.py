@@ -163,3 +163,52 @@ def periodic_box(n: int = 32):
     cfg = Config(nx=n, ny=n, nz=n, xl=0.0, xr=1.0, yl=0.0, yr=1.0, zl=0.0, zr=1.0, gamma=5.0 / 3.0, cfl=0.4,
                  bc=(BC_PERIODIC,) * 6)
     return cfg
+
+
+def gaussian_field(n: int, seed: int, slope: float = -5.0 / 3.0) -> np.ndarray:
+    """Periodic Gaussian random field on n^3 (zero mean, unit variance) whose
+    shell-integrated power spectrum goes as k^slope (3-D amplitude
+    k^((slope-2)/2)); k = 0 removed."""
+    rng = np.random.default_rng(seed)
+    k = np.fft.fftfreq(n) * n
+    kz = np.fft.rfftfreq(n) * n
+    kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2)
+    kk[0, 0, 0] = 1.0
+    amp = kk ** ((slope - 2.0) / 2.0)
+    amp[0, 0, 0] = 0.0
+    spec = amp * (rng.standard_normal(kk.shape) + 1j * rng.standard_normal(kk.shape))
+    del kk, amp
+    f = np.fft.irfftn(spec, s=(n, n, n), axes=(0, 1, 2))
+    f -= f.mean()
+    f /= f.std()
+    return f
+
+
+def clumpy(n: int = 384, seed: int = 0, cooling: int = COOL_SUBCYCLE, box_pc: float = 8.0, mach: float = 2.0,
+           sigma_log10_n: float = 1.0, cool_max_sub: int = 16, cool_sub_frac: float = 0.1):
+    """Clumpy radiative medium: n^3 periodic (8 pc)^3 box; log10 n Gaussian
+    (mean 0, std 1, k^-5/3 spectrum: a lognormal density); log10 T uniform in
+    [3, 8] (a k^-5/3 Gaussian field through its normal CDF); velocities k^-5/3
+    fields with rms Mach 2 relative to the 1e4 K sound speed; mu 1.3, gamma
+    5/3, HLLC, CFL 0.4; synthetic cooling curve."""
+    from scipy.special import ndtr
+
+    L = box_pc * PC
+    T_cool, logL = synthetic_cooling_table()
+    mu = 1.3
+    cfg = Config(nx=n, ny=n, nz=n, xl=-L / 2, xr=L / 2, yl=-L / 2, yr=L / 2, zl=-L / 2, zr=L / 2, gamma=5.0 / 3.0,
+                 cfl=0.4, eta=0.5e-2, mu0=mu, limiter=LIMITER_VANLEER, solver=SOLVER_HLLC, bc=(BC_PERIODIC,) * 6,
+                 cooling=cooling, cool_max_sub=cool_max_sub, cool_sub_frac=cool_sub_frac, cool_T=T_cool,
+                 cool_logL=logL)
+    lgn = sigma_log10_n * gaussian_field(n, seed)
+    lgT = 3.0 + 5.0 * ndtr(gaussian_field(n, seed + 1))
+    cs4 = np.sqrt(cfg.gamma * KB * 1.0e4 / (mu * AMU))
+    vel = [gaussian_field(n, seed + 2 + q) for q in range(3)]
+    scale = mach * cs4 / np.sqrt(np.mean(vel[0] ** 2 + vel[1] ** 2 + vel[2] ** 2))
+    nd = 10.0 ** lgn
+    rho_i = nd * mu * AMU
+    p_i = nd * KB * 10.0 ** lgT
+    del lgn, lgT, nd
+    # interior fields; ghosts by periodic wrap (borders() refreshes them)
+    wrap = lambda a: np.pad(a, 2, mode="wrap")
+    return cfg, conserved(cfg, wrap(rho_i), *(wrap(scale * v) for v in vel), wrap(p_i))

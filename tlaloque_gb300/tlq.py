@@ -20,7 +20,8 @@ OK, ERR_CUDA, ERR_CONFIG, ERR_NONFINITE_DT, ERR_NEG_DENSITY, ERR_TIMEOUT, ERR_AR
 BC_OUTFLOW, BC_REFLECTIVE, BC_PERIODIC, BC_INFLOW = 1, 2, 3, 4
 LIMITER_NONE, LIMITER_VANLEER, LIMITER_MINMOD, LIMITER_UMIST, LIMITER_WOODWARD, LIMITER_SUPERBEE = 1, 2, 3, 4, 5, 6
 SOLVER_HLLC, SOLVER_HLL = 0, 1
-COOL_NONE, COOL_REF, COOL_SUBCYCLE = 0, 1, 2
+COOL_NONE, COOL_REF, COOL_SUBCYCLE, COOL_MLP = 0, 1, 2, 3
+MLP_NPARAM = 8641
 PREC_FP64, PREC_MIXED = 0, 1
 
 # Every function the header declares (checked by the CPU test suite).
@@ -30,6 +31,8 @@ EXPORTS = (
     "tlq_run_until", "tlq_synchronize", "tlq_stats_get", "tlq_enable_timing", "tlq_last_error", "tlq_status_string",
     "tlq_conserved_sums", "tlq_calc_prims", "tlq_time_step", "tlq_fluxes", "tlq_godunov", "tlq_borders",
     "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
+    "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
+    "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
 )
 
 
@@ -59,7 +62,20 @@ class CStats(C.Structure):
     _fields_ = [
         ("steps", C.c_longlong), ("t", C.c_double), ("dt", C.c_double), ("status", C.c_int), ("graph", C.c_int),
         ("ms_stage1", C.c_double), ("ms_stage2", C.c_double), ("timed", C.c_longlong), ("bytes_state", C.c_double),
+        ("cool_mlp", C.c_longlong), ("cool_fallback", C.c_longlong),
     ]
+
+
+class CSurrogateOpts(C.Structure):
+    _fields_ = [("nsamples", C.c_longlong), ("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_float),
+                ("seed", C.c_ulonglong), ("box", C.c_double * 6), ("sub_frac", C.c_double), ("max_sub", C.c_int)]
+
+
+class CSurrogateReport(C.Structure):
+    _fields_ = [("loss_first", C.c_double), ("loss_last", C.c_double), ("val_rmse_y", C.c_double),
+                ("val_max_rel_T", C.c_double), ("val_p99_rel_T", C.c_double), ("val_accept", C.c_double),
+                ("ms_generate", C.c_double),
+                ("ms_train", C.c_double), ("steps", C.c_longlong)]
 
 
 _lib = None
@@ -107,6 +123,15 @@ def load_library(path: str = LIB_PATH):
         "tlq_point_potential": (I, [V, D]),
         "tlq_gravity_source": (I, [V, D, D, D]),
         "tlq_time_step_noalloc": (I, [V, I, I, I, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, V, V]),
+        "tlq_surrogate_opts_default": (None, [C.POINTER(CSurrogateOpts)]),
+        "tlq_train_cooling_surrogate": (I, [V, C.POINTER(CSurrogateOpts), C.POINTER(CSurrogateReport)]),
+        "tlq_get_cooling_surrogate": (I, [V, C.POINTER(C.c_float), C.POINTER(C.c_float), D]),
+        "tlq_set_cooling_surrogate": (I, [V, C.POINTER(C.c_float), C.POINTER(C.c_float), D]),
+        "tlq_cooling_pairs": (I, [V, C.c_longlong, C.c_ulonglong, D, C.c_double, I, C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float), D]),
+        "tlq_mlp_loss_grad": (I, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float), I, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "tlq_mlp_infer": (I, [C.POINTER(C.c_float), C.POINTER(C.c_float), I, C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -361,3 +386,85 @@ class Context:
         S = self.cfg.zeros()
         self._check(self.L.tlq_gravity_source(self.h, _dp(W), _dp(phi), _dp(S)), "gravity_source")
         return S
+
+    # -- learned cooling surrogate (TLQ_COOL_MLP) -----------------------------
+    def train_cooling_surrogate(self, **opts) -> dict:
+        """Generate pairs with the exact integrator, train the network on the
+        GPU and install it in this context; returns the training report."""
+        o = surrogate_opts(**opts)
+        rep = CSurrogateReport()
+        self._check(self.L.tlq_train_cooling_surrogate(self.h, C.byref(o), C.byref(rep)), "train_cooling_surrogate")
+        return {n: getattr(rep, n) for n, _ in CSurrogateReport._fields_}
+
+    def get_cooling_surrogate(self):
+        P = np.zeros(MLP_NPARAM, dtype=np.float32)
+        norm = np.zeros(6, dtype=np.float32)
+        box = np.zeros(6, dtype=np.float64)
+        self._check(self.L.tlq_get_cooling_surrogate(self.h, _fp(P), _fp(norm), _dp(box)), "get_cooling_surrogate")
+        return P, norm, box
+
+    def set_cooling_surrogate(self, params, norm, box):
+        P = np.ascontiguousarray(params, dtype=np.float32)
+        nm = np.ascontiguousarray(norm, dtype=np.float32)
+        bx = np.ascontiguousarray(box, dtype=np.float64)
+        assert P.size == MLP_NPARAM and nm.size == 6 and bx.size == 6
+        self._check(self.L.tlq_set_cooling_surrogate(self.h, _fp(P), _fp(nm), _dp(bx)), "set_cooling_surrogate")
+
+    def cooling_pairs(self, n: int, seed: int, box, sub_frac: float = 2e-3, max_sub: int = 20000):
+        """(X raw features [n,3], Y targets [n], raw (n, T, T_new, dt) [n,4])
+        from the exact integrator on the GPU."""
+        X = np.zeros((n, 3), dtype=np.float32)
+        Y = np.zeros(n, dtype=np.float32)
+        R = np.zeros((n, 4), dtype=np.float64)
+        bx = np.ascontiguousarray(box, dtype=np.float64)
+        self._check(self.L.tlq_cooling_pairs(self.h, int(n), int(seed), _dp(bx), float(sub_frac), int(max_sub),
+                                             _fp(X), _fp(Y), _dp(R)), "cooling_pairs")
+        return X, Y, R
+
+
+def _fp(a):
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+        raise TypeError("expected a C-contiguous float32 numpy array")
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def surrogate_opts(**kw) -> CSurrogateOpts:
+    """tlq_surrogate_opts with the library defaults, overridden by keywords."""
+    L = load_library()
+    o = CSurrogateOpts()
+    L.tlq_surrogate_opts_default(C.byref(o))
+    for k, v in kw.items():
+        if k == "box":
+            for q in range(6):
+                o.box[q] = float(v[q])
+        else:
+            setattr(o, k, v)
+    return o
+
+
+def mlp_loss_grad(params, X, Y, wt=None):
+    """Weighted mean squared error of y and its gradient (GPU training kernel)."""
+    L = load_library()
+    P = np.ascontiguousarray(params, dtype=np.float32)
+    Xc = np.ascontiguousarray(X, dtype=np.float32)
+    Yc = np.ascontiguousarray(Y, dtype=np.float32)
+    Wc = None if wt is None else np.ascontiguousarray(wt, dtype=np.float32)
+    g = np.zeros(MLP_NPARAM, dtype=np.float32)
+    loss = np.zeros(1, dtype=np.float32)
+    rc = L.tlq_mlp_loss_grad(_fp(P), _fp(Xc), _fp(Yc), None if Wc is None else _fp(Wc), int(Yc.size), _fp(g),
+                             _fp(loss))
+    if rc != OK:
+        raise TlqError(rc, f"tlq_mlp_loss_grad: {L.tlq_status_string(rc).decode()}")
+    return float(loss[0]), g
+
+
+def mlp_infer(params, X):
+    """Network output y for normalised features X [n,3] (GPU inference kernel)."""
+    L = load_library()
+    P = np.ascontiguousarray(params, dtype=np.float32)
+    Xc = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.zeros(Xc.shape[0], dtype=np.float32)
+    rc = L.tlq_mlp_infer(_fp(P), _fp(Xc), int(Xc.shape[0]), _fp(Y))
+    if rc != OK:
+        raise TlqError(rc, f"tlq_mlp_infer: {L.tlq_status_string(rc).decode()}")
+    return Y
