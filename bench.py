@@ -8,12 +8,16 @@ A "step" is one full iteration of the reference's main loop
 gravity, artificial viscosity, cooling) over the whole mesh.  The metric is
 zone-updates/s = interior cells x steps / time.
 
-* value      device-resident, headline (mixed-precision) form: K steps
+* value      device-resident, headline form (mixed precision + the learned
+             cooling surrogate when the workload cools, else mixed): K steps
              through the C ABI (tlq_advance with per-kernel CUDA events) with
              the state already in HBM, timed with CUDA events on the
-             library's stream; `forms` holds the plain FP64 form measured the
-             same way, the speed-up, and the mixed form's relative L1 density
-             error and total-energy drift against FP64 after W+K steps;
+             library's stream; `forms` holds the plain FP64 form and the
+             mixed form measured the same way, the speed-ups, and each form's
+             relative L1 density error and total-energy drift against FP64
+             after W+K steps (the surrogate against FP64 with the exact
+             integrator it falls back to); `surrogate` its training and
+             fallback rate (the network is trained on the GPU first);
 * e2e        the same metric end to end through the C ABI with host
              buffers: per step tlq_upload (pinned host -> device + layout
              conversion + calc_prims/dt), tlq_step, tlq_download;
@@ -78,18 +82,22 @@ def make_workload(name: str):
     return cfg, U0, desc
 
 
-def bytes_per_zone(cfg, mixed: bool = False) -> dict:
+def bytes_per_zone(cfg, mixed: bool = False, surrogate: bool = False) -> dict:
     """Algorithmic HBM bytes per zone-update of each stage kernel (FP64 state:
     5 conserved variables x 8 B; the plain form carries the cooled interior
     pressure (8 B written by stage 2, read by stage 1; the mixed form
     recomputes it, and moves the viscosity Laplacian into stage 1 as an FP32
-    plane); point gravity reads phi once per stage)."""
+    plane); point gravity reads phi once per stage).  With the surrogate the
+    cooling and dt pass reads U once more (40 B; the 8 B energy write of the
+    cooled cells and the fallback queue are not counted)."""
     from tlaloque_gb300 import tlq
     cool = cfg.cooling != tlq.COOL_NONE and not mixed
     grav = cfg.masses is not None and len(cfg.masses) > 0
     lap = 20 if mixed else 0  # mixed: stage 1 writes eta*Lap(U) in FP32, stage 2 reads it
     s1 = 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
     s2 = 40 + 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
+    if surrogate:
+        return {"stage1": s1, "stage2": s2, "cool": 40, "step": s1 + s2 + 40}
     return {"stage1": s1, "stage2": s2, "step": s1 + s2}
 
 
@@ -246,16 +254,19 @@ def main():
     stream = torch.cuda.Stream()
     forms = {}
 
-    def measure(precision, steps, sample_clocks):
+    def measure(precision, steps, sample_clocks, net=None, **over):
         """W warm-up + K timed steps of one form from the initial state."""
-        c = tlq.Config(**{**cfg.__dict__, "precision": precision})
+        c = tlq.Config(**{**cfg.__dict__, "precision": precision, **over})
         ctx = tlq.Context(c)
         ctx.set_stream(stream.cuda_stream)
+        if net is not None:
+            ctx.set_cooling_surrogate(*net)
         U1 = U0.copy(order="F")
         ctx.borders(U1, 1)          # mainHD.f90:38
         ctx.upload(U1)
         ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
         ctx.synchronize()
+        st0 = ctx.stats()
         sampler = ClockSampler(local) if sample_clocks else None
         if sampler:
             sampler.start()
@@ -279,30 +290,67 @@ def main():
         sums = ctx.conserved_sums()
         ms_max = allmax(dist, ms)
         return {"ctx": ctx, "ms": ms_max, "value": world * cfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
-                "k2": st.ms_stage2, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
-                "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks}
+                "k2": st.ms_stage2, "kc": st.ms_cool, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
+                "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks,
+                "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback)}
 
+    def form(m):
+        d = {"value": m["value"], "ms_per_step": m["ms"] / args.steps, "ms_stage1": m["k1"], "ms_stage2": m["k2"]}
+        if m["kc"] > 0:
+            d["ms_cool_passes"] = m["kc"]
+        return d
+
+    def accuracy(a, b):
+        """a against b after the same W+K steps: relative L1 density error and
+        total-energy drift scaled to 100 steps."""
+        nst = args.warmup + args.steps
+        return {"after_steps": nst, "l1_rho_rel": float(np.sum(np.abs(a["rho"] - b["rho"])) / np.sum(np.abs(b["rho"]))),
+                "energy_drift_rel_per_100_steps": abs(a["E"] - b["E"]) / abs(b["E"]) * (100.0 / nst)}
+
+    cooling = cfg.cooling != tlq.COOL_NONE
     f64 = measure(tlq.PREC_FP64, args.steps, False)
     f64["ctx"].close()
-    mix = measure(tlq.PREC_MIXED, args.steps, True)
-    nst = args.warmup + args.steps
-    l1 = float(np.sum(np.abs(mix["rho"] - f64["rho"])) / np.sum(np.abs(f64["rho"])))
-    drift = abs(mix["E"] - f64["E"]) / abs(f64["E"]) * (100.0 / nst)
-    forms = {"fp64": {"value": f64["value"], "ms_per_step": f64["ms"] / args.steps, "ms_stage1": f64["k1"],
-                      "ms_stage2": f64["k2"]},
-             "mixed": {"value": mix["value"], "ms_per_step": mix["ms"] / args.steps, "ms_stage1": mix["k1"],
-                       "ms_stage2": mix["k2"]},
-             "speedup_mixed_vs_fp64": mix["value"] / f64["value"],
-             "mixed_vs_fp64_after_steps": nst, "l1_rho_rel": l1, "energy_drift_rel_per_100_steps": drift}
-    value = mix["value"]
-    ms_max = mix["ms"]
+    mix = measure(tlq.PREC_MIXED, args.steps, not cooling)
+    forms = {"fp64": form(f64), "mixed": form(mix), "speedup_mixed_vs_fp64": mix["value"] / f64["value"],
+             "mixed_vs_fp64": accuracy(mix, f64)}
+    head = mix
+    surrogate = None
+    if cooling:
+        # the learned cooling surrogate: trained here on the GPU for this
+        # workload's cooling table and physics; its fallback (and the FP64
+        # step it is compared with) is the exact integrator, fine sub-cycling
+        mix["ctx"].close()
+        exact = {"cool_sub_frac": 2e-3, "cool_max_sub": 20000}
+        with tlq.Context(cfg) as tctx:
+            rep = tctx.train_cooling_surrogate()
+            net = tctx.get_cooling_surrogate()
+        f64x = measure(tlq.PREC_FP64, args.steps, False, **exact)
+        f64x["ctx"].close()
+        sur = measure(tlq.PREC_MIXED, args.steps, True, net=net, cooling=tlq.COOL_MLP, **exact)
+        nm, nf = sur["cool"]
+        forms["fp64_exact_cooling"] = form(f64x)
+        forms["mixed_surrogate"] = form(sur)
+        forms["speedup_mixed_surrogate_vs_fp64"] = sur["value"] / f64["value"]
+        forms["mixed_surrogate_vs_fp64_exact_cooling"] = accuracy(sur, f64x)
+        surrogate = {"train": {k: rep[k] for k in ("ms_generate", "ms_train", "steps", "val_accept", "val_p99_rel_T",
+                                                    "val_rmse_y")},
+                     "timed_cell_steps_network": nm, "timed_cell_steps_fallback": nf,
+                     "fallback_rate": nf / max(1, nm + nf),
+                     "fallback_note": "cooling cell-steps of the timed steps handed to the exact integrator: "
+                                      "outside the training box, failing the 1e-3 residual check, or cooling to "
+                                      "the table's first temperature within the step"}
+        head = sur
+    value = head["value"]
+    ms_max = head["ms"]
+    mix = head
 
     k1, k2 = mix["k1"], mix["k2"]
     dom = "stage2" if k2 >= k1 else "stage1"
     kms = max(k1, k2)
-    bpz_m = bytes_per_zone(cfg, mixed=True)
+    bpz_m = bytes_per_zone(cfg, mixed=True, surrogate=surrogate is not None)
     achieved = bpz_m[dom] * cfg.cells / (kms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": f"stage_kernel_mixed<{2 if dom == 'stage2' else 1}>",
+                "ms_cool_passes": mix["kc"],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if peak_kind == "measured"
                 else peak_kind,
@@ -333,7 +381,8 @@ def main():
     e2e = {"value": world * cfg.cells * args.e2e_steps / el, "unit": UNIT,
            "h2d_bytes_per_step": int(Uh.nbytes), "d2h_bytes_per_step": int(Uh.nbytes),
            "ms_per_step": 1e3 * el / args.e2e_steps,
-           "path": "tlq_upload(pinned host U) + tlq_step + tlq_download(U) per step, mixed form"}
+           "path": "tlq_upload(pinned host U) + tlq_step + tlq_download(U) per step, "
+                   + ("mixed + surrogate form" if surrogate else "mixed form")}
     ctx.close()
 
     line = {
@@ -341,12 +390,15 @@ def main():
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": desc, "mesh": [cfg.nx, cfg.ny, cfg.nz],
-                   "form": "mixed: FP32 reconstruction, Riemann fluxes, sources and cooling; FP64 state, "
-                           "accumulation, high-Mach pressure recovery and dt",
+                   "form": ("mixed + learned cooling surrogate (BF16 tensor-core MLP, exact-integrator fallback): "
+                            if surrogate else "mixed: ")
+                           + "FP32 reconstruction, Riemann fluxes, sources; FP64 state, "
+                             "accumulation, high-Mach pressure recovery and dt",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (each state array 0.7 GB; 3 arrays touched per step)",
                    "sim": mix["sim"]},
-        "forms": forms, "e2e": e2e, "roofline": roofline, "clocks": mix["clocks"], "gpu_launches": 2 * args.steps,
+        "forms": forms, "surrogate": surrogate, "e2e": e2e, "roofline": roofline, "clocks": mix["clocks"],
+        "gpu_launches": (4 if surrogate else 2) * args.steps,
         "hbm_gbs_step": bpz_m["step"] * cfg.cells * args.steps / (ms_max / 1e3) / 1e9,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -132,6 +132,7 @@ typedef struct tlq_stats {
   double bytes_state;   /* device bytes held for the mesh state */
   long long cool_mlp;      /* TLQ_COOL_MLP: cell-steps cooled by the network (since upload) */
   long long cool_fallback; /* TLQ_COOL_MLP: cell-steps handed to the exact integrator */
+  double ms_cool;          /* TLQ_COOL_MLP: average device time of the timed cooling passes */
 } tlq_stats;
 
 typedef struct tlq_ctx tlq_ctx;

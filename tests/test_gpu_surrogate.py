@@ -157,7 +157,7 @@ def run(cfg, U0, nsteps, net=None, timing=False):
             ctx.enable_timing(True)
             ctx.advance(nsteps)
             s2 = ctx.stats()
-            ms = s2.ms_stage1 + s2.ms_stage2
+            ms = s2.ms_stage1 + s2.ms_stage2 + s2.ms_cool
     return dict(U=U, W=W, t=t, it=it, rc=rc, sums=sums, mlp=st.cool_mlp, fb=st.cool_fallback, ms=ms)
 
 

@@ -170,12 +170,13 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
     CK(launch_stage_mixed(2, ctx->tm_UPP, a, ctx->grid, ctx->stream));
   else
     CK(launch_stage(2, ctx->cfg.precision, ctx->tm_UPP, ctx->tm_P, a, ctx->grid, ctx->stream));
+  if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
     CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[par ^ 1], ctx->clk, ctx->partials, ctx->mlp_params, ctx->mlp_norm,
                           ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts, ctx->mlp_queue, ctx->mlp_qcount,
                           ctx->stream));
-  if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+  if (timed) CK(cudaEventRecord(ctx->ev[3], ctx->stream));
   return TLQ_OK;
 }
 
@@ -200,12 +201,14 @@ int run_steps(tlq_ctx* ctx, int n) {
     if (ctx->timing) {
       int rc = enqueue_step(ctx, par, true);
       if (rc) return rc;
-      CK(cudaEventSynchronize(ctx->ev[2]));
-      float a = 0.f, b = 0.f;
+      CK(cudaEventSynchronize(ctx->ev[3]));
+      float a = 0.f, b = 0.f, c = 0.f;
       cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
       cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+      cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]);
       ctx->ms1_acc += a;
       ctx->ms2_acc += b;
+      ctx->mscool_acc += c;
       ctx->ntimed += 1;
     } else {
       if (!ctx->graph[par]) {
@@ -337,7 +340,7 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   if (!r) r = make_map(ctx, &ctx->tm_UPP, ctx->UPP, 5);
   if (!r) r = make_map(ctx, &ctx->tm_P, ctx->Pc, 1);
   if (r) return bail(r);
-  for (int q = 0; q < 3; ++q) cudaEventCreate(&ctx->ev[q]);
+  for (int q = 0; q < 4; ++q) cudaEventCreate(&ctx->ev[q]);
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(TLQ_ERR_CUDA);
   *out = ctx;
   return TLQ_OK;
@@ -347,7 +350,7 @@ int tlq_destroy(tlq_ctx* ctx) {
   if (!ctx) return TLQ_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   invalidate_graphs(ctx);
-  for (int q = 0; q < 3; ++q)
+  for (int q = 0; q < 4; ++q)
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
@@ -579,7 +582,7 @@ int tlq_synchronize(tlq_ctx* ctx) {
 int tlq_enable_timing(tlq_ctx* ctx, int on) {
   if (!ctx) return TLQ_ERR_ARG;
   ctx->timing = on != 0;
-  ctx->ms1_acc = ctx->ms2_acc = 0.0;
+  ctx->ms1_acc = ctx->ms2_acc = ctx->mscool_acc = 0.0;
   ctx->ntimed = 0;
   return TLQ_OK;
 }
@@ -599,6 +602,7 @@ int tlq_stats_get(tlq_ctx* ctx, tlq_stats* s) {
   s->timed = ctx->ntimed;
   s->ms_stage1 = ctx->ntimed ? ctx->ms1_acc / ctx->ntimed : 0.0;
   s->ms_stage2 = ctx->ntimed ? ctx->ms2_acc / ctx->ntimed : 0.0;
+  s->ms_cool = ctx->ntimed ? ctx->mscool_acc / ctx->ntimed : 0.0;
   s->bytes_state = (double)ctx->L.plane * 8.0 * 17.0;
   if (ctx->cool_counts) {
     unsigned long long cc[2] = {0, 0};

@@ -53,8 +53,8 @@ struct tlq_ctx {
   int it0 = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool timing = false;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  double ms1_acc = 0.0, ms2_acc = 0.0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double ms1_acc = 0.0, ms2_acc = 0.0, mscool_acc = 0.0;
   long long ntimed = 0;
   long long steps = 0;
   // learned cooling surrogate (TLQ_COOL_MLP)
