@@ -175,6 +175,9 @@ int tlq_get_time(tlq_ctx* ctx, double* t, int* it, double* dt);
 int tlq_step(tlq_ctx* ctx, double* t, int* it, double* dt);
 int tlq_advance(tlq_ctx* ctx, int nsteps);
 int tlq_run_until(tlq_ctx* ctx, double tfin, int max_steps, double* t, int* it, double* dt);
+/* The end time of the run: steps start only while t < tfin (mainHD.f90:61);
+ * +inf by default (tlq_run_until sets it for its call only). */
+int tlq_set_tfin(tlq_ctx* ctx, double tfin);
 int tlq_synchronize(tlq_ctx* ctx);
 
 /* Diagnostics. */
@@ -203,6 +206,49 @@ int tlq_cooling_pairs(tlq_ctx* ctx, long long n, unsigned long long seed, const 
 int tlq_mlp_loss_grad(const float* params, const float* X, const float* Y, const float* Wt, int n, float* grad,
                       float* loss);
 int tlq_mlp_infer(const float* params, const float* X, int n, float* Y);
+
+/* ---- Batched ensemble (no counterpart in the reference, which runs one mesh
+ * per process): many independent meshes of uneven sizes, each with its own
+ * configuration, tables, winds, point masses, clock and dt, advanced together
+ * by one persistent launch per stage over all members' tiles, the step
+ * replayed from one CUDA graph.  Members run the mixed-precision step
+ * (TLQ_PREC_MIXED; cooling NONE, REF or SUBCYCLE).  Member i is a tlq_ctx
+ * (tlq_batch_member) for every set-up and I/O call (tables, winds, masses,
+ * upload, download, get_time); it must not be destroyed on its own.  A
+ * member's failure (non-finite dt, non-positive density) stops that member
+ * only. ------------------------------------------------------------------- */
+typedef struct tlq_batch tlq_batch;
+typedef struct tlq_batch_stats {
+  int members;
+  long long cells;            /* interior cells of all members */
+  long long steps;            /* batch steps run */
+  long long steps_timed;
+  double ms_per_step;         /* average device time of the timed batch steps */
+  int items;                  /* tiles in the work list */
+  int blocks;                 /* persistent blocks per launch */
+  int launches_per_step;
+  int graph;                  /* 1 once the step is a captured graph */
+} tlq_batch_stats;
+int tlq_batch_create(const tlq_config* cfgs, int nmembers, tlq_batch** out);
+int tlq_batch_destroy(tlq_batch* b);
+int tlq_batch_size(const tlq_batch* b);
+tlq_ctx* tlq_batch_member(tlq_batch* b, int i);
+/* z-chunk length (planes per tile, >= 8) of member i; default by nz. */
+int tlq_batch_set_tiling(tlq_batch* b, int i, int zlen);
+int tlq_batch_get_tiling(const tlq_batch* b, int i, int* zlen);
+/* Autotuner: per distinct mesh size, the z-chunk length from the cache file
+ * (JSON, keyed by GPU name and size; NULL = no cache) or measured now over
+ * `steps` steps from the members' current state (restored afterwards);
+ * chosen[i] (may be NULL) receives member i's length. */
+int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* chosen);
+/* `steps` batch steps (every member whose t < its tfin advances one step). */
+int tlq_batch_run(tlq_batch* b, int steps);
+int tlq_batch_synchronize(tlq_batch* b);
+/* Per-member status (TLQ_OK or the member's sticky error). */
+int tlq_batch_status(tlq_batch* b, int* status);
+int tlq_batch_enable_timing(tlq_batch* b, int on);
+int tlq_batch_stats_get(tlq_batch* b, tlq_batch_stats* s);
+const char* tlq_batch_last_error(const tlq_batch* b);
 
 /* ---- Per-routine entry points (unit parity; host arrays in the reference
  * layout; each replaces the external subroutine cited). ------------------- */

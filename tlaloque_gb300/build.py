@@ -32,6 +32,7 @@ UNITS = [
     ("tlq_mixed.cu", ["--use_fast_math"]),
     ("tlq_mlp.cu", []),
     ("tlq_surrogate.cu", ["--use_fast_math"]),
+    ("tlq_batch.cu", ["--use_fast_math"]),
 ]
 
 

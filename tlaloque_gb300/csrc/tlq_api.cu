@@ -110,6 +110,7 @@ void fill_params(tlq_ctx* c) {
 }
 
 void invalidate_graphs(tlq_ctx* c) {
+  c->gen += 1;
   for (int q = 0; q < 2; ++q)
     if (c->graph[q]) { cudaGraphExecDestroy(c->graph[q]); c->graph[q] = nullptr; }
 }
@@ -329,7 +330,9 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   ctx->grid = dim3(gx, gy, gz);
   ctx->npartials = gx * gy * gz;
   const int nb = init_blocks(ctx->P);
-  const int npart = std::max(std::max(ctx->npartials, nb), cool_mlp_blocks(ctx->P));
+  // (tiles down to 8-plane z-chunks, which a batch's tuner may choose)
+  const int npart = std::max(std::max(std::max(ctx->npartials, nb), cool_mlp_blocks(ctx->P)),
+                             gx * gy * ((cfg->nz + 7) / 8));
   if (cudaMalloc(&ctx->partials, sizeof(double) * 3 * (size_t)npart) ||
       cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
     return bail(TLQ_ERR_NOMEM);
@@ -571,6 +574,11 @@ int tlq_run_until(tlq_ctx* ctx, double tfin, int max_steps, double* t, int* it, 
   if (rc) return rc;
   if (rc2) return rc2;
   return tlq_get_time(ctx, t, it, dt);
+}
+
+int tlq_set_tfin(tlq_ctx* ctx, double tfin) {
+  if (!ctx || tfin != tfin) return TLQ_ERR_ARG;
+  return set_tfin(ctx, tfin);
 }
 
 int tlq_synchronize(tlq_ctx* ctx) {

@@ -52,6 +52,7 @@ struct tlq_ctx {
   double t0 = 0.0;
   int it0 = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  unsigned gen = 0;  // bumped whenever set-up changes what a captured step does
   bool timing = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double ms1_acc = 0.0, ms2_acc = 0.0, mscool_acc = 0.0;

@@ -125,11 +125,12 @@ __device__ __forceinline__ void block_max3(double& a, double& b, double& c, doub
 // nprev: block maxima an earlier kernel of the same step left in
 // partials[0 .. 3 nprev); this grid's go after them and the last block
 // reduces both.
+// nblocks, bid: the blocks (tiles) of this reduction and this one's index
+// (a persistent kernel reduces per mesh over the tiles it works through).
 template <int NTHREADS>
-__device__ void cfl_reduce_finalize(double a, double b, double c, double* partials, Clock* clk, const Params& p,
-                                    bool advance, double* red, int* s_flag, unsigned nprev = 0) {
-  const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
-  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+__device__ void cfl_reduce_finalize_n(double a, double b, double c, double* partials, Clock* clk, const Params& p,
+                                      bool advance, double* red, int* s_flag, unsigned nprev, unsigned nblocks,
+                                      unsigned bid) {
   block_max3<NTHREADS>(a, b, c, red);
   if (threadIdx.x == 0) {
     partials[3 * (nprev + bid) + 0] = a;
@@ -161,6 +162,15 @@ __device__ void cfl_reduce_finalize(double a, double b, double c, double* partia
     clk->ticket = 0u;
     __threadfence();
   }
+}
+
+template <int NTHREADS>
+__device__ __forceinline__ void cfl_reduce_finalize(double a, double b, double c, double* partials, Clock* clk,
+                                                    const Params& p, bool advance, double* red, int* s_flag,
+                                                    unsigned nprev = 0) {
+  cfl_reduce_finalize_n<NTHREADS>(a, b, c, partials, clk, p, advance, red, s_flag, nprev,
+                                  gridDim.x * gridDim.y * gridDim.z,
+                                  blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
 }
 
 }  // namespace tlq

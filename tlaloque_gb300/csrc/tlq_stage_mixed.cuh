@@ -132,18 +132,19 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   u4 = u4 + f2d((w[4] - p0) / gm1);
 }
 
+// One tile (TX x TY columns, z-chunk bz of zlen planes) of a stage: the
+// body of the single-mesh kernel and of each work item of the batched
+// persistent kernel.  nblk / bid: the mesh's tiles and this one's index, for
+// the dt reduction.  Leaves every TMA copy it issued completed.
 template <int STAGE>
-__global__ void __launch_bounds__(NT, 3)
-    stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, StageArgs a) {
+__device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArgs& a, MixedSmem& s, int bx, int by,
+                                           int bz, unsigned nblk, unsigned bid) {
   constexpr int H = STAGE;
-  extern __shared__ __align__(128) unsigned char smem_bytes[];
-  MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
   const Params& p = a.p;
   const Layout& L = a.L;
   const int tid = threadIdx.x;
-  const int bx = blockIdx.x, by = blockIdx.y;
   const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
-  const int k0 = 1 + (int)blockIdx.z * a.zlen;
+  const int k0 = 1 + bz * a.zlen;
   const int k1 = min(p.nz, k0 + a.zlen - 1);
   Clock* clk = a.clk;
 
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(NT, 3)
     const int slot = raw_slot(q);
     fence_proxy_async();
     mbar_arrive_expect_tx(&s.bar[slot], 5u * PLANE_BOX * 8u);
-    tma_load_4d(s.raw[slot], &tm_in, &s.bar[slot], bx * TX, by * TY, q + 1, 0);
+    tma_load_4d(s.raw[slot], tm, &s.bar[slot], bx * TX, by * TY, q + 1, 0);
     issued = q;
   };
   uint32_t phase = 0;
@@ -419,7 +420,17 @@ __global__ void __launch_bounds__(NT, 3)
     d0 = d1 = d2 = NAN;
   }
   // with the surrogate, cooling and the dt reduction follow in their own kernel
-  if (STAGE == 2 && p.cooling != COOL_MLP) cfl_reduce_finalize<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag);
+  if (STAGE == 2 && p.cooling != COOL_MLP)
+    cfl_reduce_finalize_n<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag, 0, nblk, bid);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(NT, 3)
+    stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ StageArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_bytes[];
+  MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
+  mixed_tile<STAGE>(&tm_in, a, s, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z,
+                    blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
 }
 
 }  // namespace tlq

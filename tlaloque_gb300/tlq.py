@@ -33,6 +33,9 @@ EXPORTS = (
     "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
     "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
     "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
+    "tlq_set_tfin", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
+    "tlq_batch_set_tiling", "tlq_batch_get_tiling", "tlq_batch_autotune", "tlq_batch_run", "tlq_batch_synchronize",
+    "tlq_batch_status", "tlq_batch_enable_timing", "tlq_batch_stats_get", "tlq_batch_last_error",
 )
 
 
@@ -66,6 +69,12 @@ class CStats(C.Structure):
     ]
 
 
+class CBatchStats(C.Structure):
+    _fields_ = [("members", C.c_int), ("cells", C.c_longlong), ("steps", C.c_longlong),
+                ("steps_timed", C.c_longlong), ("ms_per_step", C.c_double), ("items", C.c_int), ("blocks", C.c_int),
+                ("launches_per_step", C.c_int), ("graph", C.c_int)]
+
+
 class CSurrogateOpts(C.Structure):
     _fields_ = [("nsamples", C.c_longlong), ("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_float),
                 ("seed", C.c_ulonglong), ("box", C.c_double * 6), ("sub_frac", C.c_double), ("max_sub", C.c_int)]
@@ -96,6 +105,20 @@ def load_library(path: str = LIB_PATH):
         "tlq_config_default": (None, [C.POINTER(CConfig)]),
         "tlq_create": (I, [C.POINTER(CConfig), C.POINTER(V)]),
         "tlq_destroy": (I, [V]),
+        "tlq_set_tfin": (I, [V, C.c_double]),
+        "tlq_batch_create": (I, [C.POINTER(CConfig), I, C.POINTER(V)]),
+        "tlq_batch_destroy": (I, [V]),
+        "tlq_batch_size": (I, [V]),
+        "tlq_batch_member": (V, [V, I]),
+        "tlq_batch_set_tiling": (I, [V, I, I]),
+        "tlq_batch_get_tiling": (I, [V, I, C.POINTER(I)]),
+        "tlq_batch_autotune": (I, [V, C.c_char_p, I, C.POINTER(I)]),
+        "tlq_batch_run": (I, [V, I]),
+        "tlq_batch_synchronize": (I, [V]),
+        "tlq_batch_status": (I, [V, C.POINTER(I)]),
+        "tlq_batch_enable_timing": (I, [V, I]),
+        "tlq_batch_stats_get": (I, [V, C.POINTER(CBatchStats)]),
+        "tlq_batch_last_error": (C.c_char_p, [V]),
         "tlq_set_stream": (I, [V, V]),
         "tlq_set_cooling_table": (I, [V, D, D, I]),
         "tlq_set_winds": (I, [V, C.POINTER(CWind), I]),
@@ -237,14 +260,18 @@ class Config:
 class Context:
     """One tlq_ctx: the whole mesh resident on one GPU."""
 
-    def __init__(self, cfg: Config):
+    def __init__(self, cfg: Config, _borrowed=None):
         self.L = load_library()
         self.cfg = cfg
-        h = C.c_void_p()
-        cc = cfg.to_c()
-        rc = self.L.tlq_create(C.byref(cc), C.byref(h))
-        if rc != OK:
-            raise TlqError(rc, f"tlq_create: {self.L.tlq_status_string(rc).decode()}")
+        self._owned = _borrowed is None
+        if _borrowed is None:
+            h = C.c_void_p()
+            cc = cfg.to_c()
+            rc = self.L.tlq_create(C.byref(cc), C.byref(h))
+            if rc != OK:
+                raise TlqError(rc, f"tlq_create: {self.L.tlq_status_string(rc).decode()}")
+        else:
+            h = C.c_void_p(_borrowed)
         self.h = h
         if cfg.cool_T is not None:
             T = np.ascontiguousarray(cfg.cool_T, dtype=np.float64)
@@ -268,7 +295,8 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
-            self.L.tlq_destroy(self.h)
+            if getattr(self, "_owned", True):
+                self.L.tlq_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -324,6 +352,9 @@ class Context:
         self._check(self.L.tlq_run_until(self.h, float(tfin), int(max_steps), C.byref(t), C.byref(it), C.byref(dt)),
                     "run_until")
         return t.value, it.value, dt.value
+
+    def set_tfin(self, tfin: float):
+        self._check(self.L.tlq_set_tfin(self.h, float(tfin)), "set_tfin")
 
     def synchronize(self):
         self._check(self.L.tlq_synchronize(self.h), "synchronize")
@@ -468,3 +499,82 @@ def mlp_infer(params, X):
     if rc != OK:
         raise TlqError(rc, f"tlq_mlp_infer: {L.tlq_status_string(rc).decode()}")
     return Y
+
+
+class Batch:
+    """A tlq_batch: independent meshes advanced together by persistent
+    launches over all members' tiles, one CUDA graph per step.  members[i]
+    is a Context on member i (set-up, upload, download, time)."""
+
+    def __init__(self, cfgs):
+        self.L = load_library()
+        arr = (CConfig * len(cfgs))()
+        for q, c in enumerate(cfgs):
+            arr[q] = c.to_c()
+        h = C.c_void_p()
+        rc = self.L.tlq_batch_create(arr, len(cfgs), C.byref(h))
+        if rc != OK:
+            raise TlqError(rc, f"tlq_batch_create: {self.L.tlq_status_string(rc).decode()}")
+        self.h = h
+        self.members = [Context(c, _borrowed=self.L.tlq_batch_member(h, q)) for q, c in enumerate(cfgs)]
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            raise TlqError(rc, f"{what}: {self.L.tlq_status_string(rc).decode()} "
+                               f"{self.L.tlq_batch_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.h = None
+            self.L.tlq_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, steps: int):
+        self._check(self.L.tlq_batch_run(self.h, int(steps)), "batch_run")
+
+    def synchronize(self):
+        self._check(self.L.tlq_batch_synchronize(self.h), "batch_synchronize")
+
+    def status(self):
+        st = (C.c_int * len(self.members))()
+        self._check(self.L.tlq_batch_status(self.h, st), "batch_status")
+        return list(st)
+
+    def set_tiling(self, i: int, zlen: int):
+        self._check(self.L.tlq_batch_set_tiling(self.h, int(i), int(zlen)), "batch_set_tiling")
+
+    def tiling(self):
+        out = []
+        for q in range(len(self.members)):
+            z = C.c_int()
+            self._check(self.L.tlq_batch_get_tiling(self.h, q, C.byref(z)), "batch_get_tiling")
+            out.append(z.value)
+        return out
+
+    def autotune(self, cache_path: str | None = None, steps: int = 3):
+        ch = (C.c_int * len(self.members))()
+        self._check(self.L.tlq_batch_autotune(self.h, cache_path.encode() if cache_path else None, int(steps), ch),
+                    "batch_autotune")
+        return list(ch)
+
+    def enable_timing(self, on: bool = True):
+        self._check(self.L.tlq_batch_enable_timing(self.h, 1 if on else 0), "batch_enable_timing")
+
+    def stats(self) -> CBatchStats:
+        s = CBatchStats()
+        self._check(self.L.tlq_batch_stats_get(self.h, C.byref(s)), "batch_stats")
+        return s
+
