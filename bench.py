@@ -344,6 +344,8 @@ def main():
     bpz = bytes_per_zone(cfg)
     stream = torch.cuda.Stream()
     forms = {}
+    import tempfile
+    tune_cache = os.path.join(tempfile.gettempdir(), "tlq_autotune.json")
 
     def measure(precision, steps, sample_clocks, net=None, **over):
         """W warm-up + K timed steps of one form from the initial state."""
@@ -355,6 +357,7 @@ def main():
         U1 = U0.copy(order="F")
         ctx.borders(U1, 1)          # mainHD.f90:38
         ctx.upload(U1)
+        zlen = ctx.autotune(tune_cache, steps=3)  # z-chunk of the stage grid (state restored)
         ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
         ctx.synchronize()
         st0 = ctx.stats()
@@ -383,10 +386,11 @@ def main():
         return {"ctx": ctx, "ms": ms_max, "value": world * cfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
                 "k2": st.ms_stage2, "kc": st.ms_cool, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
                 "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks,
-                "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback)}
+                "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback), "zlen": zlen}
 
     def form(m):
-        d = {"value": m["value"], "ms_per_step": m["ms"] / args.steps, "ms_stage1": m["k1"], "ms_stage2": m["k2"]}
+        d = {"value": m["value"], "ms_per_step": m["ms"] / args.steps, "ms_stage1": m["k1"], "ms_stage2": m["k2"],
+             "zlen": m["zlen"]}
         if m["kc"] > 0:
             d["ms_cool_passes"] = m["kc"]
         return d

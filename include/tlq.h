@@ -207,6 +207,16 @@ int tlq_mlp_loss_grad(const float* params, const float* X, const float* Y, const
                       float* loss);
 int tlq_mlp_infer(const float* params, const float* X, int n, float* Y);
 
+/* Stage tiling (no counterpart in the reference): the z-chunk length of the
+ * stage grid (>= 8 planes, or nz; default 64 for nz >= 128, 32 for nz >= 32,
+ * else nz), and the measuring autotuner that picks it -- from the cache file
+ * (JSON keyed by GPU name, mesh size and form; NULL = no cache) or timed now
+ * over `steps` steps per candidate (8, 16, 32, 64, 128) from the current
+ * state, which is restored afterwards. */
+int tlq_set_tiling(tlq_ctx* ctx, int zlen);
+int tlq_get_tiling(const tlq_ctx* ctx, int* zlen);
+int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen);
+
 /* ---- Batched ensemble (no counterpart in the reference, which runs one mesh
  * per process): many independent meshes of uneven sizes, each with its own
  * configuration, tables, winds, point masses, clock and dt, advanced together

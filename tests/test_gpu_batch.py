@@ -153,3 +153,31 @@ def test_autotune_chooses_restores_and_caches(gpu_lib, tmp_path):
     with tlq.Batch([c for c, _ in members]) as b2:
         load(b2, members)
         assert b2.autotune(str(cache), steps=2) == chosen
+
+
+@pytest.mark.parametrize("precision", [tlq.PREC_FP64, tlq.PREC_MIXED])
+def test_context_autotune_restores_state(gpu_lib, tmp_path, precision):
+    """Single-context tuner on the wind bubble (FP64: carried cooled pressure
+    is state too): the run after tuning continues exactly (FP64: bit for bit,
+    the plain form does not depend on the tiling; mixed: FP32 round-off)."""
+    cfg, U0 = problems.wind_bubble(40)
+    cfg = tlq.Config(**{**cfg.__dict__, "precision": precision})
+    ref, tr = single(cfg, U0, 6)
+    cache = tmp_path / "tune1.json"
+    U1 = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U1, 1)
+        ctx.upload(U1)
+        ctx.advance(2)
+        z = ctx.autotune(str(cache), steps=2)
+        assert z == ctx.tiling() and z in (8, 16, 32, 40)
+        ctx.advance(4)
+        t, it, dt, rc = ctx.time()
+        U = ctx.state()[0]
+    assert rc == tlq.OK and it == 6
+    if precision == tlq.PREC_FP64:
+        np.testing.assert_array_equal(interior(U), interior(ref))
+        assert t == tr[0]
+    else:
+        rel_close(interior(U), interior(ref))
+    assert json.loads(cache.read_text())["tuned"]

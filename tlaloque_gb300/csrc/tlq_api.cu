@@ -239,7 +239,29 @@ int read_clock(tlq_ctx* ctx) {
 
 }  // namespace
 
+int ctx_set_zlen(tlq_ctx* ctx, int zlen) {
+  const int nz = ctx->cfg.nz;
+  zlen = std::min(zlen, nz);
+  if (zlen < 8 && zlen != nz) return fail(ctx, TLQ_ERR_ARG, "z-chunk length must be >= 8 planes (or nz)");
+  ctx->zlen = zlen;
+  ctx->grid.z = (unsigned)((nz + zlen - 1) / zlen);
+  ctx->npartials = (int)(ctx->grid.x * ctx->grid.y * ctx->grid.z);
+  invalidate_graphs(ctx);
+  return TLQ_OK;
+}
+
 extern "C" {
+
+int tlq_set_tiling(tlq_ctx* ctx, int zlen) {
+  if (!ctx) return TLQ_ERR_ARG;
+  return ctx_set_zlen(ctx, zlen);
+}
+
+int tlq_get_tiling(const tlq_ctx* ctx, int* zlen) {
+  if (!ctx || !zlen) return TLQ_ERR_ARG;
+  *zlen = ctx->zlen;
+  return TLQ_OK;
+}
 
 void tlq_config_default(tlq_config* c) {
   if (!c) return;

@@ -274,8 +274,10 @@ std::map<std::string, std::pair<int, double>> read_cache(const char* path, const
     if (std::sscanf(line, " \"gpu\": \"%255[^\"]\"", name) == 1) same_gpu = (gpu == name);
     int nx, ny, nz, z;
     double ms;
-    if (std::sscanf(line, " \"%dx%dx%d/mixed\": {\"zlen\": %d, \"ms_per_step\": %lf", &nx, &ny, &nz, &z, &ms) == 5)
-      m[std::to_string(nx) + "x" + std::to_string(ny) + "x" + std::to_string(nz)] = {z, ms};
+    char form[16];
+    if (std::sscanf(line, " \"%dx%dx%d/%15[a-z0-9_]\": {\"zlen\": %d, \"ms_per_step\": %lf", &nx, &ny, &nz, form, &z,
+                    &ms) == 6)
+      m[std::to_string(nx) + "x" + std::to_string(ny) + "x" + std::to_string(nz) + "/" + form] = {z, ms};
   }
   std::fclose(f);
   if (!same_gpu) m.clear();
@@ -290,7 +292,7 @@ int write_cache(const char* path, const std::string& gpu, const std::map<std::st
   std::fprintf(f, "{\n  \"gpu\": \"%s\",\n  \"tuned\": {\n", gpu.c_str());
   size_t q = 0;
   for (const auto& kv : m)
-    std::fprintf(f, "    \"%s/mixed\": {\"zlen\": %d, \"ms_per_step\": %.6f}%s\n", kv.first.c_str(), kv.second.first,
+    std::fprintf(f, "    \"%s\": {\"zlen\": %d, \"ms_per_step\": %.6f}%s\n", kv.first.c_str(), kv.second.first,
                  kv.second.second, ++q < m.size() ? "," : "");
   std::fprintf(f, "  }\n}\n");
   std::fclose(f);
@@ -453,7 +455,8 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
   std::map<std::string, std::vector<int>> classes;
   for (size_t i = 0; i < b->m.size(); ++i) {
     const tlq_config& c = b->m[i]->cfg;
-    classes[std::to_string(c.nx) + "x" + std::to_string(c.ny) + "x" + std::to_string(c.nz)].push_back((int)i);
+    classes[std::to_string(c.nx) + "x" + std::to_string(c.ny) + "x" + std::to_string(c.nz) + "/batch_mixed"].push_back(
+        (int)i);
   }
   bool wrote = false;
   for (auto& kv : classes) {
@@ -524,6 +527,87 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
   }
   if (chosen)
     for (size_t i = 0; i < b->m.size(); ++i) chosen[i] = b->zlen[i];
+  return TLQ_OK;
+}
+
+// The same tuner for one context: the z-chunk length of its stage grid,
+// from the cache or measured over `steps` steps from the current state
+// (restored afterwards), keyed by mesh size and form (mixed / fp64).
+int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen) {
+  if (!ctx || steps < 1) return TLQ_ERR_ARG;
+  if (!ctx->uploaded) {
+    ctx->err = "autotune needs the state (tlq_upload)";
+    return TLQ_ERR_STATE;
+  }
+  const std::string gpu = device_name();
+  auto cache = read_cache(cache_path, gpu);
+  const tlq_config& c = ctx->cfg;
+  const std::string key = std::to_string(c.nx) + "x" + std::to_string(c.ny) + "x" + std::to_string(c.nz) +
+                          (c.precision == TLQ_PREC_MIXED ? "/mixed" : "/fp64") +
+                          (c.cooling == TLQ_COOL_MLP ? "_mlp" : "");
+  auto hit = cache.find(key);
+  int best = ctx->zlen;
+  if (hit != cache.end()) {
+    best = hit->second.first;
+  } else {
+    double t, dt;
+    int it;
+    int rc = tlq_get_time(ctx, &t, &it, &dt);
+    if (rc != TLQ_OK) return rc;
+    const int cur = ctx->cur;
+    // the state: U, and the carried cooled pressure of the plain form
+    const bool carried = c.cooling != TLQ_COOL_NONE && c.precision == TLQ_PREC_FP64;
+    const size_t bytes = (size_t)ctx->L.plane * 5 * sizeof(double);
+    const size_t pbytes = carried ? (size_t)ctx->L.plane * sizeof(double) : 0;
+    double* snap = nullptr;
+    tlq::Clock clk{};
+    if (cudaMalloc(&snap, bytes + pbytes) != cudaSuccess) return TLQ_ERR_NOMEM;
+    cudaMemcpyAsync(snap, ctx->U[cur], bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (carried) cudaMemcpyAsync(snap + ctx->L.plane * 5, ctx->Pc, pbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(&clk, ctx->clk, sizeof(clk), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    const long long steps0 = ctx->steps;
+    double best_ms = 1e300;
+    for (int z : {8, 16, 32, 64, 128}) {
+      if (z > c.nz && z != 8) continue;
+      rc = ctx_set_zlen(ctx, std::min(z, c.nz));
+      if (rc == TLQ_OK) rc = tlq_advance(ctx, 1);  // warm-up
+      if (rc == TLQ_OK) rc = tlq_enable_timing(ctx, 1);
+      if (rc == TLQ_OK) rc = tlq_advance(ctx, steps);
+      tlq_stats s{};
+      if (rc == TLQ_OK) rc = tlq_stats_get(ctx, &s);
+      tlq_enable_timing(ctx, 0);
+      if (rc != TLQ_OK) {
+        cudaFree(snap);
+        return rc;
+      }
+      const double ms = s.ms_stage1 + s.ms_stage2 + s.ms_cool;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = std::min(z, c.nz);
+      }
+      // back to the snapshot
+      cudaMemcpyAsync(ctx->U[cur], snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (carried) cudaMemcpyAsync(ctx->Pc, snap + ctx->L.plane * 5, pbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaMemcpyAsync(ctx->clk, &clk, sizeof(clk), cudaMemcpyHostToDevice, ctx->stream);
+      if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        cudaFree(snap);
+        return TLQ_ERR_CUDA;
+      }
+      ctx->cur = cur;
+    }
+    cudaFree(snap);
+    ctx->steps = steps0;
+    if (ctx->cool_counts) cudaMemsetAsync(ctx->cool_counts, 0, 2 * sizeof(unsigned long long), ctx->stream);
+    cache[key] = {best, best_ms};
+    if (write_cache(cache_path, gpu, cache) != TLQ_OK) {
+      ctx->err = std::string("cannot write the tuning cache ") + (cache_path ? cache_path : "");
+      return TLQ_ERR_ARG;
+    }
+  }
+  const int rc = ctx_set_zlen(ctx, best);
+  if (rc != TLQ_OK) return rc;
+  if (chosen) *chosen = ctx->zlen;
   return TLQ_OK;
 }
 

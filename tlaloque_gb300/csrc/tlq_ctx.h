@@ -75,3 +75,7 @@ struct tlq_ctx {
 // Closed-form cooling-time integral of the table for the surrogate's
 // residual check (tlq_surrogate.cu); called by tlq_set_cooling_table.
 int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* logL, int n);
+
+// Z-chunk length of the stage grid (>= 8 planes, or nz): regrids and drops
+// the captured graphs (tlq_api.cu).
+int ctx_set_zlen(tlq_ctx* ctx, int zlen);

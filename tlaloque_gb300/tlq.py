@@ -33,7 +33,7 @@ EXPORTS = (
     "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
     "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
     "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
-    "tlq_set_tfin", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
+    "tlq_set_tfin", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
     "tlq_batch_set_tiling", "tlq_batch_get_tiling", "tlq_batch_autotune", "tlq_batch_run", "tlq_batch_synchronize",
     "tlq_batch_status", "tlq_batch_enable_timing", "tlq_batch_stats_get", "tlq_batch_last_error",
 )
@@ -106,6 +106,9 @@ def load_library(path: str = LIB_PATH):
         "tlq_create": (I, [C.POINTER(CConfig), C.POINTER(V)]),
         "tlq_destroy": (I, [V]),
         "tlq_set_tfin": (I, [V, C.c_double]),
+        "tlq_set_tiling": (I, [V, I]),
+        "tlq_get_tiling": (I, [V, C.POINTER(I)]),
+        "tlq_autotune": (I, [V, C.c_char_p, I, C.POINTER(I)]),
         "tlq_batch_create": (I, [C.POINTER(CConfig), I, C.POINTER(V)]),
         "tlq_batch_destroy": (I, [V]),
         "tlq_batch_size": (I, [V]),
@@ -352,6 +355,20 @@ class Context:
         self._check(self.L.tlq_run_until(self.h, float(tfin), int(max_steps), C.byref(t), C.byref(it), C.byref(dt)),
                     "run_until")
         return t.value, it.value, dt.value
+
+    def set_tiling(self, zlen: int):
+        self._check(self.L.tlq_set_tiling(self.h, int(zlen)), "set_tiling")
+
+    def tiling(self) -> int:
+        z = C.c_int()
+        self._check(self.L.tlq_get_tiling(self.h, C.byref(z)), "get_tiling")
+        return z.value
+
+    def autotune(self, cache_path: str | None = None, steps: int = 3) -> int:
+        z = C.c_int()
+        self._check(self.L.tlq_autotune(self.h, cache_path.encode() if cache_path else None, int(steps), C.byref(z)),
+                    "autotune")
+        return z.value
 
     def set_tfin(self, tfin: float):
         self._check(self.L.tlq_set_tfin(self.h, float(tfin)), "set_tfin")
