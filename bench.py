@@ -320,6 +320,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--train-samples", type=int, default=20_000_000, help="surrogate training pairs")
+    ap.add_argument("--train-epochs", type=int, default=30, help="surrogate training epochs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -417,7 +419,7 @@ def main():
         mix["ctx"].close()
         exact = {"cool_sub_frac": 2e-3, "cool_max_sub": 20000}
         with tlq.Context(cfg) as tctx:
-            rep = tctx.train_cooling_surrogate()
+            rep = tctx.train_cooling_surrogate(nsamples=args.train_samples, epochs=args.train_epochs)
             net = tctx.get_cooling_surrogate()
         f64x = measure(tlq.PREC_FP64, args.steps, False, **exact)
         f64x["ctx"].close()

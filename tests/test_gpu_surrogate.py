@@ -199,12 +199,15 @@ def test_wind_bubble_bars_with_surrogate(trained):
     cfg, U0 = problems.wind_bubble(64)
     ref = run(tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, **EXACT}), U0, 100)
     got = run(mixed_cfg(cfg, tlq.COOL_MLP, **EXACT), U0, 100, net=net)
+    mix = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE, **EXACT), U0, 100)  # the mixed form's own share
+    drift_mix = abs(mix["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4])
+    drift_net = abs(got["sums"][4] - mix["sums"][4]) / abs(ref["sums"][4])
     assert got["rc"] == tlq.OK and got["it"] == 100
     err = rel_l1(interior(got["W"])[0], interior(ref["W"])[0])
     drift = abs(got["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4])
     frac_fb = got["fb"] / max(1, got["fb"] + got["mlp"])
-    print(f"wind64 surrogate: L1 rho {err:.3e} drift {drift:.3e} fallback {frac_fb:.4f} "
-          f"(mlp {got['mlp']}, fallback {got['fb']})")
+    print(f"wind64 surrogate: L1 rho {err:.3e} drift {drift:.3e} (mixed form alone {drift_mix:.3e}, surrogate "
+          f"against it {drift_net:.3e}) fallback {frac_fb:.4f} (mlp {got['mlp']}, fallback {got['fb']})")
     assert err <= 1e-2 and drift <= 1e-6
     assert got["mlp"] > 0
 

@@ -167,6 +167,8 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.out = ctx->U[par ^ 1];
   a.pout = ctx->Pc;
   a.use_p = 0;
+  a.cqueue = ctx->mlp_cqueue;
+  a.cqcount = ctx->mlp_qcount ? ctx->mlp_qcount + 1 : nullptr;
   if (mixed)
     CK(launch_stage_mixed(2, ctx->tm_UPP, a, ctx->grid, ctx->stream));
   else
@@ -174,9 +176,9 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
-    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[par ^ 1], ctx->clk, ctx->partials, ctx->mlp_params, ctx->mlp_norm,
-                          ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts, ctx->mlp_queue, ctx->mlp_qcount,
-                          ctx->stream));
+    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[par ^ 1], ctx->clk, ctx->partials, ctx->npartials,
+                          ctx->mlp_params, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
+                          ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[3], ctx->stream));
   return TLQ_OK;
 }
@@ -337,9 +339,10 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   }
   if (cfg->cooling == TLQ_COOL_MLP) {
     const size_t ncell = (size_t)cfg->nx * cfg->ny * cfg->nz;
-    if (cudaMalloc(&ctx->mlp_queue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_qcount, sizeof(unsigned)))
+    if (cudaMalloc(&ctx->mlp_queue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_cqueue, ncell * sizeof(unsigned)) ||
+        cudaMalloc(&ctx->mlp_qcount, 2 * sizeof(unsigned)))
       return bail(TLQ_ERR_NOMEM);
-    cudaMemset(ctx->mlp_qcount, 0, sizeof(unsigned));
+    cudaMemset(ctx->mlp_qcount, 0, 2 * sizeof(unsigned));
   }
   if (cudaMalloc(&ctx->clk, sizeof(Clock)) || cudaMallocHost(&ctx->clk_host, sizeof(Clock))) return bail(TLQ_ERR_NOMEM);
   std::memset(ctx->clk_host, 0, sizeof(Clock));
@@ -352,9 +355,9 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   ctx->grid = dim3(gx, gy, gz);
   ctx->npartials = gx * gy * gz;
   const int nb = init_blocks(ctx->P);
-  // (tiles down to 8-plane z-chunks, which a batch's tuner may choose)
-  const int npart = std::max(std::max(std::max(ctx->npartials, nb), cool_mlp_blocks(ctx->P)),
-                             gx * gy * ((cfg->nz + 7) / 8));
+  // (tiles down to 8-plane z-chunks, which a tuner may choose; with the
+  // surrogate, stage 2's tiles then the cooling passes' blocks)
+  const int npart = std::max(nb, gx * gy * ((cfg->nz + 7) / 8) + cool_mlp_blocks(ctx->P));
   if (cudaMalloc(&ctx->partials, sizeof(double) * 3 * (size_t)npart) ||
       cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
     return bail(TLQ_ERR_NOMEM);
@@ -380,7 +383,7 @@ int tlq_destroy(tlq_ctx* ctx) {
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
   cudaFree(ctx->mlp_params); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
-  cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_qcount);
+  cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_qcount);
   cudaFree(ctx->clk); cudaFree(ctx->partials); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);

@@ -67,8 +67,9 @@ struct tlq_ctx {
   float* gslope = nullptr;                 // per-segment power-law slopes
   unsigned long long* cool_counts = nullptr;  // device: cells cooled by the network / by the fallback
   double cool_tmin = 0.0;                  // the table's first temperature
+  unsigned* mlp_cqueue = nullptr;          // cells that cool, queued by stage 2 (capacity nx ny nz)
   unsigned* mlp_queue = nullptr;           // cells handed to the exact integrator (capacity nx ny nz)
-  unsigned* mlp_qcount = nullptr;          // their number (zero between steps)
+  unsigned* mlp_qcount = nullptr;          // [0]: fallback queue length, [1]: cooling queue length (zero between steps)
   std::string err;
 };
 

@@ -71,14 +71,17 @@ cudaError_t launch_gather_pairs(const float* X, const float* Y, const float* Wt,
                                 float* X2, float* Y2, float* Wt2, cudaStream_t s);
 cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStream_t s);
 // Surrogate cooling + dt reduction of the mixed step (tlq_surrogate.cu).
-// The network's pass queues the cells it hands to the exact integrator
-// (queue: capacity nx ny nz; qcount: zero between steps); the fallback pass
-// cools them and finishes the dt reduction over both passes' block maxima.
+// Stage 2 queues the cells that cool (cqueue) and leaves its nstage block
+// maxima in partials; the network pass cools them or queues them for the
+// exact integrator (queue); the fallback pass cools those and finishes the
+// dt reduction over all block maxima.  Queues: capacity nx ny nz; counts
+// zero between steps.
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Clock* clk, double* partials,
-                               const float* P, const float norm[6], const double box[6], const float* gcum,
-                               const float* gslope, unsigned long long* counts, unsigned* queue, unsigned* qcount,
+                               int nstage, const float* P, const float norm[6], const double box[6],
+                               const float* gcum, const float* gslope, unsigned long long* counts,
+                               const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
                                cudaStream_t s);
-int cool_mlp_blocks(const Params& p);  // block maxima both passes leave in partials
+int cool_mlp_blocks(const Params& p);  // block maxima both passes add to partials
 
 // log10 of a small device array in place (cooling-table temperatures).
 cudaError_t launch_log10_inplace(double* v, int n, cudaStream_t s);

@@ -37,6 +37,8 @@ struct StageArgs {
   int zlen;            // planes per block
   int use_p;           // STAGE 1 with cooling: interior pressure from the P plane
   float* lapf;         // mixed form: eta * Laplacian of U (FP32, written by stage 1, read by stage 2)
+  unsigned* cqueue;    // mixed form with the cooling surrogate: stage 2 queues the cells that cool
+  unsigned* cqcount;
 };
 
 template <class R>

@@ -321,6 +321,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
     double uc[5];
     float lv[5];
     double ph[6];
+    bool queued = false;  // stage 2 with the surrogate: handed to the cooling passes
     if (cell_ok) {
 #pragma unroll
       for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
@@ -394,15 +395,35 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         for (int e = 0; e < 5; ++e) un[e] = up[e] + f2d(lv[e]);
         float cf[5], w[5];
         mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
-        if (p.cooling != COOL_NONE && p.cooling != COOL_MLP) cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
+        if (p.cooling == COOL_MLP) {
+          // the surrogate's passes cool this cell and take its signal speeds
+          queued = cools_at(p, (w[4] / w[0]) * cT, un);
+        } else if (p.cooling != COOL_NONE) {
+          cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
+        }
         if (!(un[0] > 0.0)) atomicOr(&clk->status, ST_NEG_DENSITY);
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
-        const float cs = sqrtf(gf * w[4] / w[0]);
-        const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
-        m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
-        m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
-        m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
+        if (!queued) {
+          const float cs = sqrtf(gf * w[4] / w[0]);
+          const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
+          m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
+          m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
+          m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
+        }
+      }
+    }
+    if (STAGE == 2 && p.cooling == COOL_MLP) {
+      // warp-aggregated append to the cooling queue (interior cell index)
+      const unsigned qm = __ballot_sync(0xffffffffu, queued);
+      if (qm) {
+        const int lane = tid & 31;
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(a.cqcount, (unsigned)__popc(qm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (queued)
+          a.cqueue[base + __popc(qm & ((1u << lane) - 1u))] =
+              (unsigned)((i - 1) + p.nx * ((long long)(j - 1) + (long long)p.ny * (k - 1)));
       }
     }
   }
@@ -419,9 +440,20 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
     }
     d0 = d1 = d2 = NAN;
   }
-  // with the surrogate, cooling and the dt reduction follow in their own kernel
-  if (STAGE == 2 && p.cooling != COOL_MLP)
-    cfl_reduce_finalize_n<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag, 0, nblk, bid);
+  if (STAGE == 2) {
+    if (p.cooling != COOL_MLP) {
+      cfl_reduce_finalize_n<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag, 0, nblk, bid);
+    } else {
+      // with the surrogate the cooling passes finish the reduction over
+      // these block maxima and their own
+      block_max3<NT>(d0, d1, d2, s.red);
+      if (tid == 0) {
+        a.partials[3 * bid + 0] = d0;
+        a.partials[3 * bid + 1] = d1;
+        a.partials[3 * bid + 2] = d2;
+      }
+    }
+  }
 }
 
 template <int STAGE>

@@ -70,8 +70,9 @@ __device__ __forceinline__ float g_inv(const CoolTable& t, const SurrogateArgs& 
   return fabsf(a) < 1e-4f ? Tj * __expf(q) : Tj * __powf(fmaxf(1.0f + a * q, 0.0f), 1.0f / a);
 }
 
-constexpr int CT = 128;   // threads per block of the network pass
-constexpr int FT = 128;   // threads per block of the fallback pass
+constexpr int CT = 128;      // threads per block of the network pass
+constexpr int CB = 152 * 4;  // blocks of the network pass
+constexpr int FT = 128;      // threads per block of the fallback pass
 constexpr int FB = 152 * 4;  // blocks of the fallback pass
 
 __device__ __forceinline__ void speeds_max(const float* w, float gf, float& m0, float& m1, float& m2) {
@@ -90,17 +91,19 @@ __device__ __forceinline__ long long interior_offset(const Params& p, const Layo
   return L.at(i, j, k);
 }
 
-// Pass 1: for every interior cell, the network's prediction where the cell
-// cools and lies in the training box, accepted when the residual check
-// passes; the other cooling cells are queued for the exact integrator, and
-// so are the cells whose cooling reaches the table's first temperature
-// within the step (closed form: G_t <= 0): there the reference integrator's
-// last sub-step decides how far below that temperature the cell ends.  The
-// block maxima of the signal speeds of all cells not queued go to
-// partials[0 .. 3 gridDim.x).
-__global__ void __launch_bounds__(CT) k_cool_mlp(Params p, Layout L, double* __restrict__ U, const Clock* clk,
-                                                 double* partials, SurrogateArgs sa, unsigned* __restrict__ queue,
-                                                 unsigned* qcount) {
+// Pass 1 (network): stage 2 queued the interior cells that cool (temp >=
+// the table's first temperature, cooling.f90:71).  For each, densely, 32 to
+// a warp: the network's prediction where the cell lies in the training box,
+// accepted when the residual check passes; the others go to the fallback
+// queue for the exact integrator, and so do the cells whose cooling reaches
+// the table's first temperature within the step (closed form: G_t <= 0):
+// there the reference integrator's last sub-step decides how far below that
+// temperature the cell ends.  The block maxima of the signal speeds of the
+// accepted cells go to partials after the stage-2 blocks' (nprev of them).
+__global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* __restrict__ U, const Clock* clk,
+                                                 double* partials, unsigned nprev, SurrogateArgs sa,
+                                                 const unsigned* __restrict__ cqueue, const unsigned* cqcount,
+                                                 unsigned* __restrict__ queue, unsigned* qcount) {
   __shared__ mlp::SmemWeights W;
   __shared__ double red[96];
   if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
@@ -112,15 +115,17 @@ __global__ void __launch_bounds__(CT) k_cool_mlp(Params p, Layout L, double* __r
   const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
   const float dtf = (float)clk->dt;
   const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-  const long long n = (long long)p.nx * p.ny * p.nz;
+  const long long n = (long long)*cqcount;
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
   unsigned long long used = 0, fell = 0;
+  // warp-uniform trip count: the network's tiles need all 32 lanes
   for (long long base = (long long)blockIdx.x * CT; base < n; base += (long long)gridDim.x * CT) {
-    const long long cidx = base + threadIdx.x;
-    const bool valid = cidx < n;
-    long long o = 0;
+    const long long q = base + threadIdx.x;
+    const bool valid = q < n;
+    long long o = 0, cidx = 0;
     double u[5] = {1.0, 0.0, 0.0, 0.0, 1.0};
     if (valid) {
+      cidx = cqueue[q];
       o = interior_offset(p, L, cidx);
 #pragma unroll
       for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
@@ -194,7 +199,7 @@ __global__ void __launch_bounds__(CT) k_cool_mlp(Params p, Layout L, double* __r
     }
     used += ok ? 1 : 0;
     fell += queued ? 1 : 0;
-    if (valid && !queued) speeds_max(w, gf, m0, m1, m2);
+    if (ok) speeds_max(w, gf, m0, m1, m2);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -208,18 +213,20 @@ __global__ void __launch_bounds__(CT) k_cool_mlp(Params p, Layout L, double* __r
   double a = f2d(m0), b = f2d(m1), c = f2d(m2);
   block_max3<CT>(a, b, c, red);
   if (threadIdx.x == 0) {
-    partials[3 * blockIdx.x + 0] = a;
-    partials[3 * blockIdx.x + 1] = b;
-    partials[3 * blockIdx.x + 2] = c;
+    partials[3 * (nprev + blockIdx.x) + 0] = a;
+    partials[3 * (nprev + blockIdx.x) + 1] = b;
+    partials[3 * (nprev + blockIdx.x) + 2] = c;
   }
 }
 
-// Pass 2: the queued cells through the exact integrator (the sub-cycled
-// cooling with the run's sub-step settings), then the dt reduction over the
-// block maxima of both passes; the last block empties the queue.
+// Pass 2 (fallback): the queued cells through the exact integrator (the
+// sub-cycled cooling with the run's sub-step settings), then the dt
+// reduction over the block maxima of stage 2 and both passes (nprev before
+// this pass's); the last block empties both queues.
 __global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, double* __restrict__ U, Clock* clk,
-                                                         double* partials, unsigned npass1,
-                                                         const unsigned* __restrict__ queue, unsigned* qcount) {
+                                                         double* partials, unsigned nprev,
+                                                         const unsigned* __restrict__ queue, unsigned* qcount,
+                                                         unsigned* cqcount) {
   __shared__ double red[96];
   __shared__ int flag;
   if (!(clk->t < clk->tfin)) return;
@@ -240,20 +247,19 @@ __global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, dou
     U[4 * L.plane + o] = u[4];
     speeds_max(w, gf, m0, m1, m2);
   }
-  cfl_reduce_finalize<FT>(f2d(m0), f2d(m1), f2d(m2), partials, clk, p, true, red, &flag, npass1);
-  if (flag && threadIdx.x == 0) *qcount = 0u;
-}
-
-int cool_blocks(const Params& p) {
-  const long long n = (long long)p.nx * p.ny * p.nz;
-  return (int)std::max<long long>(1, std::min<long long>((n + CT - 1) / CT, 152LL * 8));
+  cfl_reduce_finalize<FT>(f2d(m0), f2d(m1), f2d(m2), partials, clk, p, true, red, &flag, nprev);
+  if (flag && threadIdx.x == 0) {
+    *qcount = 0u;
+    *cqcount = 0u;
+  }
 }
 
 }  // namespace
 
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Clock* clk, double* partials,
-                               const float* P, const float norm[6], const double box[6], const float* gcum,
-                               const float* gslope, unsigned long long* counts, unsigned* queue, unsigned* qcount,
+                               int nstage, const float* P, const float norm[6], const double box[6],
+                               const float* gcum, const float* gslope, unsigned long long* counts,
+                               const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
                                cudaStream_t s) {
   // the fallback is the sub-cycled integrator with the run's sub-step settings
   Params pf = p;
@@ -267,15 +273,14 @@ cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Cloc
   sa.gcum = gcum;
   sa.gslope = gslope;
   sa.counts = counts;
-  const int nb1 = cool_blocks(p);
-  k_cool_mlp<<<nb1, CT, 0, s>>>(pf, L, U, clk, partials, sa, queue, qcount);
+  k_cool_net<<<CB, CT, 0, s>>>(pf, L, U, clk, partials, (unsigned)nstage, sa, cqueue, cqcount, queue, qcount);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cool_fallback_dt<<<FB, FT, 0, s>>>(pf, L, U, clk, partials, (unsigned)nb1, queue, qcount);
+  k_cool_fallback_dt<<<FB, FT, 0, s>>>(pf, L, U, clk, partials, (unsigned)(nstage + CB), queue, qcount, cqcount);
   return cudaGetLastError();
 }
 
-int cool_mlp_blocks(const Params& p) { return cool_blocks(p) + FB; }
+int cool_mlp_blocks(const Params&) { return CB + FB; }
 
 }  // namespace tlq
 
