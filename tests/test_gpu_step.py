@@ -264,3 +264,39 @@ def test_sedov_128_against_similarity_solution(gpu_lib, golden):
     exact = analysis.sedov_density(rc, t, golden["sedov53"])
     inner = ok & (rc < 1.2 * Rs)
     assert analysis.norm_L1(exact[inner], prof[inner]) == pytest.approx(g["L1_rho"], rel=1e-9)
+
+
+@pytest.mark.parametrize("precision", [tlq.PREC_FP64, tlq.PREC_MIXED])
+def test_page_locked_host_arrays_take_the_direct_path(gpu_lib, precision):
+    """tlq_upload / tlq_download with page-locked host arrays (the layout
+    conversion reads and writes them directly over the host link) give the
+    same bits as with pageable arrays (staging copy)."""
+    import torch
+    cfg, U0 = problems.wind_bubble(24)
+    cfg = tlq.Config(**{**cfg.__dict__, "precision": precision})
+    U1 = U0.copy(order="F")
+
+    def pinned():
+        t = torch.zeros((cfg.nz + 4, cfg.ny + 4, cfg.nx + 4, 5), dtype=torch.float64, pin_memory=True)
+        return t, t.numpy().transpose(3, 2, 1, 0)  # Fortran-ordered view, the reference layout
+
+    outs = []
+    for pin in (False, True):
+        with tlq.Context(cfg) as ctx:
+            ctx.borders(U1, 1)
+            if pin:
+                keep, Up = pinned()
+                Up[...] = U1
+                ctx.upload(Up)
+            else:
+                ctx.upload(U1.copy(order="F"))
+            ctx.advance(4)
+            if pin:
+                k2, Uo = pinned()
+                k3, Wo = pinned()
+                ctx.download(Uo, Wo)
+                outs.append((Uo.copy(), Wo.copy()))
+            else:
+                outs.append(ctx.state())
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])

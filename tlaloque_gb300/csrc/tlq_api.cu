@@ -7,6 +7,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -132,6 +133,23 @@ int ensure_routine_scratch(tlq_ctx* ctx) {
 // interior pressures); the mixed form recomputes the pressure from U.
 bool carries_pressure(const tlq_ctx* c) {
   return c->cfg.cooling != TLQ_COOL_NONE && c->cfg.precision == TLQ_PREC_FP64;
+}
+
+// The device-visible address of a page-locked host array (cudaHostAlloc'd or
+// registered), or null for pageable memory.  Layout conversions then read or
+// write the host array directly over the host link (no staging copy).
+const void* mapped_host(const void* p) {
+  static const bool off = [] {
+    const char* e = std::getenv("TLQ_HOST_DIRECT");
+    return e && e[0] == '0';
+  }();
+  if (off) return nullptr;  // TLQ_HOST_DIRECT=0: always through the staging buffer
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (at.type == cudaMemoryTypeHost) ? at.devicePointer : nullptr;
 }
 
 int status_from_bits(int bits) {
@@ -517,8 +535,12 @@ int tlq_upload(tlq_ctx* ctx, const double* U) {
   if (!ctx || !U) return TLQ_ERR_ARG;
   if (ctx->cfg.cooling != TLQ_COOL_NONE && !ctx->dT) return fail(ctx, TLQ_ERR_STATE, "cooling on but no cooling table");
   if (ctx->cool_counts) CK(cudaMemsetAsync(ctx->cool_counts, 0, 2 * sizeof(unsigned long long), ctx->stream));
-  CK(cudaMemcpyAsync(ctx->staging, U, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_aos_to_soa(ctx->A, ctx->L, ctx->staging, ctx->U[0], ctx->stream));
+  if (const double* hU = static_cast<const double*>(mapped_host(U))) {
+    CK(launch_aos_to_soa(ctx->A, ctx->L, hU, ctx->U[0], ctx->stream));
+  } else {
+    CK(cudaMemcpyAsync(ctx->staging, U, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_aos_to_soa(ctx->A, ctx->L, ctx->staging, ctx->U[0], ctx->stream));
+  }
   Clock c{};
   c.t = ctx->t0;
   c.it = ctx->it0;
@@ -541,13 +563,21 @@ int tlq_download(tlq_ctx* ctx, double* U, double* W) {
   int rc = read_clock(ctx);
   if (rc) return rc;
   if (U) {
-    CK(launch_soa_to_aos(ctx->A, ctx->L, ctx->U[ctx->cur], ctx->staging, ctx->stream));
-    CK(cudaMemcpyAsync(U, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
+    if (double* hU = static_cast<double*>(const_cast<void*>(mapped_host(U)))) {
+      CK(launch_soa_to_aos(ctx->A, ctx->L, ctx->U[ctx->cur], hU, ctx->stream));
+    } else {
+      CK(launch_soa_to_aos(ctx->A, ctx->L, ctx->U[ctx->cur], ctx->staging, ctx->stream));
+      CK(cudaMemcpyAsync(U, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
+    }
   }
   if (W) {
-    CK(launch_prims_soa_to_aos(ctx->P, ctx->A, ctx->L, ctx->U[ctx->cur], carries_pressure(ctx) ? ctx->Pc : nullptr,
-                               ctx->staging, ctx->stream));
-    CK(cudaMemcpyAsync(W, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
+    const double* Pc = carries_pressure(ctx) ? ctx->Pc : nullptr;
+    if (double* hW = static_cast<double*>(const_cast<void*>(mapped_host(W)))) {
+      CK(launch_prims_soa_to_aos(ctx->P, ctx->A, ctx->L, ctx->U[ctx->cur], Pc, hW, ctx->stream));
+    } else {
+      CK(launch_prims_soa_to_aos(ctx->P, ctx->A, ctx->L, ctx->U[ctx->cur], Pc, ctx->staging, ctx->stream));
+      CK(cudaMemcpyAsync(W, ctx->staging, array_bytes(ctx->cfg), cudaMemcpyDeviceToHost, ctx->stream));
+    }
   }
   CK(cudaStreamSynchronize(ctx->stream));
   return TLQ_OK;

@@ -36,52 +36,80 @@ cudaError_t launch_stage(int stage, int /*precision*/, const CUtensorMap& tm_in,
 }
 
 // ===========================================================================
-// Layout conversions (reference AoS <-> device SoA), all cells.
+// Layout conversions (reference AoS <-> device SoA), all cells.  A block
+// moves BT consecutive cells at a time through shared memory, so that the
+// AoS side (5 * BT contiguous doubles, possibly a page-locked host array read
+// or written over the host link) is touched with fully coalesced accesses and
+// the SoA side with one coalesced access per variable.
 // ===========================================================================
-__global__ void k_aos_to_soa(Aos A, Layout L, const double* __restrict__ src, double* __restrict__ dst) {
+__device__ __forceinline__ long long soa_offset(const Aos& A, const Layout& L, long long c) {
+  const int i = (int)(c % (A.nx + 4)) - 1;
+  const long long r = c / (A.nx + 4);
+  const int j = (int)(r % (A.ny + 4)) - 1;
+  const int k = (int)(r / (A.ny + 4)) - 1;
+  return L.at(i, j, k);
+}
+
+__global__ void __launch_bounds__(BT) k_aos_to_soa(Aos A, Layout L, const double* __restrict__ src,
+                                                   double* __restrict__ dst) {
+  __shared__ double sh[5 * BT];
   const long long n = A.cells();
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % (A.nx + 4)) - 1;
-    const long long r = c / (A.nx + 4);
-    const int j = (int)(r % (A.ny + 4)) - 1;
-    const int k = (int)(r / (A.ny + 4)) - 1;
-    const long long o = L.at(i, j, k);
+  for (long long base = (long long)blockIdx.x * BT; base < n; base += (long long)gridDim.x * BT) {
+    const int cnt = (int)min((long long)BT, n - base);
+    for (int t = threadIdx.x; t < 5 * cnt; t += BT) sh[t] = src[5 * base + t];
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const long long o = soa_offset(A, L, base + threadIdx.x);
 #pragma unroll
-    for (int e = 0; e < 5; ++e) dst[e * L.plane + o] = src[5 * c + e];
+      for (int e = 0; e < 5; ++e) dst[e * L.plane + o] = sh[5 * threadIdx.x + e];
+    }
+    __syncthreads();
   }
 }
 
-__global__ void k_soa_to_aos(Aos A, Layout L, const double* __restrict__ src, double* __restrict__ dst) {
+__global__ void __launch_bounds__(BT) k_soa_to_aos(Aos A, Layout L, const double* __restrict__ src,
+                                                   double* __restrict__ dst) {
+  __shared__ double sh[5 * BT];
   const long long n = A.cells();
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % (A.nx + 4)) - 1;
-    const long long r = c / (A.nx + 4);
-    const int j = (int)(r % (A.ny + 4)) - 1;
-    const int k = (int)(r / (A.ny + 4)) - 1;
-    const long long o = L.at(i, j, k);
+  for (long long base = (long long)blockIdx.x * BT; base < n; base += (long long)gridDim.x * BT) {
+    const int cnt = (int)min((long long)BT, n - base);
+    if (threadIdx.x < cnt) {
+      const long long o = soa_offset(A, L, base + threadIdx.x);
 #pragma unroll
-    for (int e = 0; e < 5; ++e) dst[5 * c + e] = src[e * L.plane + o];
+      for (int e = 0; e < 5; ++e) sh[5 * threadIdx.x + e] = src[e * L.plane + o];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 5 * cnt; t += BT) dst[5 * base + t] = sh[t];
+    __syncthreads();
   }
 }
 
 // UPrim for output: calc_prims of every cell, with the carried (cooled)
 // pressure on the interior when P is given (apply_cooling updates UPrim(5)).
-__global__ void k_prims_soa_to_aos(Params p, Aos A, Layout L, const double* __restrict__ U,
-                                   const double* __restrict__ P, double* __restrict__ W) {
+__global__ void __launch_bounds__(BT) k_prims_soa_to_aos(Params p, Aos A, Layout L, const double* __restrict__ U,
+                                                         const double* __restrict__ P, double* __restrict__ W) {
+  __shared__ double sh[5 * BT];
   const long long n = A.cells();
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % (A.nx + 4)) - 1;
-    const long long r = c / (A.nx + 4);
-    const int j = (int)(r % (A.ny + 4)) - 1;
-    const int k = (int)(r / (A.ny + 4)) - 1;
-    const long long o = L.at(i, j, k);
-    double u[5], w[5];
+  for (long long base = (long long)blockIdx.x * BT; base < n; base += (long long)gridDim.x * BT) {
+    const int cnt = (int)min((long long)BT, n - base);
+    if (threadIdx.x < cnt) {
+      const long long c = base + threadIdx.x;
+      const int i = (int)(c % (A.nx + 4)) - 1;
+      const long long r = c / (A.nx + 4);
+      const int j = (int)(r % (A.ny + 4)) - 1;
+      const int k = (int)(r / (A.ny + 4)) - 1;
+      const long long o = L.at(i, j, k);
+      double u[5], w[5];
 #pragma unroll
-    for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
-    cons2prim(p.gamma, u, w);
-    if (P && i >= 1 && i <= p.nx && j >= 1 && j <= p.ny && k >= 1 && k <= p.nz) w[4] = P[o];
+      for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
+      cons2prim(p.gamma, u, w);
+      if (P && i >= 1 && i <= p.nx && j >= 1 && j <= p.ny && k >= 1 && k <= p.nz) w[4] = P[o];
 #pragma unroll
-    for (int e = 0; e < 5; ++e) W[5 * c + e] = w[e];
+      for (int e = 0; e < 5; ++e) sh[5 * threadIdx.x + e] = w[e];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 5 * cnt; t += BT) W[5 * base + t] = sh[t];
+    __syncthreads();
   }
 }
 
