@@ -207,6 +207,20 @@ int tlq_mlp_loss_grad(const float* params, const float* X, const float* Y, const
                       float* loss);
 int tlq_mlp_infer(const float* params, const float* X, int n, float* Y);
 
+/* Output, source/HydroCore.f90:253-395 (`output`): UPrim of the current
+ * state (after the steps queued so far) written in the reference's format --
+ * BIN (all cells, little-endian, file points<rank>N<nout>.bin), DAT (text,
+ * the interior, points<rank>N<nout>.dat; needs |nx - nz| <= 2, the
+ * reference's loop bounds) or VTK (big-endian structured points,
+ * EPV<rank>N<nout>.vtk) -- under outputpath.  Asynchronous: the snapshot is
+ * formed behind the queued steps, copied on a copy stream and written by a
+ * host thread while later steps run; one output is in flight at a time
+ * (the next call waits for the previous one).  tlq_output_wait waits and
+ * returns the write's status. */
+enum { TLQ_OUT_DAT = 1, TLQ_OUT_VTK = 2, TLQ_OUT_BIN = 3 }; /* constants.f90:35-37 */
+int tlq_output(tlq_ctx* ctx, int format, const char* outputpath, int nout, int rank);
+int tlq_output_wait(tlq_ctx* ctx);
+
 /* Stage tiling (no counterpart in the reference): the z-chunk length of the
  * stage grid (>= 8 planes, or nz; default 64 for nz >= 128, 32 for nz >= 32,
  * else nz), and the measuring autotuner that picks it -- from the cache file

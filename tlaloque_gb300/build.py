@@ -33,6 +33,7 @@ UNITS = [
     ("tlq_mlp.cu", []),
     ("tlq_surrogate.cu", ["--use_fast_math"]),
     ("tlq_batch.cu", ["--use_fast_math"]),
+    ("tlq_output.cu", []),
 ]
 
 

@@ -395,6 +395,7 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
 int tlq_destroy(tlq_ctx* ctx) {
   if (!ctx) return TLQ_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  output_free(ctx);
   invalidate_graphs(ctx);
   for (int q = 0; q < 4; ++q)
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);

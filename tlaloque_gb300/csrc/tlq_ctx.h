@@ -2,6 +2,7 @@
 #pragma once
 
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/tlq.h"
@@ -70,8 +71,17 @@ struct tlq_ctx {
   unsigned* mlp_cqueue = nullptr;          // cells that cool, queued by stage 2 (capacity nx ny nz)
   unsigned* mlp_queue = nullptr;           // cells handed to the exact integrator (capacity nx ny nz)
   unsigned* mlp_qcount = nullptr;          // [0]: fallback queue length, [1]: cooling queue length (zero between steps)
+  // output path (tlq_output.cu): device snapshot, page-locked copy, writer thread
+  double* out_dev = nullptr;
+  double* out_host = nullptr;
+  cudaStream_t out_stream = nullptr;
+  cudaEvent_t out_ev[2] = {nullptr, nullptr};
+  std::thread out_thread;
+  int out_rc = 0;
   std::string err;
 };
+
+void output_free(tlq_ctx* ctx);  // waits for a pending output, frees its buffers
 
 // Closed-form cooling-time integral of the table for the surrogate's
 // residual check (tlq_surrogate.cu); called by tlq_set_cooling_table.

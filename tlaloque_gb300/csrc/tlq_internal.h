@@ -45,6 +45,9 @@ cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageA
 // Layout conversions and per-step helpers (SoA device state).
 cudaError_t launch_aos_to_soa(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_prims_soa_to_aos_clocked(const Params& p, const Aos& A, const Layout& L, const double* U0,
+                                            const double* U1, const Clock* clk, long long it_base, const double* P,
+                                            double* W, cudaStream_t s);
 cudaError_t launch_prims_soa_to_aos(const Params& p, const Aos& A, const Layout& L, const double* U,
                                     const double* P, double* W, cudaStream_t s);
 // calc_prims + time_step on the uploaded state; writes P (interior pressure)

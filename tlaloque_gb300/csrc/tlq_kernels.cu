@@ -86,9 +86,14 @@ __global__ void __launch_bounds__(BT) k_soa_to_aos(Aos A, Layout L, const double
 
 // UPrim for output: calc_prims of every cell, with the carried (cooled)
 // pressure on the interior when P is given (apply_cooling updates UPrim(5)).
-__global__ void __launch_bounds__(BT) k_prims_soa_to_aos(Params p, Aos A, Layout L, const double* __restrict__ U,
+// With a clock, the state is U or U1 by the clock's buffer parity
+// ((it - it_base) & 1), so that the kernel can be queued behind steps whose
+// count the host does not know yet.
+__global__ void __launch_bounds__(BT) k_prims_soa_to_aos(Params p, Aos A, Layout L, const double* U0,
+                                                         const double* U1, const Clock* clk, long long it_base,
                                                          const double* __restrict__ P, double* __restrict__ W) {
   __shared__ double sh[5 * BT];
+  const double* __restrict__ U = (clk && ((clk->it - it_base) & 1LL)) ? U1 : U0;
   const long long n = A.cells();
   for (long long base = (long long)blockIdx.x * BT; base < n; base += (long long)gridDim.x * BT) {
     const int cnt = (int)min((long long)BT, n - base);
@@ -128,7 +133,13 @@ cudaError_t launch_soa_to_aos(const Aos& A, const Layout& L, const double* src, 
 }
 cudaError_t launch_prims_soa_to_aos(const Params& p, const Aos& A, const Layout& L, const double* U, const double* P,
                                     double* W, cudaStream_t s) {
-  k_prims_soa_to_aos<<<conv_blocks(A), BT, 0, s>>>(p, A, L, U, P, W);
+  k_prims_soa_to_aos<<<conv_blocks(A), BT, 0, s>>>(p, A, L, U, U, nullptr, 0, P, W);
+  return cudaGetLastError();
+}
+cudaError_t launch_prims_soa_to_aos_clocked(const Params& p, const Aos& A, const Layout& L, const double* U0,
+                                            const double* U1, const Clock* clk, long long it_base, const double* P,
+                                            double* W, cudaStream_t s) {
+  k_prims_soa_to_aos<<<conv_blocks(A), BT, 0, s>>>(p, A, L, U0, U1, clk, it_base, P, W);
   return cudaGetLastError();
 }
 

@@ -23,6 +23,7 @@ SOLVER_HLLC, SOLVER_HLL = 0, 1
 COOL_NONE, COOL_REF, COOL_SUBCYCLE, COOL_MLP = 0, 1, 2, 3
 MLP_NPARAM = 8641
 PREC_FP64, PREC_MIXED = 0, 1
+OUT_DAT, OUT_VTK, OUT_BIN = 1, 2, 3
 
 # Every function the header declares (checked by the CPU test suite).
 EXPORTS = (
@@ -33,7 +34,7 @@ EXPORTS = (
     "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
     "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
     "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
-    "tlq_set_tfin", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
+    "tlq_set_tfin", "tlq_output", "tlq_output_wait", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
     "tlq_batch_set_tiling", "tlq_batch_get_tiling", "tlq_batch_autotune", "tlq_batch_run", "tlq_batch_synchronize",
     "tlq_batch_status", "tlq_batch_enable_timing", "tlq_batch_stats_get", "tlq_batch_last_error",
 )
@@ -106,6 +107,8 @@ def load_library(path: str = LIB_PATH):
         "tlq_create": (I, [C.POINTER(CConfig), C.POINTER(V)]),
         "tlq_destroy": (I, [V]),
         "tlq_set_tfin": (I, [V, C.c_double]),
+        "tlq_output": (I, [V, I, C.c_char_p, I, I]),
+        "tlq_output_wait": (I, [V]),
         "tlq_set_tiling": (I, [V, I]),
         "tlq_get_tiling": (I, [V, C.POINTER(I)]),
         "tlq_autotune": (I, [V, C.c_char_p, I, C.POINTER(I)]),
@@ -355,6 +358,14 @@ class Context:
         self._check(self.L.tlq_run_until(self.h, float(tfin), int(max_steps), C.byref(t), C.byref(it), C.byref(dt)),
                     "run_until")
         return t.value, it.value, dt.value
+
+    def output(self, fmt: int, outputpath: str, nout: int, rank: int = 0):
+        """Asynchronous output of UPrim in the reference's format (OUT_BIN,
+        OUT_DAT, OUT_VTK); returns at once, output_wait() waits."""
+        self._check(self.L.tlq_output(self.h, int(fmt), outputpath.encode(), int(nout), int(rank)), "output")
+
+    def output_wait(self):
+        self._check(self.L.tlq_output_wait(self.h), "output_wait")
 
     def set_tiling(self, zlen: int):
         self._check(self.L.tlq_set_tiling(self.h, int(zlen)), "set_tiling")
