@@ -81,6 +81,19 @@ typedef struct tlq_wind {
   double mu;          /* wind mean particle mass [AMU] */
 } tlq_wind;
 
+/* plane_wind_type, source/winds.f90:15-28: a uniform stream entering
+ * through one face (plane 1..6 = left, right, front, back, bottom, top; the
+ * velocity points into the box).  Imposed like the reference's
+ * imposePlaneWind (winds.f90:92-147), which writes every i, j and the top
+ * three z-planes k = nz..nz+2 whatever the plane. */
+typedef struct tlq_plane_wind {
+  int plane;
+  double rho;   /* density */
+  double vel;   /* speed */
+  double temp;  /* temperature [K] */
+  double mu;    /* mean particle mass [AMU] */
+} tlq_plane_wind;
+
 /* Learned cooling surrogate (build-defined; the reference has none).  A
  * 3-64-64-64-1 SiLU network maps (log10 n, log10 T, log10 tau), tau =
  * Lambda(T) n^2 dt / E_th the step's cooling number, to r with
@@ -154,6 +167,9 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* log10_lam
 int tlq_set_winds(tlq_ctx* ctx, const tlq_wind* winds, int n);
 /* Point masses (x, y, z, M per mass) of pgravity (source/pointsource_gravity.f90:12-39);
  * the reference hard-codes M = 8 Msun (:23).  Copied; enables the source term. */
+/* Plane winds imposed with the spherical ones in every ghost fill of the
+ * step (user_boundaries), at most 6; n = 0 clears them. */
+int tlq_set_plane_winds(tlq_ctx* ctx, const tlq_plane_wind* w, int n);
 int tlq_set_point_masses(tlq_ctx* ctx, const double* xyzm, int n);
 
 /* State transfer.  tlq_upload takes U after borders(U,1) (mainHD.f90:38) and

@@ -31,6 +31,11 @@ class _Wind(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("xc", "yc", "zc", "vx", "vy", "vz", "radius", "mdot", "vinf", "temp", "mu")]
 
 
+class _PlaneWind(C.Structure):
+    _fields_ = [("plane", C.c_int), ("rho", C.c_double), ("vel", C.c_double), ("temp", C.c_double),
+                ("mu", C.c_double)]
+
+
 class _Params(C.Structure):
     _fields_ = [
         ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
@@ -44,6 +49,7 @@ class _Params(C.Structure):
         ("nwinds", C.c_int), ("winds", C.POINTER(_Wind)),
         ("nmasses", C.c_int), ("masses", C.POINTER(C.c_double)),
         ("nthreads", C.c_int),
+        ("nplanes", C.c_int), ("planes", C.POINTER(_PlaneWind)),
     ]
 
 
@@ -145,6 +151,7 @@ class Params:
     winds: list = field(default_factory=list)
     masses: np.ndarray | None = None  # (n, 4): x, y, z, M
     nthreads: int = 0
+    plane_winds: list = field(default_factory=list)  # objects with plane, rho, vel, temp, mu
 
     @property
     def shape(self):
@@ -195,6 +202,14 @@ class Params:
             m = np.ascontiguousarray(self.masses, dtype=np.float64).reshape(-1, 4)
             keep.append(m)
             s.nmasses, s.masses = m.shape[0], _ptr(m)
+        if self.plane_winds:
+            arr = (_PlaneWind * len(self.plane_winds))()
+            for q, w in enumerate(self.plane_winds):
+                arr[q].plane = int(w.plane)
+                for n in ("rho", "vel", "temp", "mu"):
+                    setattr(arr[q], n, float(getattr(w, n)))
+            keep.append(arr)
+            s.nplanes, s.planes = len(self.plane_winds), C.cast(arr, C.POINTER(_PlaneWind))
         return s, keep
 
 

@@ -407,6 +407,33 @@ void tlqo_impose_winds(const tlqo_params* p, double* U) {
           }
         }
   }
+  /* imposePlaneWind, source/winds.f90:92-147: i over nxmin..nxmax, j over
+   * nymin..nymax, k over nz..nzmax (the top three z-planes, whatever the
+   * plane); pres = dens/(mu AMU) KB temp. */
+  for (int s = 0; s < p->nplanes; ++s) {
+    const tlqo_plane_wind* w = &p->planes[s];
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    switch (w->plane) {
+      case 1: vx = w->vel; break;
+      case 2: vx = -w->vel; break;
+      case 3: vy = w->vel; break;
+      case 4: vy = -w->vel; break;
+      case 5: vz = w->vel; break;
+      case 6: vz = -w->vel; break;
+      default: break;
+    }
+    const double pres = w->rho / (w->mu * AMU) * KB * w->temp;
+    for (int i = -1; i <= p->nx + 2; ++i)
+      for (int j = -1; j <= p->ny + 2; ++j)
+        for (int k = p->nz; k <= p->nz + 2; ++k) {
+          double* u = U + IX(p, 0, i, j, k);
+          u[0] = w->rho;
+          u[1] = w->rho * vx;
+          u[2] = w->rho * vy;
+          u[3] = w->rho * vz;
+          u[4] = 0.5 * w->rho * ((vx * vx + vy * vy) + vz * vz) + pres / (g - 1.0);
+        }
+  }
 }
 
 /* borders, source/boundaries.f90:1-26. */

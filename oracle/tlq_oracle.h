@@ -39,6 +39,13 @@ typedef struct tlqo_wind {
   double xc, yc, zc, vx, vy, vz, radius, mdot, vinf, temp, mu;
 } tlqo_wind;
 
+/* plane_wind_type, source/winds.f90:15-28 (plane 1..6: left, right, front,
+ * back, bottom, top). */
+typedef struct tlqo_plane_wind {
+  int plane;
+  double rho, vel, temp, mu;
+} tlqo_plane_wind;
+
 /* Runtime image of user/parameters.f90 plus the per-run tables. */
 typedef struct tlqo_params {
   int nx, ny, nz;                       /* nxtot.. (parameters.f90:23-25), no MPI split */
@@ -59,6 +66,8 @@ typedef struct tlqo_params {
   int nmasses;                          /* point masses, source/pointsource_gravity.f90 */
   const double* masses;                 /* 4 per mass: x, y, z, M [g] */
   int nthreads;                         /* OpenMP threads (<=0: runtime default) */
+  int nplanes;                          /* plane winds, imposed after the spherical ones */
+  const tlqo_plane_wind* planes;
 } tlqo_params;
 
 /* Size in doubles of one conserved/primitive array (5 vars incl. ghosts). */

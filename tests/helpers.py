@@ -14,6 +14,7 @@ def oracle_params(cfg, nthreads: int = 0) -> Params:
     p.winds = [OWind(**{k: getattr(w, k) for k in ("xc", "yc", "zc", "vx", "vy", "vz", "radius", "mdot", "vinf",
                                                     "temp", "mu")}) for w in cfg.winds]
     p.masses = None if cfg.masses is None else np.asarray(cfg.masses, float)
+    p.plane_winds = list(getattr(cfg, "plane_winds", []))
     return p
 
 

@@ -106,6 +106,20 @@ def test_step_gravity_and_winds_bit_exact(gpu_lib):
     assert_bit_exact(cfg, run, hist, Ug, Wg)
 
 
+def test_step_plane_wind_bit_exact(gpu_lib):
+    """A plane wind (imposePlaneWind, winds.f90:92-147: the top three
+    z-planes, every i, j) with a spherical wind and point gravity, as the
+    reference's RCW120 set-up combines them (user.f90:290-324)."""
+    cfg, U0 = problems.wind_bubble(24, cooling=tlq.COOL_NONE)
+    rho = float(U0[0, 5, 5, 5])
+    cfg.plane_winds = [tlq.PlaneWind(plane=1, rho=3.0 * rho, vel=5.0 * problems.KMS, temp=100.0, mu=1.3),
+                       tlq.PlaneWind(plane=6, rho=0.5 * rho, vel=2.0 * problems.KMS, temp=1e3, mu=1.3)]
+    run, hist, Ug, Wg = run_both(cfg, U0, 10)
+    assert_bit_exact(cfg, run, hist, Ug, Wg)
+    # the top z-ghost plane carries the last plane wind's density
+    assert np.all(Ug[0, 2:-2, 2:-2, -1] == 0.5 * rho)
+
+
 @pytest.mark.parametrize("mode", [tlq.COOL_REF, tlq.COOL_SUBCYCLE])
 def test_step_wind_bubble_with_cooling(gpu_lib, mode):
     """The wind-bubble physics (wind, point mass, cooling) at 32^3: relative

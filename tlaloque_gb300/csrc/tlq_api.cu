@@ -468,6 +468,16 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int
   return TLQ_OK;
 }
 
+int tlq_set_plane_winds(tlq_ctx* ctx, const tlq_plane_wind* w, int n) {
+  if (!ctx || n < 0 || n > tlq::MAX_PLANE_WINDS || (n > 0 && !w)) return TLQ_ERR_ARG;
+  for (int q = 0; q < n; ++q)
+    if (w[q].plane < 1 || w[q].plane > 6) return fail(ctx, TLQ_ERR_ARG, "plane wind: plane must be 1..6");
+  ctx->P.nplanes = n;
+  for (int q = 0; q < n; ++q) ctx->P.planes[q] = tlq::PlaneWind{w[q].plane, w[q].rho, w[q].vel, w[q].temp, w[q].mu};
+  invalidate_graphs(ctx);
+  return TLQ_OK;
+}
+
 int tlq_set_winds(tlq_ctx* ctx, const tlq_wind* w, int n) {
   if (!ctx || n < 0 || (n > 0 && !w)) return TLQ_ERR_ARG;
   cudaFree(ctx->dwinds);

@@ -461,6 +461,11 @@ __global__ void k_winds_aos(Params p, Aos A, double* U) {
     for (int e = 0; e < 5; ++e) u[e] = U[5 * c + e];
     bool hit = false;
     for (int s = 0; s < p.nwinds; ++s) hit |= wind_cell(p, p.winds[s], i, j, k, u);
+    for (int s = 0; s < p.nplanes; ++s)
+      if (k >= p.nz) {
+        plane_wind_cell(p, p.planes[s], k, u);
+        hit = true;
+      }
     if (hit)
 #pragma unroll
       for (int e = 0; e < 5; ++e) U[5 * c + e] = u[e];

@@ -40,6 +40,13 @@ struct Wind {
   int ilo, ihi, jlo, jhi, klo, khi;
 };
 
+// plane_wind_type, source/winds.f90:15-28.
+constexpr int MAX_PLANE_WINDS = 6;
+struct PlaneWind {
+  int plane;  // PLANE_LEFT .. PLANE_TOP = 1..6 (winds.f90:15-20)
+  double rho, vel, temp, mu;
+};
+
 // Cooling table on the device: T (ascending), log10 T, log10 Lambda, and
 // FP32 copies of the three columns for the mixed-precision step.
 struct CoolTable {
@@ -62,6 +69,8 @@ struct Params {
   int bc[6];
   int nwinds;
   const Wind* winds;
+  int nplanes;
+  PlaneWind planes[MAX_PLANE_WINDS];
   CoolTable cool;
   int gravity;        // point-mass source term on
 };
@@ -259,8 +268,33 @@ __device__ __forceinline__ bool wind_cell(const Params& p, const Wind& w, int i,
 }
 
 // All winds in order (user/user.f90:64-68): later winds override earlier ones.
+// imposePlaneWind, source/winds.f90:92-147: every i, j and k = nz..nz+2
+// (the reference's loop writes the top three z-planes whatever the plane),
+// the velocity along the plane's normal.
+__device__ __forceinline__ void plane_wind_cell(const Params& p, const PlaneWind& w, int k, double* u) {
+  if (k < p.nz) return;
+  double vx = 0.0, vy = 0.0, vz = 0.0;
+  switch (w.plane) {
+    case 1: vx = w.vel; break;
+    case 2: vx = -w.vel; break;
+    case 3: vy = w.vel; break;
+    case 4: vy = -w.vel; break;
+    case 5: vz = w.vel; break;
+    case 6: vz = -w.vel; break;
+    default: break;
+  }
+  const double pres = w.rho / (w.mu * AMU) * KB * w.temp;
+  u[0] = w.rho;
+  u[1] = w.rho * vx;
+  u[2] = w.rho * vy;
+  u[3] = w.rho * vz;
+  u[4] = 0.5 * w.rho * ((vx * vx + vy * vy) + vz * vz) + pres / (p.gamma - 1.0);
+}
+
+// user_boundaries: the spherical winds, then the plane winds.
 __device__ __forceinline__ void winds_cell(const Params& p, int i, int j, int k, double* u) {
   for (int s = 0; s < p.nwinds; ++s) wind_cell(p, p.winds[s], i, j, k, u);
+  for (int s = 0; s < p.nplanes; ++s) plane_wind_cell(p, p.planes[s], k, u);
 }
 
 // ---------------------------------------------------------------------------

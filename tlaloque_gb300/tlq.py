@@ -34,7 +34,7 @@ EXPORTS = (
     "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
     "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
     "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
-    "tlq_set_tfin", "tlq_output", "tlq_output_wait", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
+    "tlq_set_tfin", "tlq_set_plane_winds", "tlq_output", "tlq_output_wait", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
     "tlq_batch_set_tiling", "tlq_batch_get_tiling", "tlq_batch_autotune", "tlq_batch_run", "tlq_batch_synchronize",
     "tlq_batch_status", "tlq_batch_enable_timing", "tlq_batch_stats_get", "tlq_batch_last_error",
 )
@@ -60,6 +60,11 @@ class CConfig(C.Structure):
 
 class CWind(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("xc", "yc", "zc", "vx", "vy", "vz", "radius", "mdot", "vinf", "temp", "mu")]
+
+
+class CPlaneWind(C.Structure):
+    _fields_ = [("plane", C.c_int), ("rho", C.c_double), ("vel", C.c_double), ("temp", C.c_double),
+                ("mu", C.c_double)]
 
 
 class CStats(C.Structure):
@@ -107,6 +112,7 @@ def load_library(path: str = LIB_PATH):
         "tlq_create": (I, [C.POINTER(CConfig), C.POINTER(V)]),
         "tlq_destroy": (I, [V]),
         "tlq_set_tfin": (I, [V, C.c_double]),
+        "tlq_set_plane_winds": (I, [V, C.POINTER(CPlaneWind), I]),
         "tlq_output": (I, [V, I, C.c_char_p, I, I]),
         "tlq_output_wait": (I, [V]),
         "tlq_set_tiling": (I, [V, I]),
@@ -195,6 +201,16 @@ class Wind:
 
 
 @dataclass
+class PlaneWind:
+    """tlq_plane_wind / plane_wind_type (source/winds.f90:15-28)."""
+    plane: int = 1
+    rho: float = 1.0
+    vel: float = 0.0
+    temp: float = 1.0e4
+    mu: float = 1.0
+
+
+@dataclass
 class Config:
     """tlq_config: the runtime image of user/parameters.f90 (its defaults)."""
     nx: int = 50
@@ -224,6 +240,7 @@ class Config:
     cool_logL: np.ndarray | None = None
     winds: list = field(default_factory=list)
     masses: np.ndarray | None = None  # (n, 4): x, y, z, M
+    plane_winds: list = field(default_factory=list)
 
     @property
     def shape(self):
@@ -292,6 +309,13 @@ class Context:
         if cfg.masses is not None and len(cfg.masses):
             m = np.ascontiguousarray(cfg.masses, dtype=np.float64).reshape(-1, 4)
             self._check(self.L.tlq_set_point_masses(self.h, _dp(m), m.shape[0]), "set_point_masses")
+        if cfg.plane_winds:
+            arr = (CPlaneWind * len(cfg.plane_winds))()
+            for q, w in enumerate(cfg.plane_winds):
+                arr[q].plane = int(w.plane)
+                for n in ("rho", "vel", "temp", "mu"):
+                    setattr(arr[q], n, float(getattr(w, n)))
+            self._check(self.L.tlq_set_plane_winds(self.h, arr, len(cfg.plane_winds)), "set_plane_winds")
 
     # -- plumbing ------------------------------------------------------------
     def _check(self, rc: int, what: str):
