@@ -50,7 +50,7 @@ __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
     stage_kernel_mixed_batch(const MemberDesc* __restrict__ mem, const Item* __restrict__ items, int nitems) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
   BatchSmem& bs = *reinterpret_cast<BatchSmem*>(smem_bytes);

@@ -18,12 +18,16 @@
 
 namespace tlq {
 
-constexpr int MRAW = 2;  // TMA landing slots (raw FP64 planes); a plane is requested two planes ahead
-constexpr int MCU = 4;   // FP32 conserved-state ring (faces: planes k, k+1; stage-1 Laplacian: k-1..k+1)
+// Shared memory per block is kept under 57 KB so that 4 blocks fit an SM:
+constexpr int MRAW = 1;  // TMA landing slot (raw FP64 plane); the next plane is requested as soon as the
+                         // previous one is converted, a whole plane's work (~10 us) ahead of its use
+constexpr int MCU = 3;   // FP32 conserved-state ring (faces: planes k, k+1; stage-1 Laplacian: k-1..k+1)
+constexpr int MIXED_BLOCKS_PER_SM = 4;
 
 // Ring slots of plane q.  Planes start at k0 - 2 >= -1, so q can be
 // negative; C++ '%' keeps the sign of q, hence the offset.
 __device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
+__device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
 
 struct MixedSmem {
   double raw[MRAW][5 * PLANE_BOX];  // TMA landing zone
@@ -189,7 +193,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
 
   auto convert = [&](int q) {
     const double* r0 = s.raw[raw_slot(q)];
-    const int sl = q & 3, sc = q & 3;
+    const int sl = q & 3, sc = cu_slot(q);
     constexpr int RW = TX + 2 * H;
     constexpr int NROW = RW * TY, NCOL = TX * 2 * H;
     for (int t = tid; t < NROW + NCOL; t += NT) {
@@ -228,7 +232,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         const int ly = fyl + 2;
         w0 = &s.prm[sk][0][ly][fxl];
         w1 = w0 + 1; w2 = w0 + 2; w3 = w0 + 3;
-        uL = &s.cu[k & 3][0][ly][fxl + 1];
+        uL = &s.cu[cu_slot(k)][0][ly][fxl + 1];
         uR = uL + 1;
         valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
       } else if (t < NXF + NYF) {
@@ -239,7 +243,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         const int lx = fxl + 2;
         w0 = &s.prm[sk][0][fyl][lx];
         w1 = w0 + HX; w2 = w0 + 2 * HX; w3 = w0 + 3 * HX;
-        uL = &s.cu[k & 3][0][fyl + 1][lx];
+        uL = &s.cu[cu_slot(k)][0][fyl + 1][lx];
         uR = uL + HX;
         valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
       } else {
@@ -252,8 +256,8 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         w1 = &s.prm[k & 3][0][ly][lx];
         w2 = &s.prm[(k + 1) & 3][0][ly][lx];
         w3 = &s.prm[(k + 2) & 3][0][ly][lx];
-        uL = &s.cu[k & 3][0][ly][lx];
-        uR = &s.cu[(k + 1) & 3][0][ly][lx];
+        uL = &s.cu[cu_slot(k)][0][ly][lx];
+        uR = &s.cu[cu_slot(k + 1)][0][ly][lx];
         valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
       }
       if (!valid) continue;
@@ -336,6 +340,9 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       }
     }
     wait_plane(k + H);
+    // stage 1: the previous plane's Laplacian read the ring slot this
+    // conversion overwrites (a 3-plane ring)
+    if (STAGE == 1) __syncthreads();
     convert(k + H);
     __syncthreads();  // S1
     if (s.abort) { aborted = true; break; }
@@ -373,7 +380,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       if (STAGE == 1) {
         // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U
         // this stage streams (= the old U of stage 2), in FP32 from the ring
-        const int a0 = (k - 1) & 3, a1 = k & 3, a2 = (k + 1) & 3;
+        const int a0 = cu_slot(k - 1), a1 = cu_slot(k), a2 = cu_slot(k + 1);
         const int lx = tx + 2, ly = ty + 2;
 #pragma unroll
         for (int e = 0; e < 5; ++e) {
@@ -457,7 +464,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
     stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ StageArgs a) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
   MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
