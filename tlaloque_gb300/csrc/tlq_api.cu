@@ -108,6 +108,13 @@ void fill_params(tlq_ctx* c) {
   p.cool_sub_frac = g.cool_sub_frac;
   p.limiter = g.limiter; p.solver = g.solver; p.cooling = g.cooling; p.cool_max_sub = g.cool_max_sub;
   for (int q = 0; q < 6; ++q) p.bc[q] = g.bc[q];
+  p.f_gamma = (float)p.gamma; p.f_g1 = (float)p.g1; p.f_eta = (float)p.eta;
+  p.f_inv_dx = (float)(1.0 / p.dx); p.f_inv_dy = (float)(1.0 / p.dy); p.f_inv_dz = (float)(1.0 / p.dz);
+  p.f_hdx = (float)(0.5 / p.dx); p.f_hdy = (float)(0.5 / p.dy); p.f_hdz = (float)(0.5 / p.dz);
+  p.f_cT = (float)(p.mu0 * AMU / KB);
+  p.f_inv_muamu = (float)(1.0 / (p.mu0 * AMU));
+  p.f_cool_sub_frac = (float)p.cool_sub_frac;
+  p.f_cooling_limit = (float)p.cooling_limit;
 }
 
 void invalidate_graphs(tlq_ctx* c) {

@@ -73,6 +73,15 @@ struct Params {
   PlaneWind planes[MAX_PLANE_WINDS];
   CoolTable cool;
   int gravity;        // point-mass source term on
+  // FP32 images of per-run constants for the mixed-precision kernels, formed
+  // on the host once (an FP64 division or double->float conversion costs
+  // ~64 FP32 slots on GB300, and every thread of every tile would repeat it)
+  float f_gamma, f_g1, f_eta;
+  float f_inv_dx, f_inv_dy, f_inv_dz;  // 1/dx ...
+  float f_hdx, f_hdy, f_hdz;           // 0.5/dx ... (gravity's central differences)
+  float f_cT;                          // mu0 AMU / KB: T = (p/rho) f_cT
+  float f_inv_muamu;                   // 1/(mu0 AMU): n = rho f_inv_muamu
+  float f_cool_sub_frac, f_cooling_limit;
 };
 
 // ---------------------------------------------------------------------------

@@ -107,14 +107,14 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   const float n = w[0] * inv_muamu;
   float ce = (aloss * n) * (n / ETH);
   int nsub = 1;
-  const float frac = (float)p.cool_sub_frac;
+  const float frac = p.f_cool_sub_frac;
   if (p.cooling == COOL_SUBCYCLE && ce * dt > frac) {
     const float q = ceilf(ce * dt / frac);
     nsub = (q > (float)p.cool_max_sub) ? p.cool_max_sub : (int)q;
     if (nsub < 1) nsub = 1;
   }
   const float h = dt / (float)nsub;
-  const float fmin = 1.0f - (float)p.cooling_limit;
+  const float fmin = 1.0f - p.f_cooling_limit;
   for (int s = 0; s < nsub; ++s) {
     if (s > 0) {
       temp = (w[4] / w[0]) * cT;
@@ -154,10 +154,10 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
 
   if (!(clk->t < clk->tfin)) return;  // the loop condition of mainHD.f90:61 (uniform)
   const double dtstep = clk->dt;
-  const double dt = (STAGE == 1) ? dtstep / 2.0 : dtstep;
-  const float gf = (float)p.gamma, gm1 = gf - 1.0f, g1f = (float)p.g1;
-  const float dtdx = (float)(dt / p.dx), dtdy = (float)(dt / p.dy), dtdz = (float)(dt / p.dz);
-  const float dtf = (float)dt;
+  const float dtstep_f = d2f(dtstep);
+  const float dtf = (STAGE == 1) ? 0.5f * dtstep_f : dtstep_f;
+  const float gf = p.f_gamma, gm1 = gf - 1.0f, g1f = p.f_g1;
+  const float dtdx = dtf * p.f_inv_dx, dtdy = dtf * p.f_inv_dy, dtdz = dtf * p.f_inv_dz;
   const int last_plane = k1 + H;
   const long long pxy = (long long)L.px * L.nyg;
 
@@ -294,7 +294,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
     }
   };
 
-  // ---- prologue: planes k0-H .. k0+H-1, then the z face k0-1/2 ------------
+  // ---- prologue: planes k0-H .. k0+H-1 ---------------------------------------
   if (tid == 0)
     for (int q = k0 - H; q <= min(k0 - H + MRAW - 1, last_plane); ++q) issue(q);
   bool aborted = false;
@@ -305,20 +305,21 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
     if (s.abort) { aborted = true; break; }
     if (tid == 0 && q + MRAW <= last_plane && q + MRAW > issued) issue(q + MRAW);
   }
-  if (!aborted) faces(k0 - 1, false);
-  __syncthreads();
 
   const int tx = tid % TX, ty = tid / TX;
   const int i = i0 + tx, j = j0 + ty;
   const bool cell_ok = (i <= p.nx) && (j <= p.ny);
   float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
-  const float cT = (float)(p.mu0 * AMU / KB);
-  const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
-  const float etaf = (float)p.eta;
-  const float hdx = (float)(0.5 / p.dx), hdy = (float)(0.5 / p.dy), hdz = (float)(0.5 / p.dz);
-  const float dtstep_f = (float)dtstep;
+  const float cT = p.f_cT;
+  const float inv_muamu = p.f_inv_muamu;
+  const float etaf = p.f_eta;
+  const float hdx = p.f_hdx, hdy = p.f_hdy, hdz = p.f_hdz;
 
-  for (int k = k0; k <= k1 && !aborted; ++k) {
+  // k = k0 - 1 computes only the z face below the chunk, through the same
+  // (single) copy of the face code as every other plane, so that a cell's
+  // arithmetic does not depend on where the z-chunks begin
+  for (int k = k0 - 1; k <= k1 && !aborted; ++k) {
+    const bool first = k < k0;
     // Global operands of this cell's update, requested now so that their
     // latency hides behind the conversion and face phases.
     const long long c = L.at(i, j, k);
@@ -326,7 +327,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
     float lv[5];
     double ph[6];
     bool queued = false;  // stage 2 with the surrogate: handed to the cooling passes
-    if (cell_ok) {
+    if (cell_ok && !first) {
 #pragma unroll
       for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
       if (STAGE == 2) {
@@ -339,16 +340,19 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
       }
     }
-    wait_plane(k + H);
-    // stage 1: the previous plane's Laplacian read the ring slot this
-    // conversion overwrites (a 3-plane ring)
-    if (STAGE == 1) __syncthreads();
-    convert(k + H);
-    __syncthreads();  // S1
-    if (s.abort) { aborted = true; break; }
-    if (tid == 0 && k + H + MRAW <= last_plane && k + H + MRAW > issued) issue(k + H + MRAW);
-    faces(k, true);
+    if (!first) {
+      wait_plane(k + H);
+      // stage 1: the previous plane's Laplacian read the ring slot this
+      // conversion overwrites (a 3-plane ring)
+      if (STAGE == 1) __syncthreads();
+      convert(k + H);
+      __syncthreads();  // S1
+      if (s.abort) { aborted = true; break; }
+      if (tid == 0 && k + H + MRAW <= last_plane && k + H + MRAW > issued) issue(k + H + MRAW);
+    }
+    faces(k, !first);
     __syncthreads();  // S2
+    if (first) continue;
 
     if (cell_ok) {
       const int cur = (k + 1) & 1, prv = k & 1;

@@ -110,10 +110,10 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* __r
   mlp::load_weights(sa.P, W, nullptr);
   __syncthreads();
   const CoolTable& tab = p.cool;
-  const float gm1 = (float)p.gamma - 1.0f, gf = (float)p.gamma;
-  const float cT = (float)(p.mu0 * AMU / KB);
-  const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
-  const float dtf = (float)clk->dt;
+  const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
+  const float cT = p.f_cT;
+  const float inv_muamu = p.f_inv_muamu;
+  const float dtf = d2f(clk->dt);
   const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   const long long n = (long long)*cqcount;
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
@@ -231,10 +231,10 @@ __global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, dou
   __shared__ int flag;
   if (!(clk->t < clk->tfin)) return;
   const unsigned nq = *qcount;
-  const float gm1 = (float)p.gamma - 1.0f, gf = (float)p.gamma;
-  const float cT = (float)(p.mu0 * AMU / KB);
-  const float inv_muamu = (float)(1.0 / (p.mu0 * AMU));
-  const float dtf = (float)clk->dt;
+  const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
+  const float cT = p.f_cT;
+  const float inv_muamu = p.f_inv_muamu;
+  const float dtf = d2f(clk->dt);
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
   for (unsigned q = blockIdx.x * FT + threadIdx.x; q < nq; q += gridDim.x * FT) {
     const long long o = interior_offset(p, L, (long long)queue[q]);
