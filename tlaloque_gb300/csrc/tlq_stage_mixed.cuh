@@ -27,6 +27,18 @@ constexpr int MIXED_BLOCKS_PER_SM = 4;
 // Ring slots of plane q.  Planes start at k0 - 2 >= -1, so q can be
 // negative; C++ '%' keeps the sign of q, hence the offset.
 __device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
+
+// Whether a cell may write ghost images (within two cells of a face) or lie
+// in a spherical wind's index box or a plane wind's planes.
+__device__ __forceinline__ bool near_boundary_or_wind(const Params& p, int i, int j, int k) {
+  if (i <= 2 || j <= 2 || k <= 2 || i >= p.nx - 1 || j >= p.ny - 1 || k >= p.nz - 1) return true;
+  if (p.nplanes > 0 && k >= p.nz) return true;
+  for (int s = 0; s < p.nwinds; ++s) {
+    const Wind& w = p.winds[s];
+    if (i >= w.ilo && i <= w.ihi && j >= w.jlo && j <= w.jhi && k >= w.klo && k <= w.khi) return true;
+  }
+  return false;
+}
 __device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
 
 struct MixedSmem {
@@ -378,9 +390,13 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       }
       // FP64 accumulation: U' = U - dU (Godunov's centre value is U in both
       // stages; `uold` is the stage-1 input and the stage-2 old state)
+      // Stage 2 away from the boundaries and the winds (which read or
+      // overwrite UP): U = U_old - dU + eta Lap in one FP64 addition of the
+      // FP32 increment (an FP64 addition costs ~64 FP32 slots on GB300).
+      const bool plain2 = STAGE == 2 && !near_boundary_or_wind(p, i, j, k);
       double up[5];
 #pragma unroll
-      for (int e = 0; e < 5; ++e) up[e] = uc[e] - f2d(dU[e]);
+      for (int e = 0; e < 5; ++e) up[e] = plain2 ? uc[e] : uc[e] - f2d(dU[e]);
       if (STAGE == 1) {
         // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U
         // this stage streams (= the old U of stage 2), in FP32 from the ring
@@ -394,8 +410,10 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
           a.lapf[e * L.plane + c] = etaf * lap;
         }
       }
-      write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
-      winds_cell(p, i, j, k, up);
+      if (!plain2) {
+        write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
+        winds_cell(p, i, j, k, up);
+      }
       if (STAGE == 1) {
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = up[e];
@@ -403,7 +421,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         // step: U = UP + eta * (Laplacian of the old U), from stage 1
         double un[5];
 #pragma unroll
-        for (int e = 0; e < 5; ++e) un[e] = up[e] + f2d(lv[e]);
+        for (int e = 0; e < 5; ++e) un[e] = plain2 ? up[e] + f2d(lv[e] - dU[e]) : up[e] + f2d(lv[e]);
         float cf[5], w[5];
         mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
         if (p.cooling == COOL_MLP) {
@@ -412,7 +430,12 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         } else if (p.cooling != COOL_NONE) {
           cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
         }
-        if (!(un[0] > 0.0)) atomicOr(&clk->status, ST_NEG_DENSITY);
+        {
+          // !(rho > 0) on the bits (no FP64 compare): sign set, zero or
+          // below the normal range, or not finite
+          const int hi = __double2hiint(un[0]);
+          if (hi < 0x00100000 || (hi & 0x7ff00000) == 0x7ff00000) atomicOr(&clk->status, ST_NEG_DENSITY);
+        }
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
         if (!queued) {
