@@ -175,3 +175,44 @@ def test_context_autotune_restores_state(gpu_lib, tmp_path, precision):
     np.testing.assert_array_equal(interior(U), interior(ref))
     assert t == tr[0]
     assert json.loads(cache.read_text())["tuned"]
+
+
+def test_batch_with_surrogate_members(gpu_lib):
+    """Members with the learned cooling surrogate (their two cooling passes
+    join the captured batched step) advance exactly like their single runs;
+    a plain member beside them is unaffected."""
+    cfg_a, U_a = problems.wind_bubble(32)
+    cfg_b, U_b = problems.clumpy(32, seed=5)
+    exact = dict(cool_sub_frac=2e-3, cool_max_sub=20000)
+    with tlq.Context(cfg_a) as tctx:
+        tctx.train_cooling_surrogate(nsamples=1 << 20, epochs=4, seed=3)
+        net = tctx.get_cooling_surrogate()
+    members = [(mixed(cfg_a, cooling=tlq.COOL_MLP, **exact), U_a), (mixed(cfg_b, cooling=tlq.COOL_MLP, **exact), U_b),
+               (mixed(cfg_b), U_b)]
+    n = 6
+
+    def single_mlp(cfg, U0):
+        U1 = U0.copy(order="F")
+        with tlq.Context(cfg) as ctx:
+            if cfg.cooling == tlq.COOL_MLP:
+                ctx.set_cooling_surrogate(*net)
+            ctx.borders(U1, 1)
+            ctx.upload(U1)
+            ctx.advance(n)
+            st = ctx.stats()
+            return ctx.state()[0], ctx.time(), (st.cool_mlp, st.cool_fallback)
+
+    with tlq.Batch([c for c, _ in members]) as b:
+        for m, (cfg, _) in zip(b.members, members):
+            if cfg.cooling == tlq.COOL_MLP:
+                m.set_cooling_surrogate(*net)
+        load(b, members)
+        b.run(n)
+        assert b.status() == [tlq.OK] * 3
+        assert b.stats().launches_per_step == 2 + 2 * 2
+        got = [(m.state()[0], m.time(), (m.stats().cool_mlp, m.stats().cool_fallback)) for m in b.members]
+    for (cfg, U0), (U, tm, cc) in zip(members, got):
+        ref, tr, rc = single_mlp(cfg, U0)
+        assert tm == tr
+        np.testing.assert_array_equal(interior(U), interior(ref))
+        assert cc == rc

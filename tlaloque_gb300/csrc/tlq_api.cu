@@ -201,7 +201,7 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
-    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[par ^ 1], ctx->clk, ctx->partials, ctx->npartials,
+    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->partials, ctx->npartials,
                           ctx->mlp_params, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
                           ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[3], ctx->stream));
@@ -544,7 +544,9 @@ int tlq_set_time(tlq_ctx* ctx, double t, int it) {
     long long itl = it;
     CK(cudaMemcpyAsync(&ctx->clk->it, &itl, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    ctx->it_base = it - (long long)ctx->cur;
+    const long long base = it - (long long)ctx->cur;
+    if (base != ctx->it_base) invalidate_graphs(ctx);  // captured launches read it_base
+    ctx->it_base = base;
   }
   return TLQ_OK;
 }
@@ -568,6 +570,7 @@ int tlq_upload(tlq_ctx* ctx, const double* U) {
   CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], carries_pressure(ctx) ? ctx->Pc : nullptr, ctx->clk,
                           ctx->partials, init_blocks(ctx->P), ctx->stream));
   ctx->cur = 0;
+  if (ctx->it_base != ctx->it0) invalidate_graphs(ctx);  // captured launches read it_base
   ctx->it_base = ctx->it0;
   ctx->steps = 0;
   ctx->uploaded = true;

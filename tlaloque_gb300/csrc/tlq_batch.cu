@@ -161,6 +161,8 @@ void fill_desc(tlq_batch* b, int i) {
       a.out = (st == 1) ? c->UPP : c->U[par ^ 1];
       a.pout = (st == 1) ? nullptr : c->Pc;
       a.use_p = 0;
+      a.cqueue = (st == 2) ? c->mlp_cqueue : nullptr;
+      a.cqcount = (st == 2 && c->mlp_qcount) ? c->mlp_qcount + 1 : nullptr;
     }
   d.it_base = c->it_base;
   d.gx = (c->cfg.nx + tlq::TX - 1) / tlq::TX;
@@ -214,12 +216,25 @@ int refresh_desc(tlq_batch* b) {
   return TLQ_OK;
 }
 
-int enqueue_batch_step(tlq_batch* b) {
+// One batched step of the members in `which` (all when empty): the two
+// persistent stage launches, then the surrogate's cooling passes of the
+// members that use it (their stage 2 queued the cooling cells and left the
+// dt reduction to them).
+int enqueue_batch_step(tlq_batch* b, const std::vector<int>& which = {}) {
   const size_t smem = sizeof(tlq::BatchSmem);
   tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   BCK(cudaGetLastError());
   tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   BCK(cudaGetLastError());
+  for (int i = 0; i < (int)b->m.size(); ++i) {
+    tlq_ctx* c = b->m[i];
+    if (c->cfg.cooling != TLQ_COOL_MLP) continue;
+    if (!which.empty() && std::find(which.begin(), which.end(), i) == which.end()) continue;
+    const MemberDesc& d = b->h_desc[i];
+    BCK(tlq::launch_cool_mlp_dt(c->P, c->L, c->U[0], c->U[1], c->it_base, c->clk, c->partials, d.gx * d.gy * d.gz,
+                                c->mlp_params, c->mlp_norm, c->mlp_box, c->gcum, c->gslope, c->cool_counts,
+                                c->mlp_cqueue, c->mlp_qcount + 1, c->mlp_queue, c->mlp_qcount, b->stream));
+  }
   return TLQ_OK;
 }
 
@@ -307,7 +322,7 @@ int tlq_batch_create(const tlq_config* cfgs, int n, tlq_batch** out) {
   if (!cfgs || n < 1 || !out) return TLQ_ERR_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i)
-    if (cfgs[i].precision != TLQ_PREC_MIXED || cfgs[i].cooling == TLQ_COOL_MLP) return TLQ_ERR_CONFIG;
+    if (cfgs[i].precision != TLQ_PREC_MIXED) return TLQ_ERR_CONFIG;
   tlq_batch* b = new tlq_batch();
   auto bail = [&](int code) {
     tlq_batch_destroy(b);
@@ -373,8 +388,11 @@ int tlq_batch_get_tiling(const tlq_batch* b, int i, int* zlen) {
 
 int tlq_batch_run(tlq_batch* b, int steps) {
   if (!b || steps < 0) return TLQ_ERR_ARG;
-  for (size_t i = 0; i < b->m.size(); ++i)
+  for (size_t i = 0; i < b->m.size(); ++i) {
     if (!b->m[i]->uploaded) return bfail(b, TLQ_ERR_STATE, "member " + std::to_string(i) + " has no state (tlq_upload)");
+    if (b->m[i]->cfg.cooling == TLQ_COOL_MLP && !b->m[i]->mlp_ready)
+      return bfail(b, TLQ_ERR_STATE, "member " + std::to_string(i) + " uses the cooling surrogate but has no network");
+  }
   int rc = refresh_desc(b);
   if (rc) return rc;
   if (graph_stale(b)) {
@@ -433,6 +451,7 @@ int tlq_batch_stats_get(tlq_batch* b, tlq_batch_stats* s) {
   s->items = b->nitems;
   s->blocks = b->blocks;
   s->launches_per_step = 2;
+  for (tlq_ctx* c : b->m) s->launches_per_step += (c->cfg.cooling == TLQ_COOL_MLP) ? 2 : 0;
   long long cells = 0;
   for (tlq_ctx* c : b->m) cells += (long long)c->cfg.nx * c->cfg.ny * c->cfg.nz;
   s->cells = cells;
@@ -450,6 +469,9 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
   if (!b || steps < 1) return TLQ_ERR_ARG;
   for (size_t i = 0; i < b->m.size(); ++i)
     if (!b->m[i]->uploaded) return bfail(b, TLQ_ERR_STATE, "autotune needs every member's state (tlq_upload)");
+  for (size_t i = 0; i < b->m.size(); ++i)
+    if (b->m[i]->cfg.cooling == TLQ_COOL_MLP && !b->m[i]->mlp_ready)
+      return bfail(b, TLQ_ERR_STATE, "member " + std::to_string(i) + " uses the cooling surrogate but has no network");
   const std::string gpu = device_name();
   auto cache = read_cache(cache_path, gpu);
   std::map<std::string, std::vector<int>> classes;
@@ -493,7 +515,7 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
       if (rc) return rc;
       for (int w = 0; w < steps + 1; ++w) {
         if (w == 1) BCK(cudaEventRecord(b->ev[0], b->stream));
-        rc = enqueue_batch_step(b);
+        rc = enqueue_batch_step(b, mem);
         if (rc) return rc;
       }
       BCK(cudaEventRecord(b->ev[1], b->stream));
@@ -514,7 +536,11 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
       }
       BCK(cudaStreamSynchronize(b->stream));
     }
-    for (size_t q = 0; q < mem.size(); ++q) cudaFree(snap[q]);
+    for (size_t q = 0; q < mem.size(); ++q) {
+      cudaFree(snap[q]);
+      tlq_ctx* c = b->m[mem[q]];
+      if (c->cool_counts) cudaMemsetAsync(c->cool_counts, 0, 2 * sizeof(unsigned long long), b->stream);
+    }
     for (int i : mem) b->zlen[i] = std::min(best, b->m[i]->cfg.nz);
     cache[kv.first] = {best, best_ms};
     wrote = true;

@@ -79,7 +79,8 @@ cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStr
 // exact integrator (queue); the fallback pass cools those and finishes the
 // dt reduction over all block maxima.  Queues: capacity nx ny nz; counts
 // zero between steps.
-cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Clock* clk, double* partials,
+cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
+                               Clock* clk, double* partials,
                                int nstage, const float* P, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,
                                const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,

@@ -100,13 +100,22 @@ __device__ __forceinline__ long long interior_offset(const Params& p, const Layo
 // there the reference integrator's last sub-step decides how far below that
 // temperature the cell ends.  The block maxima of the signal speeds of the
 // accepted cells go to partials after the stage-2 blocks' (nprev of them).
-__global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* __restrict__ U, const Clock* clk,
+// The state the step just wrote: U1 or U0 by the clock's buffer parity (the
+// clock has not advanced yet), so that one captured launch serves both
+// parities.
+__device__ __forceinline__ double* step_output(double* U0, double* U1, const Clock* clk, long long it_base) {
+  return ((clk->it - it_base) & 1LL) ? U0 : U1;
+}
+
+__global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0, double* U1, long long it_base,
+                                                 const Clock* clk,
                                                  double* partials, unsigned nprev, SurrogateArgs sa,
                                                  const unsigned* __restrict__ cqueue, const unsigned* cqcount,
                                                  unsigned* __restrict__ queue, unsigned* qcount) {
   __shared__ mlp::SmemWeights W;
   __shared__ double red[96];
   if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
+  double* __restrict__ U = step_output(U0, U1, clk, it_base);
   mlp::load_weights(sa.P, W, nullptr);
   __syncthreads();
   const CoolTable& tab = p.cool;
@@ -223,13 +232,15 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* __r
 // sub-cycled cooling with the run's sub-step settings), then the dt
 // reduction over the block maxima of stage 2 and both passes (nprev before
 // this pass's); the last block empties both queues.
-__global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, double* __restrict__ U, Clock* clk,
+__global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, double* U0, double* U1,
+                                                         long long it_base, Clock* clk,
                                                          double* partials, unsigned nprev,
                                                          const unsigned* __restrict__ queue, unsigned* qcount,
                                                          unsigned* cqcount) {
   __shared__ double red[96];
   __shared__ int flag;
   if (!(clk->t < clk->tfin)) return;
+  double* __restrict__ U = step_output(U0, U1, clk, it_base);
   const unsigned nq = *qcount;
   const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
   const float cT = p.f_cT;
@@ -256,7 +267,8 @@ __global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, dou
 
 }  // namespace
 
-cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Clock* clk, double* partials,
+cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
+                               Clock* clk, double* partials,
                                int nstage, const float* P, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,
                                const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
@@ -273,10 +285,12 @@ cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U, Cloc
   sa.gcum = gcum;
   sa.gslope = gslope;
   sa.counts = counts;
-  k_cool_net<<<CB, CT, 0, s>>>(pf, L, U, clk, partials, (unsigned)nstage, sa, cqueue, cqcount, queue, qcount);
+  k_cool_net<<<CB, CT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)nstage, sa, cqueue, cqcount, queue,
+                               qcount);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cool_fallback_dt<<<FB, FT, 0, s>>>(pf, L, U, clk, partials, (unsigned)(nstage + CB), queue, qcount, cqcount);
+  k_cool_fallback_dt<<<FB, FT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)(nstage + CB), queue, qcount,
+                                       cqcount);
   return cudaGetLastError();
 }
 
@@ -519,6 +533,7 @@ int tlq_train_cooling_surrogate(tlq_ctx* ctx, const tlq_surrogate_opts* opts, tl
     ctx->mlp_box[q] = o.box[q];
   }
   ctx->mlp_ready = true;
+  ctx->gen += 1;
   for (int q = 0; q < 2; ++q)
     if (ctx->graph[q]) { cudaGraphExecDestroy(ctx->graph[q]); ctx->graph[q] = nullptr; }
   if (rep) {
@@ -553,6 +568,7 @@ int tlq_set_cooling_surrogate(tlq_ctx* ctx, const float* params, const float* no
   std::memcpy(ctx->mlp_norm, norm6, 6 * sizeof(float));
   std::memcpy(ctx->mlp_box, box6, 6 * sizeof(double));
   ctx->mlp_ready = true;
+  ctx->gen += 1;
   for (int q = 0; q < 2; ++q)
     if (ctx->graph[q]) { cudaGraphExecDestroy(ctx->graph[q]); ctx->graph[q] = nullptr; }
   return TLQ_OK;
