@@ -115,6 +115,11 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
   __shared__ mlp::SmemWeights W;
   __shared__ double red[96];
   if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
+  const long long n = (long long)*cqcount;
+  if ((long long)blockIdx.x * CT >= n) {  // no queued cell for this block: a neutral maximum, no weights
+    if (threadIdx.x < 3) partials[3 * (nprev + blockIdx.x) + threadIdx.x] = 0.0;
+    return;
+  }
   double* __restrict__ U = step_output(U0, U1, clk, it_base);
   mlp::load_weights(sa.P, W, nullptr);
   __syncthreads();
@@ -124,7 +129,6 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
   const float inv_muamu = p.f_inv_muamu;
   const float dtf = d2f(clk->dt);
   const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-  const long long n = (long long)*cqcount;
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
   unsigned long long used = 0, fell = 0;
   // warp-uniform trip count: the network's tiles need all 32 lanes
