@@ -300,6 +300,18 @@ __device__ __forceinline__ void plane_wind_cell(const Params& p, const PlaneWind
   u[4] = 0.5 * w.rho * ((vx * vx + vy * vy) + vz * vz) + pres / (p.gamma - 1.0);
 }
 
+// Whether a cell may write ghost images (within two cells of a face) or lie
+// in a spherical wind's index box or a plane wind's planes.
+__device__ __forceinline__ bool near_boundary_or_wind(const Params& p, int i, int j, int k) {
+  if (i <= 2 || j <= 2 || k <= 2 || i >= p.nx - 1 || j >= p.ny - 1 || k >= p.nz - 1) return true;
+  if (p.nplanes > 0 && k >= p.nz) return true;
+  for (int s = 0; s < p.nwinds; ++s) {
+    const Wind& w = p.winds[s];
+    if (i >= w.ilo && i <= w.ihi && j >= w.jlo && j <= w.jhi && k >= w.klo && k <= w.khi) return true;
+  }
+  return false;
+}
+
 // user_boundaries: the spherical winds, then the plane winds.
 __device__ __forceinline__ void winds_cell(const Params& p, int i, int j, int k, double* u) {
   for (int s = 0; s < p.nwinds; ++s) wind_cell(p, p.winds[s], i, j, k, u);

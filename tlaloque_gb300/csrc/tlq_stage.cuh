@@ -323,9 +323,13 @@ __global__ void __launch_bounds__(NT, 2)
 #pragma unroll
         for (int e = 0; e < 5; ++e) up[e] = up[e] + dt * sv[e];
       }
-      // borders: face ghosts from the pre-wind value, then the winds.
-      write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
-      winds_cell(p, i, j, k, up);
+      // borders: face ghosts from the pre-wind value, then the winds (only
+      // cells near a face or in a wind's box can be concerned; the gate also
+      // keeps the winds' distance arithmetic from being evaluated everywhere)
+      if (near_boundary_or_wind(p, i, j, k)) {
+        write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
+        winds_cell(p, i, j, k, up);
+      }
       if (STAGE == 1) {
 #pragma unroll
         for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = up[e];

@@ -28,17 +28,7 @@ constexpr int MIXED_BLOCKS_PER_SM = 4;
 // negative; C++ '%' keeps the sign of q, hence the offset.
 __device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
 
-// Whether a cell may write ghost images (within two cells of a face) or lie
-// in a spherical wind's index box or a plane wind's planes.
-__device__ __forceinline__ bool near_boundary_or_wind(const Params& p, int i, int j, int k) {
-  if (i <= 2 || j <= 2 || k <= 2 || i >= p.nx - 1 || j >= p.ny - 1 || k >= p.nz - 1) return true;
-  if (p.nplanes > 0 && k >= p.nz) return true;
-  for (int s = 0; s < p.nwinds; ++s) {
-    const Wind& w = p.winds[s];
-    if (i >= w.ilo && i <= w.ihi && j >= w.jlo && j <= w.jhi && k >= w.klo && k <= w.khi) return true;
-  }
-  return false;
-}
+
 __device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
 
 struct MixedSmem {
@@ -393,7 +383,10 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       // Stage 2 away from the boundaries and the winds (which read or
       // overwrite UP): U = U_old - dU + eta Lap in one FP64 addition of the
       // FP32 increment (an FP64 addition costs ~64 FP32 slots on GB300).
-      const bool plain2 = STAGE == 2 && !near_boundary_or_wind(p, i, j, k);
+      // (the gate also keeps the winds' FP64 distance and density, which the
+      // compiler would otherwise evaluate for every cell, off the FP64 pipe)
+      const bool special = near_boundary_or_wind(p, i, j, k);
+      const bool plain2 = STAGE == 2 && !special;
       double up[5];
 #pragma unroll
       for (int e = 0; e < 5; ++e) up[e] = plain2 ? uc[e] : uc[e] - f2d(dU[e]);
@@ -410,7 +403,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
           a.lapf[e * L.plane + c] = etaf * lap;
         }
       }
-      if (!plain2) {
+      if (special) {
         write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
         winds_cell(p, i, j, k, up);
       }

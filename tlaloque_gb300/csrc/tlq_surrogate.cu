@@ -71,9 +71,16 @@ __device__ __forceinline__ float g_inv(const CoolTable& t, const SurrogateArgs& 
 }
 
 constexpr int CT = 128;      // threads per block of the network pass
-constexpr int CB = 152 * 4;  // blocks of the network pass
+constexpr int CB = 152 * 4;  // blocks of the network pass (at most)
 constexpr int FT = 128;      // threads per block of the fallback pass
-constexpr int FB = 152 * 4;  // blocks of the fallback pass
+constexpr int FB = 152 * 4;  // blocks of the fallback pass (at most)
+
+// Blocks of each cooling pass for a mesh: enough for its cells to cool at
+// once (2048 cells a block), at most 4 per SM.
+int pass_blocks(const Params& p) {
+  const long long n = (long long)p.nx * p.ny * p.nz;
+  return (int)std::max<long long>(4, std::min<long long>((n + 2047) / 2048, CB));
+}
 
 __device__ __forceinline__ void speeds_max(const float* w, float gf, float& m0, float& m1, float& m2) {
   const float cs = sqrtf(gf * w[4] / w[0]);
@@ -289,11 +296,12 @@ cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, dou
   sa.gcum = gcum;
   sa.gslope = gslope;
   sa.counts = counts;
-  k_cool_net<<<CB, CT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)nstage, sa, cqueue, cqcount, queue,
+  const int nb = pass_blocks(p);
+  k_cool_net<<<nb, CT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)nstage, sa, cqueue, cqcount, queue,
                                qcount);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cool_fallback_dt<<<FB, FT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)(nstage + CB), queue, qcount,
+  k_cool_fallback_dt<<<nb, FT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)(nstage + nb), queue, qcount,
                                        cqcount);
   return cudaGetLastError();
 }
