@@ -49,7 +49,7 @@ __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
   asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int STAGE>
+template <int STAGE, int LIM = -1, int SOLV = -1>
 __global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
     stage_kernel_mixed_batch(const MemberDesc* __restrict__ mem, const Item* __restrict__ items, int nitems) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
     const CUtensorMap* tm = (STAGE == 1) ? &m.tm_U[par] : &m.tm_UPP;
     const unsigned nblk = (unsigned)(m.gx * m.gy * m.gz);
     const unsigned bid = (unsigned)(it.bx + m.gx * (it.by + m.gy * it.bz));
-    mixed_tile<STAGE>(tm, bs.a, bs.s, it.bx, it.by, it.bz, nblk, bid);
+    mixed_tile<STAGE, LIM, SOLV>(tm, bs.a, bs.s, it.bx, it.by, it.bz, nblk, bid);
     __syncthreads();
     // a tile that gave up on a copy (its member's status says so) may have
     // left it in flight: this block takes no further tile
@@ -92,11 +92,18 @@ static_assert(alignof(MemberDesc) >= 64, "tensor maps 64-byte aligned");
 
 }  // namespace
 
+constexpr int SPEC_LIM = LIM_VANLEER, SPEC_SOLV = SOLVER_HLLC;  // as the single-mesh kernels
+
 cudaError_t prepare_batch_kernels() {
   const int smem = (int)sizeof(BatchSmem);
-  cudaError_t e = cudaFuncSetAttribute(stage_kernel_mixed_batch<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(stage_kernel_mixed_batch<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const void* ks[4] = {(const void*)stage_kernel_mixed_batch<1>, (const void*)stage_kernel_mixed_batch<2>,
+                       (const void*)stage_kernel_mixed_batch<1, SPEC_LIM, SPEC_SOLV>,
+                       (const void*)stage_kernel_mixed_batch<2, SPEC_LIM, SPEC_SOLV>};
+  for (const void* k : ks) {
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace tlq
@@ -222,9 +229,20 @@ int refresh_desc(tlq_batch* b) {
 // dt reduction to them).
 int enqueue_batch_step(tlq_batch* b, const std::vector<int>& which = {}) {
   const size_t smem = sizeof(tlq::BatchSmem);
-  tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
-  BCK(cudaGetLastError());
-  tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+  // the specialised kernels when every member uses their limiter and solver
+  bool spec = true;
+  for (tlq_ctx* c : b->m) spec = spec && c->P.limiter == tlq::SPEC_LIM && c->P.solver == tlq::SPEC_SOLV;
+  if (spec) {
+    tlq::stage_kernel_mixed_batch<1, tlq::SPEC_LIM, tlq::SPEC_SOLV>
+        <<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+    BCK(cudaGetLastError());
+    tlq::stage_kernel_mixed_batch<2, tlq::SPEC_LIM, tlq::SPEC_SOLV>
+        <<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+  } else {
+    tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+    BCK(cudaGetLastError());
+    tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+  }
   BCK(cudaGetLastError());
   for (int i = 0; i < (int)b->m.size(); ++i) {
     tlq_ctx* c = b->m[i];

@@ -140,9 +140,11 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
 
 // One tile (TX x TY columns, z-chunk bz of zlen planes) of a stage: the
 // body of the single-mesh kernel and of each work item of the batched
-// persistent kernel.  nblk / bid: the mesh's tiles and this one's index, for
+// persistent kernel.  LIM / SOLV >= 0 fix the limiter and the Riemann solver
+// at compile time (their switches fold away and the face code becomes one
+// straight block the compiler can schedule); -1 reads them from the params.  nblk / bid: the mesh's tiles and this one's index, for
 // the dt reduction.  Leaves every TMA copy it issued completed.
-template <int STAGE>
+template <int STAGE, int LIM = -1, int SOLV = -1>
 __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArgs& a, MixedSmem& s, int bx, int by,
                                            int bz, unsigned nblk, unsigned bid) {
   constexpr int H = STAGE;
@@ -277,9 +279,9 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
           wll[e] = w0[e * VS];
           wrr[e] = w3[e * VS];
         }
-        limiter(wll, wl, wr, wrr, p.limiter);
+        limiter(wll, wl, wr, wrr, LIM >= 0 ? LIM : p.limiter);
       }
-      if (!riemann(p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
+      if (!riemann(SOLV >= 0 ? SOLV : p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
 #pragma unroll
         for (int e = 0; e < 5; ++e) ff[e] = NAN;
       }
@@ -483,12 +485,12 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   }
 }
 
-template <int STAGE>
+template <int STAGE, int LIM = -1, int SOLV = -1>
 __global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
     stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ StageArgs a) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
   MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
-  mixed_tile<STAGE>(&tm_in, a, s, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z,
+  mixed_tile<STAGE, LIM, SOLV>(&tm_in, a, s, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z,
                     blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
 }
 
