@@ -397,7 +397,8 @@ def main():
         return {"ctx": ctx, "ms": ms_max, "value": world * cfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
                 "k2": st.ms_stage2, "kc": st.ms_cool, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
                 "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks,
-                "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback), "zlen": zlen}
+                "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback,
+                         st.cool_single - st0.cool_single), "zlen": zlen}
 
     def form(m):
         d = {"value": m["value"], "ms_per_step": m["ms"] / args.steps, "ms_stage1": m["k1"], "ms_stage2": m["k2"],
@@ -433,7 +434,7 @@ def main():
         f64x = measure(tlq.PREC_FP64, args.steps, False, **exact)
         f64x["ctx"].close()
         sur = measure(tlq.PREC_MIXED, args.steps, True, net=net, cooling=tlq.COOL_MLP, **exact)
-        nm, nf = sur["cool"]
+        nm, nf, ns = sur["cool"]
         forms["fp64_exact_cooling"] = form(f64x)
         forms["mixed_surrogate"] = form(sur)
         forms["speedup_mixed_surrogate_vs_fp64"] = sur["value"] / f64["value"]
@@ -441,10 +442,13 @@ def main():
         surrogate = {"train": {k: rep[k] for k in ("ms_generate", "ms_train", "steps", "val_accept", "val_p99_rel_T",
                                                     "val_rmse_y")},
                      "timed_cell_steps_network": nm, "timed_cell_steps_fallback": nf,
+                     "timed_cell_steps_single_step": ns,
                      "fallback_rate": nf / max(1, nm + nf),
-                     "fallback_note": "cooling cell-steps of the timed steps handed to the exact integrator: "
-                                      "outside the training box, failing the 1e-3 residual check, or cooling to "
-                                      "the table's first temperature within the step"}
+                     "fallback_note": "of the cooling cell-steps with tau above the integrator's sub-step (the "
+                                      "network's domain), the share handed to the exact integrator: outside the "
+                                      "training box, failing the 1e-3 residual check, or cooling to the table's "
+                                      "first temperature within the step; cells with smaller tau take the exact "
+                                      "integrator's single exponential step directly (single_step)"}
         head = sur
     value = head["value"]
     ms_max = head["ms"]

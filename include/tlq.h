@@ -146,6 +146,8 @@ typedef struct tlq_stats {
   long long cool_mlp;      /* TLQ_COOL_MLP: cell-steps cooled by the network (since upload) */
   long long cool_fallback; /* TLQ_COOL_MLP: cell-steps handed to the exact integrator */
   double ms_cool;          /* TLQ_COOL_MLP: average device time of the timed cooling passes */
+  long long cool_single;   /* TLQ_COOL_MLP: cell-steps with tau <= cool_sub_frac, cooled by the exact
+                              integrator's single exponential step (the network has nothing to gain) */
 } tlq_stats;
 
 typedef struct tlq_ctx tlq_ctx;

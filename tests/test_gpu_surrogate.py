@@ -158,7 +158,8 @@ def run(cfg, U0, nsteps, net=None, timing=False):
             ctx.advance(nsteps)
             s2 = ctx.stats()
             ms = s2.ms_stage1 + s2.ms_stage2 + s2.ms_cool
-    return dict(U=U, W=W, t=t, it=it, rc=rc, sums=sums, mlp=st.cool_mlp, fb=st.cool_fallback, ms=ms)
+    return dict(U=U, W=W, t=t, it=it, rc=rc, sums=sums, mlp=st.cool_mlp, fb=st.cool_fallback, one=st.cool_single,
+                ms=ms)
 
 
 def test_no_network_is_an_error(gpu_lib):
@@ -207,7 +208,8 @@ def test_wind_bubble_bars_with_surrogate(trained):
     drift = abs(got["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4])
     frac_fb = got["fb"] / max(1, got["fb"] + got["mlp"])
     print(f"wind64 surrogate: L1 rho {err:.3e} drift {drift:.3e} (mixed form alone {drift_mix:.3e}, surrogate "
-          f"against it {drift_net:.3e}) fallback {frac_fb:.4f} (mlp {got['mlp']}, fallback {got['fb']})")
+          f"against it {drift_net:.3e}) fallback {frac_fb:.4f} (mlp {got['mlp']}, fallback {got['fb']}, "
+          f"single step {got['one']})")
     assert err <= 1e-2 and drift <= 1e-6
     assert got["mlp"] > 0
 

@@ -554,7 +554,7 @@ int tlq_set_time(tlq_ctx* ctx, double t, int it) {
 int tlq_upload(tlq_ctx* ctx, const double* U) {
   if (!ctx || !U) return TLQ_ERR_ARG;
   if (ctx->cfg.cooling != TLQ_COOL_NONE && !ctx->dT) return fail(ctx, TLQ_ERR_STATE, "cooling on but no cooling table");
-  if (ctx->cool_counts) CK(cudaMemsetAsync(ctx->cool_counts, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  if (ctx->cool_counts) CK(cudaMemsetAsync(ctx->cool_counts, 0, 3 * sizeof(unsigned long long), ctx->stream));
   if (const double* hU = static_cast<const double*>(mapped_host(U))) {
     CK(launch_aos_to_soa(ctx->A, ctx->L, hU, ctx->U[0], ctx->stream));
   } else {
@@ -689,11 +689,12 @@ int tlq_stats_get(tlq_ctx* ctx, tlq_stats* s) {
   s->ms_cool = ctx->ntimed ? ctx->mscool_acc / ctx->ntimed : 0.0;
   s->bytes_state = (double)ctx->L.plane * 8.0 * 17.0;
   if (ctx->cool_counts) {
-    unsigned long long cc[2] = {0, 0};
+    unsigned long long cc[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(cc, ctx->cool_counts, sizeof(cc), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     s->cool_mlp = (long long)cc[0];
     s->cool_fallback = (long long)cc[1];
+    s->cool_single = (long long)cc[2];
   }
   return TLQ_OK;
 }

@@ -557,7 +557,7 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
     for (size_t q = 0; q < mem.size(); ++q) {
       cudaFree(snap[q]);
       tlq_ctx* c = b->m[mem[q]];
-      if (c->cool_counts) cudaMemsetAsync(c->cool_counts, 0, 2 * sizeof(unsigned long long), b->stream);
+      if (c->cool_counts) cudaMemsetAsync(c->cool_counts, 0, 3 * sizeof(unsigned long long), b->stream);
     }
     for (int i : mem) b->zlen[i] = std::min(best, b->m[i]->cfg.nz);
     cache[kv.first] = {best, best_ms};
@@ -642,7 +642,7 @@ int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen) {
     }
     cudaFree(snap);
     ctx->steps = steps0;
-    if (ctx->cool_counts) cudaMemsetAsync(ctx->cool_counts, 0, 2 * sizeof(unsigned long long), ctx->stream);
+    if (ctx->cool_counts) cudaMemsetAsync(ctx->cool_counts, 0, 3 * sizeof(unsigned long long), ctx->stream);
     cache[key] = {best, best_ms};
     if (write_cache(cache_path, gpu, cache) != TLQ_OK) {
       ctx->err = std::string("cannot write the tuning cache ") + (cache_path ? cache_path : "");

@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
   const float dtf = d2f(clk->dt);
   const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-  unsigned long long used = 0, fell = 0;
+  unsigned long long used = 0, fell = 0, one = 0;
   // warp-uniform trip count: the network's tiles need all 32 lanes
   for (long long base = (long long)blockIdx.x * CT; base < n; base += (long long)gridDim.x * CT) {
     const long long q = base + threadIdx.x;
@@ -171,7 +171,14 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
       feat[1] = (f1 - sa.norm[2]) / sa.norm[3];
       feat[2] = (f2 - sa.norm[4]) / sa.norm[5];
     }
-    const bool run = need && inbox;
+    // tau at most the integrator's sub-step: the exact integrator is a single
+    // exponential step, cheaper and exact, and the network has nothing to gain
+    const bool single = need && !(tau > p.f_cool_sub_frac);
+    if (single) {
+      cool_cell_f(p, cT, inv_muamu, gm1, w, u[4], dtf, u);
+      U[4 * L.plane + o] = u[4];
+    }
+    const bool run = need && inbox && !single;
     float y = 0.f;
     if (__ballot_sync(0xffffffffu, run)) {
       // the warp's 32 cells as two m16 tiles (rows = lanes 0-15, 16-31)
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
         }
       }
     }
-    const bool queued = need && !ok;
+    const bool queued = need && !ok && !single;
     // warp-aggregated append to the fallback queue
     const unsigned qm = __ballot_sync(0xffffffffu, queued);
     if (qm) {
@@ -219,16 +226,19 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
     }
     used += ok ? 1 : 0;
     fell += queued ? 1 : 0;
-    if (ok) speeds_max(w, gf, m0, m1, m2);
+    one += single ? 1 : 0;
+    if (ok || single) speeds_max(w, gf, m0, m1, m2);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     used += __shfl_xor_sync(0xffffffffu, used, off);
     fell += __shfl_xor_sync(0xffffffffu, fell, off);
+    one += __shfl_xor_sync(0xffffffffu, one, off);
   }
   if (lane == 0) {
     atomicAdd(&sa.counts[0], used);
     atomicAdd(&sa.counts[1], fell);
+    atomicAdd(&sa.counts[2], one);
   }
   double a = f2d(m0), b = f2d(m1), c = f2d(m2);
   block_max3<CT>(a, b, c, red);
@@ -379,8 +389,8 @@ int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* log
   SCK(cudaMemcpy(ctx->gcum, gc.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   SCK(cudaMemcpy(ctx->gslope, sl.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   if (!ctx->cool_counts) {
-    SCK(cudaMalloc(&ctx->cool_counts, 2 * sizeof(unsigned long long)));
-    SCK(cudaMemset(ctx->cool_counts, 0, 2 * sizeof(unsigned long long)));
+    SCK(cudaMalloc(&ctx->cool_counts, 3 * sizeof(unsigned long long)));
+    SCK(cudaMemset(ctx->cool_counts, 0, 3 * sizeof(unsigned long long)));
   }
   return TLQ_OK;
 }
