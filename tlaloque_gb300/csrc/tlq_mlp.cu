@@ -371,13 +371,10 @@ size_t mlp_train_smem() { return sizeof(mlp::TrainSmem); }
 
 cudaError_t launch_mlp_grad(const float* P, const float* X, const float* Y, const float* Wt, int nb, float* grad,
                             float* loss, int nblocks, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(mlp::k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(mlp::TrainSmem));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // (set on every call: the attribute belongs to the current device)
+  const cudaError_t e = cudaFuncSetAttribute(mlp::k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(mlp::TrainSmem));
+  if (e != cudaSuccess) return e;
   mlp::k_mlp_grad<<<nblocks, mlp::TT, sizeof(mlp::TrainSmem), s>>>(P, X, Y, Wt, nb, grad, loss);
   return cudaGetLastError();
 }
