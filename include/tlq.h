@@ -68,6 +68,9 @@ typedef struct tlq_config {
   double cool_sub_frac;           /* TLQ_COOL_SUBCYCLE: max Lambda n^2 h / E_th per sub-step */
   int precision;                  /* TLQ_PREC_* */
   int device;                     /* CUDA device ordinal */
+  double cool_mlp_tol;            /* TLQ_COOL_MLP: residual tolerance |T_pred - T_int|/T of an accepted
+                                     cell, in (0, 1e-3] (default 1e-3; smaller trades speed for energy
+                                     accuracy: more cells fall back) */
 } tlq_config;
 
 /* spherical_wind_type, source/winds.f90:5-16 (same fields, same order). */

@@ -239,3 +239,8 @@ def test_surrogate_gain_over_sub_cycling(trained):
           f"ms/step coarse {coarse['ms']:.3f} fine {fine['ms']:.3f} mlp {mlp['ms']:.3f}; fallback {frac_fb:.4f}")
     assert e_mlp < 0.5 * e_coarse
     assert mlp["ms"] < 0.5 * fine["ms"]
+    # a tighter residual tolerance: fewer accepted cells, closer to the exact integrator
+    tight = run(mixed_cfg(cfg, tlq.COOL_MLP, cool_mlp_tol=1e-5, **fine_kw), U0, n, net=net)
+    e_tight = rel_l1(eth(tight), eth(exact))
+    print(f"clumpy48 tol 1e-5: err {e_tight:.3e} network {tight['mlp']} fallback {tight['fb']}")
+    assert e_tight <= e_mlp and tight["fb"] >= mlp["fb"] and tight["mlp"] <= mlp["mlp"]

@@ -85,6 +85,10 @@ int validate(const tlq_config* c, std::string& why) {
     return TLQ_ERR_CONFIG;
   }
   if (c->precision != TLQ_PREC_FP64 && c->precision != TLQ_PREC_MIXED) { why = "unknown precision"; return TLQ_ERR_CONFIG; }
+  if (c->cooling == TLQ_COOL_MLP && !(c->cool_mlp_tol > 0.0 && c->cool_mlp_tol <= 1e-3)) {
+    why = "the surrogate's residual tolerance must lie in (0, 1e-3]";
+    return TLQ_ERR_CONFIG;
+  }
   if (c->cooling == TLQ_COOL_MLP && c->precision != TLQ_PREC_MIXED) {
     why = "the cooling surrogate runs in the mixed-precision step";
     return TLQ_ERR_CONFIG;
@@ -114,6 +118,7 @@ void fill_params(tlq_ctx* c) {
   p.f_cT = (float)(p.mu0 * AMU / KB);
   p.f_inv_muamu = (float)(1.0 / (p.mu0 * AMU));
   p.f_cool_sub_frac = (float)p.cool_sub_frac;
+  p.f_mlp_tol = (float)g.cool_mlp_tol;
   p.f_cooling_limit = (float)p.cooling_limit;
 }
 
@@ -304,6 +309,7 @@ void tlq_config_default(tlq_config* c) {
   c->limiter = TLQ_LIMITER_VANLEER;
   c->solver = TLQ_SOLVER_HLLC;
   for (int q = 0; q < 6; ++q) c->bc[q] = TLQ_BC_REFLECTIVE;
+  c->cool_mlp_tol = 1e-3;
   c->cooling = TLQ_COOL_NONE;
   c->cool_max_sub = 1;
   c->cool_sub_frac = 0.1;

@@ -82,6 +82,7 @@ struct Params {
   float f_cT;                          // mu0 AMU / KB: T = (p/rho) f_cT
   float f_inv_muamu;                   // 1/(mu0 AMU): n = rho f_inv_muamu
   float f_cool_sub_frac, f_cooling_limit;
+  float f_mlp_tol;  // the surrogate's residual tolerance
 };
 
 // ---------------------------------------------------------------------------

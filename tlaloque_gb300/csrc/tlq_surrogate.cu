@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
         // the network's r: ln(T_new/T) = -(tau + tau^2 r); q = T_new/T - 1
         // without cancellation, clamped at the table's first temperature
         const float q = fmaxf(expm1f(-(1.0f + tau * y) * tau), tab.Tf[0] / T - 1.0f);
-        ok = fabsf(T * q - (Tint - T)) <= 1e-3f * T;
+        ok = fabsf(T * q - (Tint - T)) <= p.f_mlp_tol * T;
         if (ok) {
           const float dp = w[4] * q;
           w[4] = w[4] + dp;

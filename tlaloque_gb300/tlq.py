@@ -55,6 +55,7 @@ class CConfig(C.Structure):
         ("cooling_limit", C.c_double),
         ("limiter", C.c_int), ("solver", C.c_int), ("bc", C.c_int * 6), ("cooling", C.c_int),
         ("cool_max_sub", C.c_int), ("cool_sub_frac", C.c_double), ("precision", C.c_int), ("device", C.c_int),
+        ("cool_mlp_tol", C.c_double),
     ]
 
 
@@ -234,6 +235,7 @@ class Config:
     cooling: int = COOL_NONE
     cool_max_sub: int = 1
     cool_sub_frac: float = 0.1
+    cool_mlp_tol: float = 1e-3
     precision: int = PREC_FP64
     device: int = 0
     # run-time tables (not part of tlq_config; set through their own calls)
@@ -274,7 +276,8 @@ class Config:
         c = CConfig()
         for n in ("nx", "ny", "nz", "limiter", "solver", "cooling", "cool_max_sub", "precision", "device"):
             setattr(c, n, int(getattr(self, n)))
-        for n in ("xl", "xr", "yl", "yr", "zl", "zr", "gamma", "cfl", "eta", "mu0", "cooling_limit", "cool_sub_frac"):
+        for n in ("xl", "xr", "yl", "yr", "zl", "zr", "gamma", "cfl", "eta", "mu0", "cooling_limit", "cool_sub_frac",
+                  "cool_mlp_tol"):
             setattr(c, n, float(getattr(self, n)))
         for q in range(6):
             c.bc[q] = int(self.bc[q])
