@@ -62,7 +62,9 @@ int make_map(tlq_ctx* ctx, CUtensorMap* m, double* base, int nvar) {
   cuuint64_t dims[4] = {(cuuint64_t)(ctx->cfg.nx + 4), (cuuint64_t)(ctx->cfg.ny + 4), (cuuint64_t)(ctx->cfg.nz + 4),
                         (cuuint64_t)nvar};
   cuuint64_t strides[3] = {(cuuint64_t)L.px * 8, (cuuint64_t)L.px * L.nyg * 8, (cuuint64_t)L.plane * 8};
-  cuuint32_t box[4] = {(cuuint32_t)HX, (cuuint32_t)HY, 1, (cuuint32_t)nvar};
+  // the halo-2 box of one tile of the form's kernels
+  const bool mixed = ctx->cfg.precision == TLQ_PREC_MIXED;
+  cuuint32_t box[4] = {(cuuint32_t)(mixed ? MHX : HX), (cuuint32_t)(mixed ? MHY : HY), 1, (cuuint32_t)nvar};
   cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -379,8 +381,10 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   std::memset(ctx->clk_host, 0, sizeof(Clock));
   ctx->clk_host->tfin = std::numeric_limits<double>::infinity();
   cudaMemcpy(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice);
-  // stage grid: TX x TY column tiles, z split into chunks of zlen planes
-  const int gx = (cfg->nx + TX - 1) / TX, gy = (cfg->ny + TY - 1) / TY;
+  // stage grid: column tiles (TX x TY plain, MTX x MTY mixed), z split into
+  // chunks of zlen planes
+  const int tx_ = cfg->precision == TLQ_PREC_MIXED ? MTX : TX, ty_ = cfg->precision == TLQ_PREC_MIXED ? MTY : TY;
+  const int gx = (cfg->nx + tx_ - 1) / tx_, gy = (cfg->ny + ty_ - 1) / ty_;
   ctx->zlen = cfg->nz >= 128 ? 64 : (cfg->nz >= 32 ? 32 : cfg->nz);
   const int gz = (cfg->nz + ctx->zlen - 1) / ctx->zlen;
   ctx->grid = dim3(gx, gy, gz);

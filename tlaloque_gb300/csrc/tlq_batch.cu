@@ -50,7 +50,7 @@ __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
 }
 
 template <int STAGE, int LIM = -1, int SOLV = -1>
-__global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
+__global__ void __launch_bounds__(MNT, MIXED_BLOCKS_PER_SM)
     stage_kernel_mixed_batch(const MemberDesc* __restrict__ mem, const Item* __restrict__ items, int nitems) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
   BatchSmem& bs = *reinterpret_cast<BatchSmem*>(smem_bytes);
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
     {
       const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&m.args[STAGE - 1][par]);
       unsigned long long* dst = reinterpret_cast<unsigned long long*>(&bs.a);
-      for (int q = threadIdx.x; q < (int)(sizeof(StageArgs) / 8); q += NT) dst[q] = src[q];
+      for (int q = threadIdx.x; q < (int)(sizeof(StageArgs) / 8); q += MNT) dst[q] = src[q];
     }
     __syncthreads();
     const CUtensorMap* tm = (STAGE == 1) ? &m.tm_U[par] : &m.tm_UPP;
@@ -172,8 +172,8 @@ void fill_desc(tlq_batch* b, int i) {
       a.cqcount = (st == 2 && c->mlp_qcount) ? c->mlp_qcount + 1 : nullptr;
     }
   d.it_base = c->it_base;
-  d.gx = (c->cfg.nx + tlq::TX - 1) / tlq::TX;
-  d.gy = (c->cfg.ny + tlq::TY - 1) / tlq::TY;
+  d.gx = (c->cfg.nx + tlq::MTX - 1) / tlq::MTX;
+  d.gy = (c->cfg.ny + tlq::MTY - 1) / tlq::MTY;
   d.gz = tiles_z(c, b->zlen[i]);
 }
 
@@ -188,7 +188,7 @@ std::vector<Item> make_items(const tlq_batch* b, const std::vector<int>& which) 
   std::stable_sort(ms.begin(), ms.end(), [&](int x, int y) { return b->zlen[x] > b->zlen[y]; });
   for (int i : ms) {
     const tlq_ctx* c = b->m[i];
-    const int gx = (c->cfg.nx + tlq::TX - 1) / tlq::TX, gy = (c->cfg.ny + tlq::TY - 1) / tlq::TY;
+    const int gx = (c->cfg.nx + tlq::MTX - 1) / tlq::MTX, gy = (c->cfg.ny + tlq::MTY - 1) / tlq::MTY;
     const int gz = tiles_z(c, b->zlen[i]);
     for (int bz = 0; bz < gz; ++bz)
       for (int by = 0; by < gy; ++by)
@@ -210,7 +210,7 @@ int upload_items(tlq_batch* b, const std::vector<Item>& v) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tlq::stage_kernel_mixed_batch<2>, tlq::NT,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tlq::stage_kernel_mixed_batch<2>, tlq::MNT,
                                                 sizeof(tlq::BatchSmem));
   b->blocks = std::max(1, std::min(b->nitems, nsm * std::max(per_sm, 1)));
   return TLQ_OK;
@@ -234,14 +234,14 @@ int enqueue_batch_step(tlq_batch* b, const std::vector<int>& which = {}) {
   for (tlq_ctx* c : b->m) spec = spec && c->P.limiter == tlq::SPEC_LIM && c->P.solver == tlq::SPEC_SOLV;
   if (spec) {
     tlq::stage_kernel_mixed_batch<1, tlq::SPEC_LIM, tlq::SPEC_SOLV>
-        <<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+        <<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
     BCK(cudaGetLastError());
     tlq::stage_kernel_mixed_batch<2, tlq::SPEC_LIM, tlq::SPEC_SOLV>
-        <<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+        <<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   } else {
-    tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+    tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
     BCK(cudaGetLastError());
-    tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::NT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+    tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   }
   BCK(cudaGetLastError());
   for (int i = 0; i < (int)b->m.size(); ++i) {

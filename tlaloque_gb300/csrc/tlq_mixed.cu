@@ -30,14 +30,14 @@ cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageA
   const bool spec = a.p.limiter == SPEC_LIM && a.p.solver == SPEC_SOLV;
   if (stage == 1) {
     if (spec)
-      stage_kernel_mixed<1, SPEC_LIM, SPEC_SOLV><<<grid, NT, smem, s>>>(tm_in, a);
+      stage_kernel_mixed<1, SPEC_LIM, SPEC_SOLV><<<grid, MNT, smem, s>>>(tm_in, a);
     else
-      stage_kernel_mixed<1><<<grid, NT, smem, s>>>(tm_in, a);
+      stage_kernel_mixed<1><<<grid, MNT, smem, s>>>(tm_in, a);
   } else {
     if (spec)
-      stage_kernel_mixed<2, SPEC_LIM, SPEC_SOLV><<<grid, NT, smem, s>>>(tm_in, a);
+      stage_kernel_mixed<2, SPEC_LIM, SPEC_SOLV><<<grid, MNT, smem, s>>>(tm_in, a);
     else
-      stage_kernel_mixed<2><<<grid, NT, smem, s>>>(tm_in, a);
+      stage_kernel_mixed<2><<<grid, MNT, smem, s>>>(tm_in, a);
   }
   return cudaGetLastError();
 }

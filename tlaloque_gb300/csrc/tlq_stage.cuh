@@ -22,6 +22,16 @@ namespace tlq {
 constexpr int TX = 16, TY = 8, NT = TX * TY;
 constexpr int HX = TX + 4, HY = TY + 4;  // halo-2 box
 constexpr int PLANE_BOX = HY * HX;
+
+// Tile of the mixed-form kernels (its own constants, so that it can be tuned
+// apart from the plain form's): 16 x 8 columns on 128 threads.  Measured
+// alternative: 16 x 7 (the plane's 359 faces in three rounds of 128 threads
+// instead of 408 in four) was 2 % slower at 256^3 -- fewer cells per tile
+// outweighed the shorter face phase.
+constexpr int MTX = 16, MTY = 8, MNT = 128;
+constexpr int MHX = MTX + 4, MHY = MTY + 4;  // halo-2 box
+constexpr int MPLANE_BOX = MHY * MHX;
+static_assert(MTX * MTY <= MNT, "one cell per thread");
 constexpr int NRING = 4;
 constexpr long long WAIT_LIMIT = 1LL << 24;  // mbarrier polls before giving up
 

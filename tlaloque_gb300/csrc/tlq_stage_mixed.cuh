@@ -18,6 +18,7 @@
 
 namespace tlq {
 
+
 // Shared memory per block is kept under 57 KB so that 4 blocks fit an SM:
 constexpr int MRAW = 1;  // TMA landing slot (raw FP64 plane); the next plane is requested as soon as the
                          // previous one is converted, a whole plane's work (~10 us) ahead of its use
@@ -32,12 +33,12 @@ __device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
 __device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
 
 struct MixedSmem {
-  double raw[MRAW][5 * PLANE_BOX];  // TMA landing zone
-  float cu[MCU][5][HY][HX];         // conserved state of the ring planes (FP32)
-  float prm[NRING][5][HY][HX];      // primitives of the ring planes (FP32)
-  float fx[5][TY][TX + 1];
-  float fy[5][TY + 1][TX];
-  float fz[2][5][TY][TX];
+  double raw[MRAW][5 * MPLANE_BOX];  // TMA landing zone
+  float cu[MCU][5][MHY][MHX];         // conserved state of the ring planes (FP32)
+  float prm[NRING][5][MHY][MHX];      // primitives of the ring planes (FP32)
+  float fx[5][MTY][MTX + 1];
+  float fy[5][MTY + 1][MTX];
+  float fz[2][5][MTY][MTX];
   uint64_t bar[MRAW];
   double red[96];
   int flag;
@@ -138,7 +139,7 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   u4 = u4 + f2d((w[4] - p0) / gm1);
 }
 
-// One tile (TX x TY columns, z-chunk bz of zlen planes) of a stage: the
+// One tile (MTX x MTY columns, z-chunk bz of zlen planes) of a stage: the
 // body of the single-mesh kernel and of each work item of the batched
 // persistent kernel.  LIM / SOLV >= 0 fix the limiter and the Riemann solver
 // at compile time (their switches fold away and the face code becomes one
@@ -151,7 +152,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   const Params& p = a.p;
   const Layout& L = a.L;
   const int tid = threadIdx.x;
-  const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
+  const int i0 = 1 + bx * MTX, j0 = 1 + by * MTY;
   const int k0 = 1 + bz * a.zlen;
   const int k1 = min(p.nz, k0 + a.zlen - 1);
   Clock* clk = a.clk;
@@ -176,8 +177,8 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   auto issue = [&](int q) {
     const int slot = raw_slot(q);
     fence_proxy_async();
-    mbar_arrive_expect_tx(&s.bar[slot], 5u * PLANE_BOX * 8u);
-    tma_load_4d(s.raw[slot], tm, &s.bar[slot], bx * TX, by * TY, q + 1, 0);
+    mbar_arrive_expect_tx(&s.bar[slot], 5u * MPLANE_BOX * 8u);
+    tma_load_4d(s.raw[slot], tm, &s.bar[slot], bx * MTX, by * MTY, q + 1, 0);
     issued = q;
   };
   uint32_t phase = 0;
@@ -198,20 +199,20 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   auto convert = [&](int q) {
     const double* r0 = s.raw[raw_slot(q)];
     const int sl = q & 3, sc = cu_slot(q);
-    constexpr int RW = TX + 2 * H;
-    constexpr int NROW = RW * TY, NCOL = TX * 2 * H;
-    for (int t = tid; t < NROW + NCOL; t += NT) {
+    constexpr int RW = MTX + 2 * H;
+    constexpr int NROW = RW * MTY, NCOL = MTX * 2 * H;
+    for (int t = tid; t < NROW + NCOL; t += MNT) {
       int lx, ly;
       if (t < NROW) {
         lx = 2 - H + t % RW;
         ly = 2 + t / RW;
       } else {
-        const int u = t - NROW, r2 = u / TX;
-        lx = 2 + u % TX;
-        ly = (r2 < H) ? (2 - H + r2) : (TY + 2 + r2 - H);
+        const int u = t - NROW, r2 = u / MTX;
+        lx = 2 + u % MTX;
+        ly = (r2 < H) ? (2 - H + r2) : (MTY + 2 + r2 - H);
       }
       float cf[5], w[5];
-      mixed_cell(gm1, r0 + ly * HX + lx, PLANE_BOX, cf, w);
+      mixed_cell(gm1, r0 + ly * MHX + lx, MPLANE_BOX, cf, w);
 #pragma unroll
       for (int e = 0; e < 5; ++e) {
         s.cu[sc][e][ly][lx] = cf[e];
@@ -221,18 +222,18 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   };
 
   auto faces = [&](int k, bool xy) {
-    constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1), NZF = TX * TY;
+    constexpr int NXF = (MTX + 1) * MTY, NYF = MTX * (MTY + 1), NZF = MTX * MTY;
     const int tbeg = xy ? 0 : NXF + NYF;
     const int sk = k & 3;
-    constexpr int VS = PLANE_BOX;
-    for (int t = tbeg + tid; t < NXF + NYF + NZF; t += NT) {
+    constexpr int VS = MPLANE_BOX;
+    for (int t = tbeg + tid; t < NXF + NYF + NZF; t += MNT) {
       int d, fxl, fyl;
       const float *w0, *w1, *w2, *w3, *uL, *uR;
       bool valid;
       if (t < NXF) {
         d = 1;
-        fxl = t % (TX + 1);
-        fyl = t / (TX + 1);
+        fxl = t % (MTX + 1);
+        fyl = t / (MTX + 1);
         const int ly = fyl + 2;
         w0 = &s.prm[sk][0][ly][fxl];
         w1 = w0 + 1; w2 = w0 + 2; w3 = w0 + 3;
@@ -242,19 +243,19 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       } else if (t < NXF + NYF) {
         d = 2;
         const int u = t - NXF;
-        fxl = u % TX;
-        fyl = u / TX;
+        fxl = u % MTX;
+        fyl = u / MTX;
         const int lx = fxl + 2;
         w0 = &s.prm[sk][0][fyl][lx];
-        w1 = w0 + HX; w2 = w0 + 2 * HX; w3 = w0 + 3 * HX;
+        w1 = w0 + MHX; w2 = w0 + 2 * MHX; w3 = w0 + 3 * MHX;
         uL = &s.cu[cu_slot(k)][0][fyl + 1][lx];
-        uR = uL + HX;
+        uR = uL + MHX;
         valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
       } else {
         d = 3;
         const int u = t - NXF - NYF;
-        fxl = u % TX;
-        fyl = u / TX;
+        fxl = u % MTX;
+        fyl = u / MTX;
         const int lx = fxl + 2, ly = fyl + 2;
         w0 = &s.prm[(k - 1) & 3][0][ly][lx];
         w1 = &s.prm[k & 3][0][ly][lx];
@@ -310,9 +311,9 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
     if (tid == 0 && q + MRAW <= last_plane && q + MRAW > issued) issue(q + MRAW);
   }
 
-  const int tx = tid % TX, ty = tid / TX;
+  const int tx = tid % MTX, ty = tid / MTX;
   const int i = i0 + tx, j = j0 + ty;
-  const bool cell_ok = (i <= p.nx) && (j <= p.ny);
+  const bool cell_ok = (ty < MTY) && (i <= p.nx) && (j <= p.ny);
   float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
   const float cT = p.f_cT;
   const float inv_muamu = p.f_inv_muamu;
@@ -471,11 +472,11 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   }
   if (STAGE == 2) {
     if (p.cooling != COOL_MLP) {
-      cfl_reduce_finalize_n<NT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag, 0, nblk, bid);
+      cfl_reduce_finalize_n<MNT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag, 0, nblk, bid);
     } else {
       // with the surrogate the cooling passes finish the reduction over
       // these block maxima and their own
-      block_max3<NT>(d0, d1, d2, s.red);
+      block_max3<MNT>(d0, d1, d2, s.red);
       if (tid == 0) {
         a.partials[3 * bid + 0] = d0;
         a.partials[3 * bid + 1] = d1;
@@ -486,7 +487,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
 }
 
 template <int STAGE, int LIM = -1, int SOLV = -1>
-__global__ void __launch_bounds__(NT, MIXED_BLOCKS_PER_SM)
+__global__ void __launch_bounds__(MNT, MIXED_BLOCKS_PER_SM)
     stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ StageArgs a) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
   MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
