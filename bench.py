@@ -421,8 +421,8 @@ def main():
     forms = {"fp64": form(f64), "mixed": form(mix), "speedup_mixed_vs_fp64": mix["value"] / f64["value"],
              "mixed_vs_fp64": accuracy(mix, f64)}
     # the plain form's bound: its HBM fraction next to its FP64-pipe occupancy
-    # (ncu: the FP64 pipe 79 % busy in both stage kernels, the figure of
-    # profiles/stage_kernels_wind128_fp64_ncu_full.md): FP64-pipe bound
+    # (ncu --set full of the plain stage kernels on the 128^3 wind bubble: the
+    # FP64 pipe 79 % busy in both): FP64-pipe bound
     bpz64 = bytes_per_zone(cfg)
     forms["fp64"]["roofline"] = {
         "bound": "fp64 pipe", "fp64_pipe_busy_ncu": 0.79,

@@ -3,7 +3,7 @@ cooling; FP64 accumulation, high-Mach pressure recovery and dt) against the
 plain FP64 step.  The plain step is bit-identical to the oracle (its own
 tests), so it stands in for the oracle on runs too long for the CPU.
 
-Bars (the benchmark spec's): relative L1 density error <= 1 % and relative
+Bars (the mixed form's targets): relative L1 density error <= 1 % and relative
 total-energy drift <= 1e-6 per 100 steps against FP64; short runs are held
 much tighter (they are FP32 round-off only)."""
 import numpy as np

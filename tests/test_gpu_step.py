@@ -3,8 +3,8 @@ step) against the oracle's main loop (mainHD.f90:61-100) on the same inputs.
 
 Without cooling the plain FP64 path is bit-identical to the oracle on every
 cell the scheme defines (interior and the first ghost layer of each face);
-with cooling the transcendental functions differ by ulps, so the bar is the
-spec one, relative L1 <= 1e-10 per conserved variable after 10 steps.
+with cooling the transcendental functions differ by ulps, so the bar is
+relative L1 <= 1e-10 per conserved variable after 10 steps.
 The physics checks rerun the reference's own tests at full size and compare
 the scores with the oracle's (tests/golden/oracle_metrics.json)."""
 import json
