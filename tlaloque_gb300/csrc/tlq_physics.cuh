@@ -233,11 +233,14 @@ __device__ __forceinline__ bool riemann(int solver, R g, R g1, R* ff, const R* w
   else if (sst >= R(0)) { star = true; left = true; }
   else if (sst <= R(0)) { star = true; left = false; }
   else return false;
-  const R* ws = left ? wl : wr;
-  const R* Us = left ? UL : UR;
+  // element-wise selects (a pointer to one of two register arrays would
+  // force both into local memory)
   R w[5], uc[5];
 #pragma unroll
-  for (int e = 0; e < 5; ++e) { w[e] = ws[e]; uc[e] = Us[e]; }
+  for (int e = 0; e < 5; ++e) {
+    w[e] = left ? wl[e] : wr[e];
+    uc[e] = left ? UL[e] : UR[e];
+  }
   prim2f(g1, ff, w, d);
   if (star) {
     const R s = left ? sl : sr;
