@@ -334,17 +334,16 @@ int tlq_gravity_source(tlq_ctx* ctx, const double* UPrim, const double* phi, dou
  * above, on the device) and d_dt (one double) are device buffers the caller
  * owns; dt is written to *d_dt asynchronously on cuda_stream (NULL: the
  * legacy default stream).  Calls no cudaMalloc, cudaFree or other allocating
- * routine.  Its reduction scratch is one fixed device array inside the
- * library (about 192 KiB, held by every GPU that loads the library until
- * exit), so:
- *   - meshes with more than 33,554,432 interior cells (nx*ny*nz) are
- *     rejected with TLQ_ERR_ARG, as are NULL pointers and sizes < 1;
- *   - the first call on a device looks the array's device address up on that
- *     device (cudaGetSymbolAddress); make that first call outside any stream
- *     capture;
- *   - all calls share the array: calls that overlap on the GPU (concurrent
- *     streams, several host threads) race and must be serialised by the
- *     caller. */
+ * routine.  Its reduction scratch is one fixed device variable inside the
+ * library (72 bytes, held by every GPU that loads the library until exit),
+ * so:
+ *   - NULL pointers and sizes < 1 are rejected with TLQ_ERR_ARG;
+ *   - the first call on a device looks the variable's device address up on
+ *     that device (cudaGetSymbolAddress); make that first call outside any
+ *     stream capture;
+ *   - all calls share the variable: calls that overlap on the GPU
+ *     (concurrent streams, several host threads) race and must be serialised
+ *     by the caller. */
 int tlq_time_step_noalloc(const double* d_uprim, int nx, int ny, int nz, double dx, double dy, double dz,
                           double gamma, double cfl, double* d_dt, void* cuda_stream);
 

@@ -139,7 +139,6 @@ int ensure_routine_scratch(tlq_ctx* ctx) {
   }
   CK(cudaMalloc(&ctx->rphi, phi_bytes(ctx->cfg)));
   CK(cudaMalloc(&ctx->rclk, sizeof(Clock)));
-  CK(cudaMalloc(&ctx->rpartials, sizeof(double) * 3 * (size_t)init_blocks(ctx->P)));
   return TLQ_OK;
 }
 
@@ -179,7 +178,6 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.p = ctx->P;
   a.L = ctx->L;
   a.clk = ctx->clk;
-  a.partials = ctx->partials;
   a.zlen = ctx->zlen;
   a.phi = ctx->phi;
   a.lapf = ctx->lapf;
@@ -208,8 +206,7 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
-    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->partials, ctx->npartials,
-                          ctx->mlp_params, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
+    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->mlp_image, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
                           ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[3], ctx->stream));
   return TLQ_OK;
@@ -279,7 +276,6 @@ int ctx_set_zlen(tlq_ctx* ctx, int zlen) {
   if (zlen < 8 && zlen != nz) return fail(ctx, TLQ_ERR_ARG, "z-chunk length must be >= 8 planes (or nz)");
   ctx->zlen = zlen;
   ctx->grid.z = (unsigned)((nz + zlen - 1) / zlen);
-  ctx->npartials = (int)(ctx->grid.x * ctx->grid.y * ctx->grid.z);
   invalidate_graphs(ctx);
   return TLQ_OK;
 }
@@ -388,13 +384,8 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   ctx->zlen = cfg->nz >= 128 ? 64 : (cfg->nz >= 32 ? 32 : cfg->nz);
   const int gz = (cfg->nz + ctx->zlen - 1) / ctx->zlen;
   ctx->grid = dim3(gx, gy, gz);
-  ctx->npartials = gx * gy * gz;
   const int nb = init_blocks(ctx->P);
-  // (tiles down to 8-plane z-chunks, which a tuner may choose; with the
-  // surrogate, stage 2's tiles then the cooling passes' blocks)
-  const int npart = std::max(nb, gx * gy * ((cfg->nz + 7) / 8) + cool_mlp_blocks(ctx->P));
-  if (cudaMalloc(&ctx->partials, sizeof(double) * 3 * (size_t)npart) ||
-      cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
+  if (cudaMalloc(&ctx->sums_partials, sizeof(double) * 5 * (size_t)nb) || cudaMalloc(&ctx->sums_out, sizeof(double) * 5))
     return bail(TLQ_ERR_NOMEM);
   if (prepare_stage_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
   if (cfg->precision == TLQ_PREC_MIXED && prepare_mixed_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
@@ -418,14 +409,14 @@ int tlq_destroy(tlq_ctx* ctx) {
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
-  cudaFree(ctx->mlp_params); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
+  cudaFree(ctx->mlp_params); cudaFree(ctx->mlp_image); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
   cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_qcount);
-  cudaFree(ctx->clk); cudaFree(ctx->partials); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
+  cudaFree(ctx->clk); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);
   cudaFree(ctx->dTf); cudaFree(ctx->dlogTf); cudaFree(ctx->dCf);
   for (int q = 0; q < 6; ++q) cudaFree(ctx->rb[q]);
-  cudaFree(ctx->rphi); cudaFree(ctx->rclk); cudaFree(ctx->rpartials);
+  cudaFree(ctx->rphi); cudaFree(ctx->rclk);
   if (ctx->clk_host) cudaFreeHost(ctx->clk_host);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -578,7 +569,7 @@ int tlq_upload(tlq_ctx* ctx, const double* U) {
   *ctx->clk_host = c;
   CK(cudaMemcpyAsync(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], carries_pressure(ctx) ? ctx->Pc : nullptr, ctx->clk,
-                          ctx->partials, init_blocks(ctx->P), ctx->stream));
+                          init_blocks(ctx->P), ctx->stream));
   ctx->cur = 0;
   if (ctx->it_base != ctx->it0) invalidate_graphs(ctx);  // captured launches read it_base
   ctx->it_base = ctx->it0;
@@ -746,7 +737,7 @@ int tlq_time_step(tlq_ctx* ctx, const double* W, double* dt) {
   CK(cudaMemcpyAsync(ctx->rb[0], W, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
   Clock c{};
   CK(cudaMemcpyAsync(ctx->rclk, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_time_step_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rclk, ctx->rpartials, init_blocks(ctx->P), ctx->stream));
+  CK(launch_time_step_aos(ctx->P, ctx->A, ctx->rb[0], ctx->rclk, init_blocks(ctx->P), ctx->stream));
   CK(cudaMemcpyAsync(&c, ctx->rclk, sizeof(Clock), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   *dt = c.dt;

@@ -123,6 +123,9 @@ struct tlq_batch {
   MemberDesc* d_desc = nullptr;
   Item* d_items = nullptr;
   int nitems = 0, cap_items = 0;
+  std::vector<unsigned char> h_cool;  // cooling-pass arguments of the surrogate members, in member order
+  void* d_cool = nullptr;
+  int ncool = 0, cool_blocks = 0;
   int blocks = 0;
   cudaGraphExec_t graph = nullptr;
   bool timing = false;
@@ -160,7 +163,6 @@ void fill_desc(tlq_batch* b, int i) {
       a.p = c->P;
       a.L = c->L;
       a.clk = c->clk;
-      a.partials = c->partials;
       a.zlen = b->zlen[i];
       a.phi = c->phi;
       a.lapf = c->lapf;
@@ -216,18 +218,48 @@ int upload_items(tlq_batch* b, const std::vector<Item>& v) {
   return TLQ_OK;
 }
 
-int refresh_desc(tlq_batch* b) {
+// Descriptors of all members, and the cooling-pass arguments of the
+// surrogate members in `which` (all when empty).
+int refresh_desc(tlq_batch* b, const std::vector<int>& which = {}) {
   for (int i = 0; i < (int)b->m.size(); ++i) fill_desc(b, i);
   BCK(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), b->h_desc.size() * sizeof(MemberDesc), cudaMemcpyHostToDevice,
                       b->stream));
+  // each surrogate member gets its own blocks of the two cooling passes: one
+  // resident wave of the network pass (152 SMs x 3 blocks) shared in
+  // proportion to the cells
+  const size_t jb = tlq::cool_job_bytes();
+  std::vector<int> cool;
+  long long cells = 0;
+  for (int i = 0; i < (int)b->m.size(); ++i) {
+    tlq_ctx* c = b->m[i];
+    if (c->cfg.cooling != TLQ_COOL_MLP) continue;
+    if (!which.empty() && std::find(which.begin(), which.end(), i) == which.end()) continue;
+    cool.push_back(i);
+    cells += (long long)c->cfg.nx * c->cfg.ny * c->cfg.nz;
+  }
+  constexpr long long WAVE = 152 * 3;
+  b->ncool = 0;
+  b->cool_blocks = 0;
+  for (int i : cool) {
+    tlq_ctx* c = b->m[i];
+    const long long ci = (long long)c->cfg.nx * c->cfg.ny * c->cfg.nz;
+    const int nblk = (int)std::max(1LL, std::min((long long)tlq::cool_pass_blocks(c->P), WAVE * ci / cells));
+    const MemberDesc& d = b->h_desc[i];
+    tlq::fill_cool_job(b->h_cool.data() + b->ncool * jb, c->P, c->L, c->U[0], c->U[1], c->it_base, c->clk,
+                       c->mlp_image, c->mlp_norm, c->mlp_box, c->gcum, c->gslope, c->cool_counts, c->mlp_cqueue,
+                       c->mlp_qcount + 1, c->mlp_queue, c->mlp_qcount, b->cool_blocks, nblk);
+    b->cool_blocks += nblk;
+    ++b->ncool;
+  }
+  if (b->ncool) BCK(cudaMemcpyAsync(b->d_cool, b->h_cool.data(), b->ncool * jb, cudaMemcpyHostToDevice, b->stream));
   return TLQ_OK;
 }
 
-// One batched step of the members in `which` (all when empty): the two
-// persistent stage launches, then the surrogate's cooling passes of the
-// members that use it (their stage 2 queued the cooling cells and left the
-// dt reduction to them).
-int enqueue_batch_step(tlq_batch* b, const std::vector<int>& which = {}) {
+// One batched step of the members the item list holds: the two persistent
+// stage launches, then the surrogate's two cooling passes over the members
+// that use it (their stage 2 queued the cooling cells and left the dt
+// reduction to them; refresh_desc wrote their arguments).
+int enqueue_batch_step(tlq_batch* b) {
   const size_t smem = sizeof(tlq::BatchSmem);
   // the specialised kernels when every member uses their limiter and solver
   bool spec = true;
@@ -244,15 +276,7 @@ int enqueue_batch_step(tlq_batch* b, const std::vector<int>& which = {}) {
     tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   }
   BCK(cudaGetLastError());
-  for (int i = 0; i < (int)b->m.size(); ++i) {
-    tlq_ctx* c = b->m[i];
-    if (c->cfg.cooling != TLQ_COOL_MLP) continue;
-    if (!which.empty() && std::find(which.begin(), which.end(), i) == which.end()) continue;
-    const MemberDesc& d = b->h_desc[i];
-    BCK(tlq::launch_cool_mlp_dt(c->P, c->L, c->U[0], c->U[1], c->it_base, c->clk, c->partials, d.gx * d.gy * d.gz,
-                                c->mlp_params, c->mlp_norm, c->mlp_box, c->gcum, c->gslope, c->cool_counts,
-                                c->mlp_cqueue, c->mlp_qcount + 1, c->mlp_queue, c->mlp_qcount, b->stream));
-  }
+  if (b->ncool) BCK(tlq::launch_cool_mlp_dt_batch(b->d_cool, b->ncool, b->cool_blocks, b->stream));
   return TLQ_OK;
 }
 
@@ -359,6 +383,8 @@ int tlq_batch_create(const tlq_config* cfgs, int n, tlq_batch** out) {
     if (tlq_set_stream(c, b->stream) != TLQ_OK) return bail(TLQ_ERR_CUDA);
   b->h_desc.resize(n);
   if (cudaMalloc(&b->d_desc, n * sizeof(MemberDesc)) != cudaSuccess) return bail(TLQ_ERR_NOMEM);
+  b->h_cool.resize((size_t)n * tlq::cool_job_bytes());
+  if (cudaMalloc(&b->d_cool, b->h_cool.size()) != cudaSuccess) return bail(TLQ_ERR_NOMEM);
   if (tlq::prepare_batch_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
   for (int q = 0; q < 2; ++q) cudaEventCreate(&b->ev[q]);
   *out = b;
@@ -372,6 +398,7 @@ int tlq_batch_destroy(tlq_batch* b) {
   for (tlq_ctx* c : b->m) tlq_destroy(c);  // the batch's stream is borrowed, not destroyed there
   cudaFree(b->d_desc);
   cudaFree(b->d_items);
+  cudaFree(b->d_cool);
   for (int q = 0; q < 2; ++q)
     if (b->ev[q]) cudaEventDestroy(b->ev[q]);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -468,8 +495,12 @@ int tlq_batch_stats_get(tlq_batch* b, tlq_batch_stats* s) {
   s->ms_per_step = b->steps_timed ? b->ms_acc / (double)b->steps_timed : 0.0;
   s->items = b->nitems;
   s->blocks = b->blocks;
-  s->launches_per_step = 2;
-  for (tlq_ctx* c : b->m) s->launches_per_step += (c->cfg.cooling == TLQ_COOL_MLP) ? 2 : 0;
+  s->launches_per_step = 2;  // the two stages, and the two cooling passes when a member uses the surrogate
+  for (tlq_ctx* c : b->m)
+    if (c->cfg.cooling == TLQ_COOL_MLP) {
+      s->launches_per_step = 4;
+      break;
+    }
   long long cells = 0;
   for (tlq_ctx* c : b->m) cells += (long long)c->cfg.nx * c->cfg.ny * c->cfg.nz;
   s->cells = cells;
@@ -528,12 +559,12 @@ int tlq_batch_autotune(tlq_batch* b, const char* cache_path, int steps, int* cho
     for (int z : {8, 16, 32, 64, 128}) {
       if (z > nz && z != 8) continue;
       for (int i : mem) b->zlen[i] = std::min(z, b->m[i]->cfg.nz);
-      int rc = refresh_desc(b);
+      int rc = refresh_desc(b, mem);
       if (!rc) rc = upload_items(b, make_items(b, mem));
       if (rc) return rc;
       for (int w = 0; w < steps + 1; ++w) {
         if (w == 1) BCK(cudaEventRecord(b->ev[0], b->stream));
-        rc = enqueue_batch_step(b, mem);
+        rc = enqueue_batch_step(b);
         if (rc) return rc;
       }
       BCK(cudaEventRecord(b->ev[1], b->stream));

@@ -25,8 +25,6 @@ struct tlq_ctx {
   float* lapf = nullptr;  // mixed form: eta * Laplacian of U between the stages
   Clock* clk = nullptr;
   Clock* clk_host = nullptr;  // pinned mirror
-  double* partials = nullptr;
-  int npartials = 0;
   double* sums_partials = nullptr;
   double* sums_out = nullptr;
   double* staging = nullptr;  // one reference-layout array
@@ -41,7 +39,6 @@ struct tlq_ctx {
   double* rb[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double* rphi = nullptr;
   Clock* rclk = nullptr;
-  double* rpartials = nullptr;
   // stage launch geometry and tensor maps
   dim3 grid{};
   int zlen = 0;
@@ -61,6 +58,7 @@ struct tlq_ctx {
   long long steps = 0;
   // learned cooling surrogate (TLQ_COOL_MLP)
   float* mlp_params = nullptr;             // FP32 master parameters (device)
+  void* mlp_image = nullptr;               // the step's image of the network (launch_pack_weights)
   float mlp_norm[6] = {0, 1, 0, 1, 0, 1};  // feature centres and half-widths
   double mlp_box[6] = {0, 0, 0, 0, 0, 0};  // training box of the features (the hull)
   bool mlp_ready = false;

@@ -16,8 +16,9 @@ constexpr int ST_NONFINITE_DT = 1;
 constexpr int ST_NEG_DENSITY = 2;
 constexpr int ST_TIMEOUT = 4;
 
-// Device-resident time of the run (mainHD.f90's t, dt, it) and the ticket of
-// the single-pass CFL reduction.
+// Device-resident time of the run (mainHD.f90's t, dt, it) and the state of
+// the single-pass CFL reduction (its ticket and running maxima, zero between
+// reductions).
 struct Clock {
   double t;          // simulated time
   double dt;         // dt of the next step (time_step's result)
@@ -26,6 +27,7 @@ struct Clock {
   long long it;      // iterations
   unsigned int ticket;
   int status;
+  unsigned long long vmax[3];  // max |u|+c, |v|+c, |w|+c so far, as max_key keys
 };
 
 // Structure-of-arrays mesh layout: 5 planes of px * nyg * nzg doubles (x
@@ -87,10 +89,11 @@ __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 
 // ---------------------------------------------------------------------------
 // Single-pass CFL reduction (time_step, source/HydroCore.f90:138-150):
-// warp shuffles -> shared memory -> one partial per block -> a ticket; the
-// last block to arrive reduces the partials and writes dt (and advances t,
-// it when `advance` is set, as `step` does at HydroCore.f90:208-209).
-// No block ever waits for another.  `partials` holds 3 doubles per block.
+// warp shuffles -> shared memory -> one maximum per block, folded into the
+// clock's running maxima by 64-bit atomic max -> a ticket; the last block to
+// arrive reads the three maxima and writes dt (and advances t, it when
+// `advance` is set, as `step` does at HydroCore.f90:208-209).  No block ever
+// waits for another, and the maximum is exact whatever the order.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_max_nan(double v) {
 #pragma unroll
@@ -122,55 +125,68 @@ __device__ __forceinline__ void block_max3(double& a, double& b, double& c, doub
   }
 }
 
-// nprev: block maxima an earlier kernel of the same step left in
-// partials[0 .. 3 nprev); this grid's go after them and the last block
-// reduces both.
-// nblocks, bid: the blocks (tiles) of this reduction and this one's index
-// (a persistent kernel reduces per mesh over the tiles it works through).
+// A maximum of signal speeds as an unsigned key whose integer order is
+// max_nan's order from 0: the bits of a positive double order like its value,
+// a NaN takes the largest key (it wins, as max_nan lets it), and values <= 0
+// the key 0 (they never beat the reduction's starting 0).  Key 0 reads back
+// as +0.0 and the largest key as a NaN.
+__device__ __forceinline__ unsigned long long max_key(double x) {
+  if (x != x) return ~0ull;
+  return x > 0.0 ? (unsigned long long)__double_as_longlong(x) : 0ull;
+}
+__device__ __forceinline__ double key_value(unsigned long long k) { return __longlong_as_double((long long)k); }
+
+// Thread 0 folds a block's maxima (from block_max3) into the clock's.
+__device__ __forceinline__ void cfl_fold(double a, double b, double c, Clock* clk) {
+  atomicMax(&clk->vmax[0], max_key(a));
+  atomicMax(&clk->vmax[1], max_key(b));
+  atomicMax(&clk->vmax[2], max_key(c));
+}
+
+// A block's maxima without finishing the reduction (a later kernel of the
+// same step, stream-ordered after this one, finishes it).
 template <int NTHREADS>
-__device__ void cfl_reduce_finalize_n(double a, double b, double c, double* partials, Clock* clk, const Params& p,
-                                      bool advance, double* red, int* s_flag, unsigned nprev, unsigned nblocks,
-                                      unsigned bid) {
+__device__ __forceinline__ void cfl_contribute(double a, double b, double c, Clock* clk, double* red) {
+  block_max3<NTHREADS>(a, b, c, red);
+  if (threadIdx.x == 0) cfl_fold(a, b, c, clk);
+}
+
+// nblocks: the blocks (tiles) of this reduction, each arriving once (a
+// persistent kernel reduces per mesh over the tiles it works through).
+// Maxima that earlier kernels of the step folded in (cfl_contribute) take
+// part.  *s_flag is set in the block that finished.
+template <int NTHREADS>
+__device__ void cfl_reduce_finalize_n(double a, double b, double c, Clock* clk, const Params& p, bool advance,
+                                      double* red, int* s_flag, unsigned nblocks) {
   block_max3<NTHREADS>(a, b, c, red);
   if (threadIdx.x == 0) {
-    partials[3 * (nprev + bid) + 0] = a;
-    partials[3 * (nprev + bid) + 1] = b;
-    partials[3 * (nprev + bid) + 2] = c;
+    cfl_fold(a, b, c, clk);
     __threadfence();
     const unsigned t = atomicAdd(&clk->ticket, 1u);
     *s_flag = (t == nblocks - 1);
   }
   __syncthreads();
-  if (!*s_flag) return;
+  if (!*s_flag || threadIdx.x != 0) return;
   __threadfence();
-  a = b = c = 0.0;
-  for (unsigned q = threadIdx.x; q < nprev + nblocks; q += NTHREADS) {
-    a = max_nan(a, ld_cg(partials + 3 * q + 0));
-    b = max_nan(b, ld_cg(partials + 3 * q + 1));
-    c = max_nan(c, ld_cg(partials + 3 * q + 2));
+  unsigned long long* vm = clk->vmax;
+  const double m0 = key_value(__ldcg(vm)), m1 = key_value(__ldcg(vm + 1)), m2 = key_value(__ldcg(vm + 2));
+  const double dtn = cfl_dt(p.cfl, p.dx, p.dy, p.dz, m0, m1, m2);
+  if (advance) {
+    clk->t = clk->t + clk->dt;
+    clk->it = clk->it + 1;
+    clk->dt_used = clk->dt;
   }
-  block_max3<NTHREADS>(a, b, c, red);
-  if (threadIdx.x == 0) {
-    const double dtn = cfl_dt(p.cfl, p.dx, p.dy, p.dz, a, b, c);
-    if (advance) {
-      clk->t = clk->t + clk->dt;
-      clk->it = clk->it + 1;
-      clk->dt_used = clk->dt;
-    }
-    clk->dt = dtn;
-    if (!(dtn > 0.0) || dtn != dtn || dtn > 1.0e300) atomicOr(&clk->status, ST_NONFINITE_DT);
-    clk->ticket = 0u;
-    __threadfence();
-  }
+  clk->dt = dtn;
+  if (!(dtn > 0.0) || dtn != dtn || dtn > 1.0e300) atomicOr(&clk->status, ST_NONFINITE_DT);
+  vm[0] = vm[1] = vm[2] = 0ull;
+  clk->ticket = 0u;
+  __threadfence();
 }
 
 template <int NTHREADS>
-__device__ __forceinline__ void cfl_reduce_finalize(double a, double b, double c, double* partials, Clock* clk,
-                                                    const Params& p, bool advance, double* red, int* s_flag,
-                                                    unsigned nprev = 0) {
-  cfl_reduce_finalize_n<NTHREADS>(a, b, c, partials, clk, p, advance, red, s_flag, nprev,
-                                  gridDim.x * gridDim.y * gridDim.z,
-                                  blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
+__device__ __forceinline__ void cfl_reduce_finalize(double a, double b, double c, Clock* clk, const Params& p,
+                                                    bool advance, double* red, int* s_flag) {
+  cfl_reduce_finalize_n<NTHREADS>(a, b, c, clk, p, advance, red, s_flag, gridDim.x * gridDim.y * gridDim.z);
 }
 
 }  // namespace tlq

@@ -51,10 +51,9 @@ cudaError_t launch_prims_soa_to_aos_clocked(const Params& p, const Aos& A, const
 cudaError_t launch_prims_soa_to_aos(const Params& p, const Aos& A, const Layout& L, const double* U,
                                     const double* P, double* W, cudaStream_t s);
 // calc_prims + time_step on the uploaded state; writes P (interior pressure)
-// when P is non-null; clk->dt receives the first dt.  `grid_blocks` returns
-// the number of partials used.
+// when P is non-null; clk->dt receives the first dt.
 cudaError_t launch_init_prims_dt(const Params& p, const Layout& L, const double* U, double* P, Clock* clk,
-                                 double* partials, int nblocks, cudaStream_t s);
+                                 int nblocks, cudaStream_t s);
 int init_blocks(const Params& p);
 cudaError_t launch_point_potential_soa(const Params& p, const Layout& L, const double* xyzm, int n, double* phi,
                                        cudaStream_t s);
@@ -68,32 +67,46 @@ cudaError_t launch_mlp_grad(const float* P, const float* X, const float* Y, cons
 cudaError_t launch_adam(float* P, float* m, float* v, const float* grad, int n, float lr, float b1, float b2,
                         float eps, int t, cudaStream_t s);
 cudaError_t launch_mlp_infer(const float* P, const float* X, int n, float* Y, cudaStream_t s);
+// The step's image of a network (its shared-memory layout, mlp_image_bytes()
+// of device memory), formed from the FP32 parameters P.
+size_t mlp_image_bytes();
+cudaError_t launch_pack_weights(const float* P, void* img, cudaStream_t s);
 cudaError_t launch_cool_pairs(const Params& p, long long N, unsigned long long seed, const double box[6], float* X,
                               float* Y, float* Wt, double* raw, cudaStream_t s);
 cudaError_t launch_gather_pairs(const float* X, const float* Y, const float* Wt, const long long* perm, long long N,
                                 float* X2, float* Y2, float* Wt2, cudaStream_t s);
 cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStream_t s);
 // Surrogate cooling + dt reduction of the mixed step (tlq_surrogate.cu).
-// Stage 2 queues the cells that cool (cqueue) and leaves its nstage block
-// maxima in partials; the network pass cools them or queues them for the
-// exact integrator (queue); the fallback pass cools those and finishes the
-// dt reduction over all block maxima.  Queues: capacity nx ny nz; counts
-// zero between steps.
+// Stage 2 queues the cells that cool (cqueue) and folds its block maxima
+// into the clock's; the network pass cools the queued cells or queues them
+// for the exact integrator (queue); the fallback pass cools those and
+// finishes the dt reduction.  Queues: capacity nx ny nz; counts zero
+// between steps.
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
-                               Clock* clk, double* partials,
-                               int nstage, const float* P, const float norm[6], const double box[6],
+                               Clock* clk, const void* img, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,
                                const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
                                cudaStream_t s);
-int cool_mlp_blocks(const Params& p);  // block maxima both passes add to partials
+// The same two passes for several meshes in two launches: fill_cool_job
+// writes one mesh's arguments (cool_job_bytes() of them) into a host array
+// that is copied to the device; mesh m runs on blocks [blk0, blk0 + nblk) of
+// each pass (ranges ascending and back to back from 0, nblk between 1 and
+// cool_pass_blocks, nblocks their total).
+size_t cool_job_bytes();
+int cool_pass_blocks(const Params& p);
+void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, double* U1, long long it_base, Clock* clk,
+                   const void* img, const float norm[6], const double box[6],
+                   const float* gcum, const float* gslope, unsigned long long* counts, const unsigned* cqueue,
+                   unsigned* cqcount, unsigned* queue, unsigned* qcount, int blk0, int nblk);
+cudaError_t launch_cool_mlp_dt_batch(const void* jobs, int njobs, int nblocks, cudaStream_t s);
 
 // log10 of a small device array in place (cooling-table temperatures).
 cudaError_t launch_log10_inplace(double* v, int n, cudaStream_t s);
 
 // Per-routine kernels on the reference layout.
 cudaError_t launch_calc_prims_aos(const Params& p, const Aos& A, double* W, const double* U, cudaStream_t s);
-cudaError_t launch_time_step_aos(const Params& p, const Aos& A, const double* W, Clock* clk, double* partials,
-                                 int nblocks, cudaStream_t s);
+cudaError_t launch_time_step_aos(const Params& p, const Aos& A, const double* W, Clock* clk, int nblocks,
+                                 cudaStream_t s);
 cudaError_t launch_fluxes_aos(const Params& p, const Aos& A, const double* U, const double* W, double* F, double* G,
                               double* H, int choice, cudaStream_t s);
 cudaError_t launch_godunov_aos(const Params& p, const Aos& A, double* out, const double* UU, const double* F,

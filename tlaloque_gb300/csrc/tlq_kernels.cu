@@ -153,7 +153,7 @@ int init_blocks(const Params& p) {
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_init_prims_dt(Params p, Layout L, const double* __restrict__ U,
-                                                               double* __restrict__ P, Clock* clk, double* partials) {
+                                                               double* __restrict__ P, Clock* clk) {
   __shared__ double red[96];
   __shared__ int flag;
   const long long n = (long long)p.nx * p.ny * p.nz;
@@ -174,12 +174,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_init_prims_dt(Params p, Layout 
     m1 = max_nan(m1, v3[1]);
     m2 = max_nan(m2, v3[2]);
   }
-  cfl_reduce_finalize<RED_THREADS>(m0, m1, m2, partials, clk, p, false, red, &flag);
+  cfl_reduce_finalize<RED_THREADS>(m0, m1, m2, clk, p, false, red, &flag);
 }
 
 cudaError_t launch_init_prims_dt(const Params& p, const Layout& L, const double* U, double* P, Clock* clk,
-                                 double* partials, int nblocks, cudaStream_t s) {
-  k_init_prims_dt<<<nblocks, RED_THREADS, 0, s>>>(p, L, U, P, clk, partials);
+                                 int nblocks, cudaStream_t s) {
+  k_init_prims_dt<<<nblocks, RED_THREADS, 0, s>>>(p, L, U, P, clk);
   return cudaGetLastError();
 }
 
@@ -318,7 +318,7 @@ __global__ void k_calc_prims_aos(Params p, Aos A, double* __restrict__ W, const 
 
 // time_step, source/HydroCore.f90:113-155 (interior, single-pass reduction).
 __global__ void __launch_bounds__(RED_THREADS) k_time_step_aos(Params p, Aos A, const double* __restrict__ W,
-                                                               Clock* clk, double* partials) {
+                                                               Clock* clk) {
   __shared__ double red[96];
   __shared__ int flag;
   const long long n = (long long)p.nx * p.ny * p.nz;
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_time_step_aos(Params p, Aos A, 
     m1 = max_nan(m1, v3[1]);
     m2 = max_nan(m2, v3[2]);
   }
-  cfl_reduce_finalize<RED_THREADS>(m0, m1, m2, partials, clk, p, false, red, &flag);
+  cfl_reduce_finalize<RED_THREADS>(m0, m1, m2, clk, p, false, red, &flag);
 }
 
 // HLLCFluxes / HLLFluxes, faces i, j, k in 0..n (source/HLLC.f90:94-96, :223-225).
@@ -540,9 +540,9 @@ cudaError_t launch_calc_prims_aos(const Params& p, const Aos& A, double* W, cons
   k_calc_prims_aos<<<grid_for(A.cells()), BT, 0, s>>>(p, A, W, U);
   return cudaGetLastError();
 }
-cudaError_t launch_time_step_aos(const Params& p, const Aos& A, const double* W, Clock* clk, double* partials,
-                                 int nblocks, cudaStream_t s) {
-  k_time_step_aos<<<nblocks, RED_THREADS, 0, s>>>(p, A, W, clk, partials);
+cudaError_t launch_time_step_aos(const Params& p, const Aos& A, const double* W, Clock* clk, int nblocks,
+                                 cudaStream_t s) {
+  k_time_step_aos<<<nblocks, RED_THREADS, 0, s>>>(p, A, W, clk);
   return cudaGetLastError();
 }
 cudaError_t launch_fluxes_aos(const Params& p, const Aos& A, const double* U, const double* W, double* F, double* G,

@@ -386,6 +386,19 @@ cudaError_t launch_adam(float* P, float* m, float* v, const float* grad, int n, 
   return cudaGetLastError();
 }
 
+namespace {
+__global__ void k_pack_weights(const float* __restrict__ P, mlp::SmemWeights* img) { mlp::load_weights(P, *img, nullptr); }
+}  // namespace
+
+size_t mlp_image_bytes() { return sizeof(mlp::SmemWeights); }
+
+cudaError_t launch_pack_weights(const float* P, void* img, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(img, 0, sizeof(mlp::SmemWeights), s);  // (struct padding too)
+  if (e != cudaSuccess) return e;
+  k_pack_weights<<<1, 256, 0, s>>>(P, static_cast<mlp::SmemWeights*>(img));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mlp_infer(const float* P, const float* X, int n, float* Y, cudaStream_t s) {
   const int tiles = (n + mlp::TS - 1) / mlp::TS;
   const int blocks = std::max(1, std::min((tiles + mlp::TW - 1) / mlp::TW, 152 * 8));

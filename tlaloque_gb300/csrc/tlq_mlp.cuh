@@ -87,6 +87,28 @@ __device__ inline void load_weights(const float* __restrict__ P, SmemWeights& W,
   if (threadIdx.x == 0) W.b4 = P[OFF_B4];
 }
 
+// A block's copy of a network image that pack_weights (tlq_mlp.cu) formed
+// once in device memory with load_weights: 16-byte loads, all of a thread's
+// issued before the first store, instead of load_weights' scalar gathers
+// and conversions in every block.  Same bytes, so the same results.
+template <int NT>
+__device__ __forceinline__ void copy_weights(const SmemWeights* __restrict__ img, SmemWeights& W) {
+  constexpr int NV = (int)(sizeof(SmemWeights) / 16), R = (NV + NT - 1) / NT;
+  const uint4* __restrict__ src = reinterpret_cast<const uint4*>(img);
+  uint4* dst = reinterpret_cast<uint4*>(&W);
+  uint4 v[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = (int)threadIdx.x + r * NT;
+    if (q < NV) v[r] = __ldg(src + q);
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = (int)threadIdx.x + r * NT;
+    if (q < NV) dst[q] = v[r];
+  }
+}
+
 // Input layer in FP32 for one m16 tile, straight into the accumulator
 // layout: acc[j] = (rows g, g+8) x (columns 8j+2tig, 8j+2tig+1).
 __device__ __forceinline__ void input_layer(float acc[8][4], const SmemWeights& W, const float* xg, const float* xg8,

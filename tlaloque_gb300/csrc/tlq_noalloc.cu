@@ -9,10 +9,9 @@
 // own; this entry point then allocates nothing at all: no cudaMalloc, no
 // cudaFree, no allocating library routine.
 //
-// The per-block partial maxima and the ticket of the single-pass CFL
-// reduction live in one file-scope device array of fixed size (below), which
-// every GPU that loads the library holds until the process exits.  That
-// fixes the largest mesh this entry point accepts.
+// The ticket and the running maxima of the single-pass CFL reduction live in
+// one file-scope device variable (below, 72 bytes), which every GPU that
+// loads the library holds until the process exits.
 #include <mutex>
 
 #include "../../include/tlq.h"
@@ -24,22 +23,18 @@ namespace {
 constexpr int NA_THREADS = 256;
 constexpr int NA_CELLS_PER_THREAD = 16;
 constexpr long long NA_CELLS_PER_BLOCK = (long long)NA_THREADS * NA_CELLS_PER_THREAD;  // 4096
-constexpr int NA_MAX_BLOCKS = 8192;
-constexpr long long NA_MAX_CELLS = NA_CELLS_PER_BLOCK * NA_MAX_BLOCKS;  // 33,554,432 interior cells
 constexpr int NA_MAX_DEVICES = 64;
 
 struct NoAllocScratch {
-  Clock clk;                          // ticket (must start at 0) and the reduction's dt
-  double partials[3 * NA_MAX_BLOCKS];  // one (max |u|+c, max |v|+c, max |w|+c) per block
+  Clock clk;  // the reduction's ticket and maxima (zero before a call) and its dt
 };
 
-// The scratch: 196,656 bytes per device.  Host code must not use this name as
-// an address; it looks the device address up once per device (below).
+// The scratch, per device.  Host code must not use this name as an address;
+// it looks the device address up once per device (below).
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 // Same reduction as the per-routine time_step kernel, with a fixed chunk of
-// NA_CELLS_PER_BLOCK interior cells per block so that the number of partials
-// (and hence the scratch needed) follows from the mesh size.
+// NA_CELLS_PER_BLOCK interior cells per block.
 __global__ void __launch_bounds__(NA_THREADS) k_time_step_noalloc(Params p, Aos A, const double* __restrict__ W,
                                                                   NoAllocScratch* sc, double* d_dt) {
   __shared__ double red[96];
@@ -62,7 +57,7 @@ __global__ void __launch_bounds__(NA_THREADS) k_time_step_noalloc(Params p, Aos 
     m1 = max_nan(m1, v3[1]);
     m2 = max_nan(m2, v3[2]);
   }
-  cfl_reduce_finalize<NA_THREADS>(m0, m1, m2, sc->partials, &sc->clk, p, false, red, &flag);
+  cfl_reduce_finalize<NA_THREADS>(m0, m1, m2, &sc->clk, p, false, red, &flag);
   if (flag && threadIdx.x == 0) *d_dt = sc->clk.dt;
 }
 
@@ -95,7 +90,6 @@ extern "C" int tlq_time_step_noalloc(const double* d_uprim, int nx, int ny, int 
   using namespace tlq;
   if (!d_uprim || !d_dt || nx < 1 || ny < 1 || nz < 1) return TLQ_ERR_ARG;
   const long long n = (long long)nx * ny * nz;
-  if (n > NA_MAX_CELLS) return TLQ_ERR_ARG;  // more interior cells than the fixed scratch can reduce
   NoAllocScratch* sc = nullptr;
   if (scratch_address(&sc) != cudaSuccess) return TLQ_ERR_CUDA;
   Params p{};
@@ -104,9 +98,11 @@ extern "C" int tlq_time_step_noalloc(const double* d_uprim, int nx, int ny, int 
   p.gamma = gamma;
   p.cfl = cfl;
   const Aos A{nx, ny, nz};
-  const int nblocks = (int)((n + NA_CELLS_PER_BLOCK - 1) / NA_CELLS_PER_BLOCK);
+  const long long nblk = (n + NA_CELLS_PER_BLOCK - 1) / NA_CELLS_PER_BLOCK;
+  if (nblk > 0x7fffffffLL) return TLQ_ERR_ARG;  // beyond one grid's x extent
+  const int nblocks = (int)nblk;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
-  // The array keeps the previous call's contents: the ticket must start at 0.
+  // The scratch keeps the previous call's contents: ticket and maxima must start at 0.
   if (cudaMemsetAsync(&sc->clk, 0, sizeof(Clock), s) != cudaSuccess) return TLQ_ERR_CUDA;
   k_time_step_noalloc<<<nblocks, NA_THREADS, 0, s>>>(p, A, d_uprim, sc, d_dt);
   return cudaGetLastError() == cudaSuccess ? TLQ_OK : TLQ_ERR_CUDA;

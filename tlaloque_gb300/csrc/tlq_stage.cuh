@@ -42,8 +42,7 @@ struct StageArgs {
   double* out;         // STAGE 1: UPP; STAGE 2: U of the next step
   double* pout;        // STAGE 2 with cooling: carried (cooled) interior pressure
   const double* phi;   // point-mass potential plane (null without gravity)
-  Clock* clk;
-  double* partials;    // 3 doubles per block (CFL reduction scratch)
+  Clock* clk;          // time, and the CFL reduction's ticket and maxima
   int zlen;            // planes per block
   int use_p;           // STAGE 1 with cooling: interior pressure from the P plane
   float* lapf;         // mixed form: eta * Laplacian of U (FP32, written by stage 1, read by stage 2)
@@ -382,7 +381,7 @@ __global__ void __launch_bounds__(NT, 2)
     }
     m0 = m1 = m2 = NAN;
   }
-  if (STAGE == 2) cfl_reduce_finalize<NT>(m0, m1, m2, a.partials, clk, p, true, s.red, &s.flag);
+  if (STAGE == 2) cfl_reduce_finalize<NT>(m0, m1, m2, clk, p, true, s.red, &s.flag);
 }
 
 }  // namespace tlq

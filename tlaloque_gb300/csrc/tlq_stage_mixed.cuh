@@ -47,7 +47,10 @@ struct MixedSmem {
 
 // One cell: FP64 conserved (stride vs) -> FP32 conserved and primitives.
 // The pressure of a cell whose kinetic energy exceeds 0.99 of its total
-// energy is recovered in FP64 (FP32 would lose it to cancellation).
+// energy is recovered in FP64 (FP32 would lose it to cancellation).  The
+// sums are written with explicit-rounding intrinsics, so the compiler cannot
+// contract them differently in the kernels that inline this (the stages,
+// the surrogate's passes): every kernel gets the same bits for a cell.
 __device__ __forceinline__ void mixed_cell(float gm1, const double* u, long long vs, float* cf, float* w) {
 #pragma unroll
   for (int e = 0; e < 5; ++e) cf[e] = d2f(u[e * vs]);
@@ -56,13 +59,15 @@ __device__ __forceinline__ void mixed_cell(float gm1, const double* u, long long
   w[1] = cf[1] * inv;
   w[2] = cf[2] * inv;
   w[3] = cf[3] * inv;
-  const float ek = 0.5f * (cf[1] * w[1] + cf[2] * w[2] + cf[3] * w[3]);
+  const float ek =
+      __fmul_rn(0.5f, __fmaf_rn(cf[3], w[3], __fmaf_rn(cf[2], w[2], __fmul_rn(cf[1], w[1]))));
   float p;
-  if (ek > 0.99f * cf[4]) {
+  if (ek > __fmul_rn(0.99f, cf[4])) {
     const double r = u[0], m1 = u[vs], m2 = u[2 * vs], m3 = u[3 * vs], E = u[4 * vs];
-    p = d2f((double)gm1 * (E - 0.5 * ((m1 * m1 + m2 * m2) + m3 * m3) / r));
+    const double k2 = __fma_rn(m3, m3, __fma_rn(m2, m2, __dmul_rn(m1, m1)));
+    p = d2f(__dmul_rn((double)gm1, __dsub_rn(E, __ddiv_rn(__dmul_rn(0.5, k2), r))));
   } else {
-    p = gm1 * (cf[4] - ek);
+    p = __fmul_rn(gm1, __fsub_rn(cf[4], ek));
   }
   w[4] = fmaxf(p, 1e-20f);
 }
@@ -80,7 +85,7 @@ __device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
   if (lo >= t.n) return exp10f(t.Cf[t.n - 1]);
   const float T0 = t.logTf[lo - 1], C0 = t.Cf[lo - 1];
   const float T1 = t.logTf[lo], C1 = t.Cf[lo];
-  return exp10f((C1 - C0) / (T1 - T0) * (log10f(temp) - T0) + C0);
+  return exp10f(__fmaf_rn((C1 - C0) / (T1 - T0), __fsub_rn(log10f(temp), T0), C0));
 }
 
 // Whether cooling applies (temp >= the table's first temperature,
@@ -90,7 +95,7 @@ __device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
 // plain step's arithmetic (uncontracted intrinsics), so both forms agree.
 __device__ __forceinline__ bool cools_at(const Params& p, float temp, const double* u) {
   const float Tmin = p.cool.Tf[0];
-  if (fabsf(temp - Tmin) > 1e-6f * Tmin) return temp >= Tmin;
+  if (fabsf(__fsub_rn(temp, Tmin)) > 1e-6f * Tmin) return temp >= Tmin;
   const double r = u[0];
   const double k2 = __dadd_rn(__dadd_rn(__dmul_rn(u[1], u[1]), __dmul_rn(u[2], u[2])), __dmul_rn(u[3], u[3]));
   double pr = __dmul_rn(__dsub_rn(p.gamma, 1.0), __dsub_rn(u[4], __ddiv_rn(__dmul_rn(0.5, k2), r)));
@@ -136,7 +141,7 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
     w[4] = w[4] * f;
     if (floored) break;
   }
-  u4 = u4 + f2d((w[4] - p0) / gm1);
+  u4 = u4 + f2d(__fsub_rn(w[4], p0) / gm1);
 }
 
 // One tile (MTX x MTY columns, z-chunk bz of zlen planes) of a stage: the
@@ -472,16 +477,11 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   }
   if (STAGE == 2) {
     if (p.cooling != COOL_MLP) {
-      cfl_reduce_finalize_n<MNT>(d0, d1, d2, a.partials, clk, p, true, s.red, &s.flag, 0, nblk, bid);
+      cfl_reduce_finalize_n<MNT>(d0, d1, d2, clk, p, true, s.red, &s.flag, nblk);
     } else {
       // with the surrogate the cooling passes finish the reduction over
       // these block maxima and their own
-      block_max3<MNT>(d0, d1, d2, s.red);
-      if (tid == 0) {
-        a.partials[3 * bid + 0] = d0;
-        a.partials[3 * bid + 1] = d1;
-        a.partials[3 * bid + 2] = d2;
-      }
+      cfl_contribute<MNT>(d0, d1, d2, clk, s.red);
     }
   }
 }

@@ -26,7 +26,7 @@ namespace tlq {
 namespace {
 
 struct SurrogateArgs {
-  const float* P;       // FP32 network parameters
+  const mlp::SmemWeights* img;  // the network's image (launch_pack_weights)
   float norm[6];        // centre, half-width per feature
   float box[6];         // training box (lo, hi per feature)
   const float* gcum;    // closed-form integral at the table nodes
@@ -71,15 +71,14 @@ __device__ __forceinline__ float g_inv(const CoolTable& t, const SurrogateArgs& 
 }
 
 constexpr int CT = 128;      // threads per block of the network pass
-constexpr int CB = 152 * 4;  // blocks of the network pass (at most)
 constexpr int FT = 128;      // threads per block of the fallback pass
-constexpr int FB = 152 * 4;  // blocks of the fallback pass (at most)
+constexpr int PB = 152 * 3;  // blocks of each pass (at most): one resident wave of the network pass
 
 // Blocks of each cooling pass for a mesh: enough for its cells to cool at
-// once (2048 cells a block), at most 4 per SM.
+// once (2048 cells a block), at most one wave.
 int pass_blocks(const Params& p) {
   const long long n = (long long)p.nx * p.ny * p.nz;
-  return (int)std::max<long long>(4, std::min<long long>((n + 2047) / 2048, CB));
+  return (int)std::max<long long>(4, std::min<long long>((n + 2047) / 2048, PB));
 }
 
 __device__ __forceinline__ void speeds_max(const float* w, float gf, float& m0, float& m1, float& m2) {
@@ -106,7 +105,8 @@ __device__ __forceinline__ long long interior_offset(const Params& p, const Layo
 // the table's first temperature within the step (closed form: G_t <= 0):
 // there the reference integrator's last sub-step decides how far below that
 // temperature the cell ends.  The block maxima of the signal speeds of the
-// accepted cells go to partials after the stage-2 blocks' (nprev of them).
+// cells cooled here are folded into the clock's (stage 2 left out the cells
+// it queued).
 // The state the step just wrote: U1 or U0 by the clock's buffer parity (the
 // clock has not advanced yet), so that one captured launch serves both
 // parities.
@@ -114,21 +114,62 @@ __device__ __forceinline__ double* step_output(double* U0, double* U1, const Clo
   return ((clk->it - it_base) & 1LL) ? U0 : U1;
 }
 
-__global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0, double* U1, long long it_base,
-                                                 const Clock* clk,
-                                                 double* partials, unsigned nprev, SurrogateArgs sa,
-                                                 const unsigned* __restrict__ cqueue, const unsigned* cqcount,
-                                                 unsigned* __restrict__ queue, unsigned* qcount) {
-  __shared__ mlp::SmemWeights W;
-  __shared__ double red[96];
-  if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
-  const long long n = (long long)*cqcount;
-  if ((long long)blockIdx.x * CT >= n) {  // no queued cell for this block: a neutral maximum, no weights
-    if (threadIdx.x < 3) partials[3 * (nprev + blockIdx.x) + threadIdx.x] = 0.0;
-    return;
+// Everything one mesh's cooling passes need (a kernel argument for one
+// mesh, a device array entry for a batch of them).
+struct CoolJob {
+  Params p;  // the run's parameters, cooling = the sub-cycled integrator (the fallback)
+  Layout L;
+  double* U0;
+  double* U1;
+  long long it_base;
+  Clock* clk;
+  SurrogateArgs sa;
+  const unsigned* cqueue;  // cells stage 2 queued (they cool)
+  unsigned* cqcount;
+  unsigned* queue;  // cells handed to the exact integrator
+  unsigned* qcount;
+  unsigned blk0, nblk;  // this mesh's blocks of each pass: [blk0, blk0 + nblk)
+};
+
+// The mesh block b of a pass works on: `one` for a single mesh (jobs null),
+// else the job whose block range holds b (ranges ascending, back to back).
+__device__ __forceinline__ const CoolJob* job_of_block(const CoolJob& one, const CoolJob* jobs, int njobs,
+                                                      unsigned b) {
+  if (!jobs) return &one;
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= b) lo = mid; else hi = mid - 1;
   }
-  double* __restrict__ U = step_output(U0, U1, clk, it_base);
-  mlp::load_weights(sa.P, W, nullptr);
+  return &jobs[lo];
+}
+
+// A block's copy of its job in shared memory (8-byte words): the passes read
+// their arguments from there whichever path launched them.
+static_assert(sizeof(CoolJob) % 8 == 0 && alignof(CoolJob) <= 16, "CoolJob copies as 8-byte words");
+struct SmemJob {
+  alignas(16) unsigned long long w[sizeof(CoolJob) / 8];
+};
+__device__ __forceinline__ const CoolJob& stage_job(SmemJob& s, const CoolJob* src) {
+  const unsigned long long* from = reinterpret_cast<const unsigned long long*>(src);
+  for (int q = threadIdx.x; q < (int)(sizeof(CoolJob) / 8); q += blockDim.x) s.w[q] = from[q];
+  __syncthreads();
+  return *reinterpret_cast<const CoolJob*>(s.w);
+}
+
+__device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red, unsigned nblocks, unsigned bid) {
+  const Params& p = j.p;
+  const Layout& L = j.L;
+  const Clock* clk = j.clk;
+  const SurrogateArgs& sa = j.sa;
+  const unsigned* __restrict__ cqueue = j.cqueue;
+  unsigned* __restrict__ queue = j.queue;
+  unsigned* qcount = j.qcount;
+  if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
+  const long long n = (long long)*j.cqcount;
+  if ((long long)bid * CT >= n) return;  // no queued cell for this block: no weights, nothing to fold
+  double* __restrict__ U = step_output(j.U0, j.U1, clk, j.it_base);
+  mlp::copy_weights<CT>(sa.img, W);
   __syncthreads();
   const CoolTable& tab = p.cool;
   const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
@@ -139,7 +180,7 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
   unsigned long long used = 0, fell = 0, one = 0;
   // warp-uniform trip count: the network's tiles need all 32 lanes
-  for (long long base = (long long)blockIdx.x * CT; base < n; base += (long long)gridDim.x * CT) {
+  for (long long base = (long long)bid * CT; base < n; base += (long long)nblocks * CT) {
     const long long q = base + threadIdx.x;
     const bool valid = q < n;
     long long o = 0, cidx = 0;
@@ -240,35 +281,36 @@ __global__ void __launch_bounds__(CT) k_cool_net(Params p, Layout L, double* U0,
     atomicAdd(&sa.counts[1], fell);
     atomicAdd(&sa.counts[2], one);
   }
-  double a = f2d(m0), b = f2d(m1), c = f2d(m2);
-  block_max3<CT>(a, b, c, red);
-  if (threadIdx.x == 0) {
-    partials[3 * (nprev + blockIdx.x) + 0] = a;
-    partials[3 * (nprev + blockIdx.x) + 1] = b;
-    partials[3 * (nprev + blockIdx.x) + 2] = c;
-  }
+  cfl_contribute<CT>(f2d(m0), f2d(m1), f2d(m2), j.clk, red);
 }
 
-// Pass 2 (fallback): the queued cells through the exact integrator (the
-// sub-cycled cooling with the run's sub-step settings), then the dt
-// reduction over the block maxima of stage 2 and both passes (nprev before
-// this pass's); the last block empties both queues.
-__global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, double* U0, double* U1,
-                                                         long long it_base, Clock* clk,
-                                                         double* partials, unsigned nprev,
-                                                         const unsigned* __restrict__ queue, unsigned* qcount,
-                                                         unsigned* cqcount) {
+// The network pass of one mesh (jobs null: `one`) or of njobs meshes, each
+// on its own range of the grid's blocks.  One kernel, one call site: the
+// single-mesh and batched steps run the same instructions, so their FP32
+// results agree bit for bit.
+__global__ void __launch_bounds__(CT, 3) k_cool_net(const __grid_constant__ CoolJob one,
+                                                 const CoolJob* __restrict__ jobs, int njobs) {
+  __shared__ mlp::SmemWeights W;
   __shared__ double red[96];
-  __shared__ int flag;
+  __shared__ SmemJob sj;
+  const CoolJob& j = stage_job(sj, job_of_block(one, jobs, njobs, blockIdx.x));
+  cool_net_mesh(j, W, red, j.nblk, blockIdx.x - j.blk0);
+}
+
+__device__ void cool_fallback_mesh(const CoolJob& j, double* red, int* flag, unsigned nblocks, unsigned bid) {
+  const Params& p = j.p;
+  const Layout& L = j.L;
+  Clock* clk = j.clk;
   if (!(clk->t < clk->tfin)) return;
-  double* __restrict__ U = step_output(U0, U1, clk, it_base);
-  const unsigned nq = *qcount;
+  double* __restrict__ U = step_output(j.U0, j.U1, clk, j.it_base);
+  const unsigned* __restrict__ queue = j.queue;
+  const unsigned nq = *j.qcount;
   const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
   const float cT = p.f_cT;
   const float inv_muamu = p.f_inv_muamu;
   const float dtf = d2f(clk->dt);
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-  for (unsigned q = blockIdx.x * FT + threadIdx.x; q < nq; q += gridDim.x * FT) {
+  for (unsigned q = bid * FT + threadIdx.x; q < nq; q += nblocks * FT) {
     const long long o = interior_offset(p, L, (long long)queue[q]);
     double u[5];
 #pragma unroll
@@ -279,44 +321,88 @@ __global__ void __launch_bounds__(FT) k_cool_fallback_dt(Params p, Layout L, dou
     U[4 * L.plane + o] = u[4];
     speeds_max(w, gf, m0, m1, m2);
   }
-  cfl_reduce_finalize<FT>(f2d(m0), f2d(m1), f2d(m2), partials, clk, p, true, red, &flag, nprev);
-  if (flag && threadIdx.x == 0) {
-    *qcount = 0u;
-    *cqcount = 0u;
+  cfl_reduce_finalize_n<FT>(f2d(m0), f2d(m1), f2d(m2), clk, p, true, red, flag, nblocks);
+  if (*flag && threadIdx.x == 0) {
+    *j.qcount = 0u;
+    *j.cqcount = 0u;
   }
+}
+
+// Pass 2 (fallback): the queued cells through the exact integrator (the
+// sub-cycled cooling with the run's sub-step settings), then the dt
+// reduction over the block maxima of stage 2 and both passes (the same
+// number of blocks each); the last block of a mesh empties its queues.  One
+// mesh (jobs null: `one`) or njobs meshes, as the network pass.
+__global__ void __launch_bounds__(FT) k_cool_fallback_dt(const __grid_constant__ CoolJob one,
+                                                         const CoolJob* __restrict__ jobs, int njobs) {
+  __shared__ double red[96];
+  __shared__ int flag;
+  __shared__ SmemJob sj;
+  const CoolJob& j = stage_job(sj, job_of_block(one, jobs, njobs, blockIdx.x));
+  cool_fallback_mesh(j, red, &flag, j.nblk, blockIdx.x - j.blk0);
 }
 
 }  // namespace
 
+size_t cool_job_bytes() { return sizeof(CoolJob); }
+
+void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, double* U1, long long it_base, Clock* clk,
+                   const void* img, const float norm[6], const double box[6],
+                   const float* gcum, const float* gslope, unsigned long long* counts, const unsigned* cqueue,
+                   unsigned* cqcount, unsigned* queue, unsigned* qcount, int blk0, int nblk) {
+  CoolJob j{};
+  j.p = p;
+  j.p.cooling = COOL_SUBCYCLE;  // the fallback: the sub-cycled integrator with the run's sub-step settings
+  j.L = L;
+  j.U0 = U0;
+  j.U1 = U1;
+  j.it_base = it_base;
+  j.clk = clk;
+  j.sa.img = static_cast<const mlp::SmemWeights*>(img);
+  for (int q = 0; q < 6; ++q) {
+    j.sa.norm[q] = norm[q];
+    j.sa.box[q] = (float)box[q];
+  }
+  j.sa.gcum = gcum;
+  j.sa.gslope = gslope;
+  j.sa.counts = counts;
+  j.cqueue = cqueue;
+  j.cqcount = cqcount;
+  j.queue = queue;
+  j.qcount = qcount;
+  j.blk0 = (unsigned)blk0;
+  j.nblk = (unsigned)nblk;
+  std::memcpy(dst, &j, sizeof j);
+}
+
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
-                               Clock* clk, double* partials,
-                               int nstage, const float* P, const float norm[6], const double box[6],
+                               Clock* clk, const void* img, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,
                                const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
                                cudaStream_t s) {
-  // the fallback is the sub-cycled integrator with the run's sub-step settings
-  Params pf = p;
-  pf.cooling = COOL_SUBCYCLE;
-  SurrogateArgs sa{};
-  sa.P = P;
-  for (int q = 0; q < 6; ++q) {
-    sa.norm[q] = norm[q];
-    sa.box[q] = (float)box[q];
-  }
-  sa.gcum = gcum;
-  sa.gslope = gslope;
-  sa.counts = counts;
   const int nb = pass_blocks(p);
-  k_cool_net<<<nb, CT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)nstage, sa, cqueue, cqcount, queue,
-                               qcount);
+  CoolJob j;
+  fill_cool_job(&j, p, L, U0, U1, it_base, clk, img, norm, box, gcum, gslope, counts, cqueue, cqcount, queue, qcount, 0,
+                nb);
+  k_cool_net<<<nb, CT, 0, s>>>(j, nullptr, 1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cool_fallback_dt<<<nb, FT, 0, s>>>(pf, L, U0, U1, it_base, clk, partials, (unsigned)(nstage + nb), queue, qcount,
-                                       cqcount);
+  k_cool_fallback_dt<<<nb, FT, 0, s>>>(j, nullptr, 1);
   return cudaGetLastError();
 }
 
-int cool_mlp_blocks(const Params&) { return CB + FB; }
+int cool_pass_blocks(const Params& p) { return pass_blocks(p); }
+
+cudaError_t launch_cool_mlp_dt_batch(const void* jobs, int njobs, int nblocks, cudaStream_t s) {
+  const CoolJob* d = static_cast<const CoolJob*>(jobs);
+  const CoolJob none{};
+  k_cool_net<<<nblocks, CT, 0, s>>>(none, d, njobs);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cool_fallback_dt<<<nblocks, FT, 0, s>>>(none, d, njobs);
+  return cudaGetLastError();
+}
+
 
 }  // namespace tlq
 
@@ -548,8 +634,18 @@ int tlq_train_cooling_surrogate(tlq_ctx* ctx, const tlq_surrogate_opts* opts, tl
   }
   if (rel.empty()) rel.push_back(0.0);
   std::sort(rel.begin(), rel.end());
+  if (!ctx->mlp_image && cudaMalloc(&ctx->mlp_image, tlq::mlp_image_bytes()) != cudaSuccess) {
+    cleanup();
+    cudaFree(P);
+    return sfail(ctx, TLQ_ERR_NOMEM, "network image");  // (the previous network, if any, stays)
+  }
   cudaFree(ctx->mlp_params);
   ctx->mlp_params = P;
+  if (tlq::launch_pack_weights(P, ctx->mlp_image, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    cleanup();
+    ctx->mlp_ready = false;
+    return sfail(ctx, TLQ_ERR_CUDA, "network image");
+  }
   for (int q = 0; q < 6; ++q) {
     ctx->mlp_norm[q] = norm[q];
     ctx->mlp_box[q] = o.box[q];
@@ -585,8 +681,12 @@ int tlq_get_cooling_surrogate(tlq_ctx* ctx, float* params, float* norm6, double*
 
 int tlq_set_cooling_surrogate(tlq_ctx* ctx, const float* params, const float* norm6, const double* box6) {
   if (!ctx || !params || !norm6 || !box6) return TLQ_ERR_ARG;
+  ctx->mlp_ready = false;  // until the parameters and their image are the new network's
   if (!ctx->mlp_params) SCK(cudaMalloc(&ctx->mlp_params, tlq::mlp::NPARAM * sizeof(float)));
   SCK(cudaMemcpy(ctx->mlp_params, params, tlq::mlp::NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+  if (!ctx->mlp_image) SCK(cudaMalloc(&ctx->mlp_image, tlq::mlp_image_bytes()));
+  SCK(tlq::launch_pack_weights(ctx->mlp_params, ctx->mlp_image, ctx->stream));
+  SCK(cudaStreamSynchronize(ctx->stream));
   std::memcpy(ctx->mlp_norm, norm6, 6 * sizeof(float));
   std::memcpy(ctx->mlp_box, box6, 6 * sizeof(double));
   ctx->mlp_ready = true;
