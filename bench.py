@@ -51,6 +51,13 @@ if ROOT not in sys.path:
 METRIC = "zone-updates/s on 1 GB300 at 256³ (mixed+surrogate vs plain FP64 at ≤1% L1 err); HBM GB/s"
 UNIT = "zone-updates/s"
 
+# FP64 operations per zone-update of the reference algorithm (add, mul, div,
+# sqrt, exp/log/pow; comparisons not counted), counted by the oracle's
+# counting build at each workload's size: python -m oracle.flops_report
+# --wind-n 256 --sedov-n 128 (one step after the first).
+FP64_FLOPS_PER_ZONE = {"wind256": 1022.8, "sedov128": 774.5, "sod": 1338.3}
+FP64_TFLOPS_NOMINAL = 1.25  # GB300 dense FP64, nominal (no measured figure on this machine)
+
 
 def load_peaks():
     try:
@@ -153,13 +160,14 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def cpu_oracle_rate(cfg, U0, budget_s: float, nthreads: int, min_steps: int = 2, max_steps: int = 10 ** 6):
+def cpu_oracle_rate(cfg, U0, budget_s: float, nthreads: int, min_steps: int = 2, max_steps: int = 10 ** 6,
+                    warm: int = 1):
     """Time the oracle restatement on the host: zone-updates/s over a bounded
     number of steps of the same workload (steps until budget_s elapses)."""
     from oracle.oracle import Run
     from tests.helpers import oracle_params
     run = Run(oracle_params(cfg, nthreads=nthreads), U0)
-    run.run(1)  # first touch of the arrays
+    run.run(warm)  # first touch of the arrays (and the workload's first, heavier step)
     steps = 0
     t0 = time.perf_counter()
     while steps < max_steps:
@@ -270,6 +278,20 @@ def run_ensemble(args, world, rank, dist):
             ctx.advance(args.steps)
             s = ctx.stats()
             seq_ms += (s.ms_stage1 + s.ms_stage2 + s.ms_cool) * args.steps
+    # and in the plain FP64 form with the exact integrator (what the reference
+    # computes), one context after another
+    seq64_ms = 0.0
+    for cfg, U0 in members:
+        cfg64 = tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, "cooling": tlq.COOL_SUBCYCLE})
+        with tlq.Context(cfg64) as ctx:
+            U1 = U0.copy(order="F")
+            ctx.borders(U1, 1)
+            ctx.upload(U1)
+            ctx.advance(args.warmup)
+            ctx.enable_timing(True)
+            ctx.advance(args.steps)
+            s = ctx.stats()
+            seq64_ms += (s.ms_stage1 + s.ms_stage2 + s.ms_cool) * args.steps
     value = world * cells * args.steps / (ms / 1e3)
     line = {"metric": "zone-updates/s of a 48-member wind-bubble ensemble on 1 GB300 (batched persistent step)",
             "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -286,6 +308,10 @@ def run_ensemble(args, world, rank, dist):
             "sequential": {"value": cells * args.steps / (seq_ms / 1e3), "ms_per_step": seq_ms / args.steps,
                            "path": "each member alone, its own graph-replayed step, one after another"},
             "speedup_vs_sequential": (seq_ms / args.steps) / (ms / args.steps),
+            "sequential_fp64": {"value": cells * args.steps / (seq64_ms / 1e3), "ms_per_step": seq64_ms / args.steps,
+                                "path": "each member alone in the plain FP64 form with the exact cooling integrator, "
+                                        "one after another"},
+            "speedup_vs_sequential_fp64": (seq64_ms / args.steps) / (ms / args.steps),
             "gpu_launches": st.launches_per_step * args.steps, "clocks": clocks}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -428,6 +454,15 @@ def main():
         "bound": "fp64 pipe", "fp64_pipe_busy_ncu": 0.79,
         "hbm_achieved_gbs": bpz64["step"] * f64["value"] / 1e9,
         "hbm_frac": bpz64["step"] * f64["value"] / 1e9 / peak}
+    flops = FP64_FLOPS_PER_ZONE.get(args.workload)
+    if flops:
+        # oracle-counted arithmetic at the nominal FP64 rate; divisions and
+        # square roots take several FP64 instructions each, so the pipe
+        # occupancy above is the tighter measure
+        forms["fp64"]["roofline"].update({
+            "fp64_flops_per_zone": flops, "fp64_tflops_achieved": flops * f64["value"] / 1e12,
+            "fp64_tflops_peak_nominal": FP64_TFLOPS_NOMINAL,
+            "fp64_flop_frac_nominal": flops * f64["value"] / 1e12 / FP64_TFLOPS_NOMINAL})
     head = mix
     surrogate = None
     if cooling:
@@ -525,6 +560,10 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port",
                                 "sample": f"{steps} full steps of the same workload ({secs:.1f} s) on the oracle "
                                           f"restatement, OpenMP over {ncores} host threads"}
+        # the same restatement on one core (the reference itself is serial)
+        rate1, steps1, secs1 = cpu_oracle_rate(cfg, U0, 0.0, 1, min_steps=1)
+        line["cpu_baseline"]["serial"] = {"value": rate1, "unit": UNIT, "cores": 1,
+                                          "sample": f"{steps1} full step ({secs1:.1f} s) after one warm-up step"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     barrier(dist)

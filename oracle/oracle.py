@@ -278,8 +278,10 @@ class Oracle:
 class Run:
     """The main loop of source/mainHD.f90 on the restatement."""
 
-    def __init__(self, params: Params, U0: np.ndarray):
+    def __init__(self, params: Params, U0: np.ndarray, _lib=None):
         self.o = Oracle(params)
+        if _lib is not None:
+            self.o.L = _lib
         p = params
         self.arrays = {n: p.zeros() for n in ("U", "UP", "UPP", "UPrim", "F", "G", "H")}
         self.arrays["U"][...] = U0
@@ -316,3 +318,49 @@ class Run:
     @property
     def UPrim(self):
         return self.arrays["UPrim"]
+
+
+# ---------------------------------------------------------------------------
+# FP64 operation counts: the same source compiled with a counting double
+# (tlq_oracle_count.cpp); serial, and bit-identical to the oracle.
+# ---------------------------------------------------------------------------
+COUNT_LIB_PATH = os.path.join(HERE, "_build", "libtlq_oracle_count.so")
+_count_lib = None
+
+
+class _Flops(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("add", "mul", "div", "sqrt", "cmp", "trans")]
+
+
+def count_lib():
+    global _count_lib
+    if _count_lib is None:
+        srcs = [os.path.join(HERE, f) for f in ("tlq_oracle_count.cpp", "tlq_oracle.c", "tlq_oracle.h")]
+        if not os.path.exists(COUNT_LIB_PATH) or os.path.getmtime(COUNT_LIB_PATH) < max(map(os.path.getmtime, srcs)):
+            subprocess.run(["make", "-s", "-C", HERE, "count"], check=True)
+        L = C.CDLL(COUNT_LIB_PATH)
+        L.tlqo_init.argtypes = [C.POINTER(_Params), C.POINTER(_State)]
+        L.tlqo_run.restype = C.c_int
+        L.tlqo_run.argtypes = [C.POINTER(_Params), C.POINTER(_State), C.c_int, C.c_double]
+        L.tlqo_flops_reset.argtypes = []
+        L.tlqo_flops_get.argtypes = [C.POINTER(_Flops)]
+        _count_lib = L
+    return _count_lib
+
+
+def count_flops(params: Params, U0: np.ndarray, nsteps: int, tfin: float = float("inf"), skip: int = 0):
+    """Run skip uncounted steps, then nsteps counted steps of the main loop on
+    the counting build; return (counts per category over the counted steps,
+    the Run).  The set-up before the loop (borders, calc_prims, potential) is
+    not counted."""
+    L = count_lib()
+    r = Run(params, U0, _lib=L)  # tlqo_init ran on the counting build
+    if skip:
+        r.run(skip, tfin)
+    L.tlqo_flops_reset()
+    n = r.run(nsteps, tfin)
+    f = _Flops()
+    L.tlqo_flops_get(C.byref(f))
+    counts = {k: getattr(f, k) for k, _ in _Flops._fields_}
+    counts["steps"] = n
+    return counts, r

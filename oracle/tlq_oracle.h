@@ -104,9 +104,6 @@ void tlqo_init(const tlqo_params* p, tlqo_state* s);
  * Returns the number of iterations run. */
 int tlqo_run(const tlqo_params* p, tlqo_state* s, int nsteps, double tfin);
 
-/* Floating-point operation counts of the instrumented build (oracle_count.c). */
-typedef struct tlqo_flops { double add, mul, div, sqrt, cmp, trans; } tlqo_flops;
-
 #ifdef __cplusplus
 }
 #endif
