@@ -71,7 +71,19 @@ typedef struct tlq_config {
   double cool_mlp_tol;            /* TLQ_COOL_MLP: residual tolerance |T_pred - T_int|/T of an accepted
                                      cell, in (0, 1e-3] (default 1e-3; smaller trades speed for energy
                                      accuracy: more cells fall back) */
+  int self_gravity;               /* the reference's -DGRAV: MultiGrid (sources.f90:99-193) before each
+                                     stage, PHIT = PHIP + PHI (HLLC.f90:15-24); needs nx = ny = nz = 2^L,
+                                     2 <= nx <= 1024 */
+  int grav_bc;                    /* TLQ_GBC_*: the potential's values on the mesh faces */
 } tlq_config;
+
+/* Self-gravity boundary values.  ZERO: the reference's serial build, which
+ * never imposes any (its neighbour ranks stay 0, so the `left < 0` tests of
+ * sources.f90:112-130 fail) -- the face ghosts keep their first value, 0.
+ * MULTIPOLE: its MPI build on one rank (no neighbours): the multipole
+ * expansion to l = 4 (sources.f90:599-787) every 10 steps; not with
+ * periodic boundaries (that build exchanges the potential's ghosts there). */
+enum { TLQ_GBC_ZERO = 0, TLQ_GBC_MULTIPOLE = 1 };
 
 /* spherical_wind_type, source/winds.f90:5-16 (same fields, same order). */
 typedef struct tlq_wind {
@@ -324,6 +336,11 @@ int tlq_cooling(tlq_ctx* ctx, double* UPrim, double* U, double dt);
 int tlq_point_potential(tlq_ctx* ctx, double* phi);
 /* S_Solver, source/sources.f90:872-897. */
 int tlq_gravity_source(tlq_ctx* ctx, const double* UPrim, const double* phi, double* S);
+/* MultiGrid, source/sources.f90:99-193: one call on the density of U
+ * (reference layout), the potential phi(0:nx+1, 0:ny+1, 0:nz+1) in and out,
+ * it the step counter (multipole faces when it % 10 == 0); *cycles receives
+ * the V-cycles run (may be NULL).  Needs self_gravity in the configuration. */
+int tlq_multigrid(tlq_ctx* ctx, const double* U, double* phi, int it, int* cycles);
 
 /* ---- Allocation-free entry point (no counterpart in the reference) ------
  * time_step for callers that cannot allocate device memory: hosts whose GPU

@@ -25,6 +25,7 @@ BC_OUTFLOW, BC_REFLECTIVE, BC_PERIODIC, BC_INFLOW = 1, 2, 3, 4
 LIM_NONE, LIM_VANLEER, LIM_MINMOD, LIM_UMIST, LIM_WOODWARD, LIM_SUPERBEE = 1, 2, 3, 4, 5, 6
 SOLVER_HLLC, SOLVER_HLL = 0, 1
 COOL_NONE, COOL_REF, COOL_SUBCYCLE = 0, 1, 2
+GBC_ZERO, GBC_MULTIPOLE = 0, 1
 
 
 class _Wind(C.Structure):
@@ -50,12 +51,14 @@ class _Params(C.Structure):
         ("nmasses", C.c_int), ("masses", C.POINTER(C.c_double)),
         ("nthreads", C.c_int),
         ("nplanes", C.c_int), ("planes", C.POINTER(_PlaneWind)),
+        ("self_gravity", C.c_int), ("grav_bc", C.c_int),
     ]
 
 
 class _State(C.Structure):
     _fields_ = [(n, C.POINTER(C.c_double)) for n in ("U", "UP", "UPP", "UPrim", "F", "G", "H", "S", "PHI")] + [
-        ("t", C.c_double), ("dt", C.c_double), ("it", C.c_int)]
+        ("t", C.c_double), ("dt", C.c_double), ("it", C.c_int)] + [
+        (n, C.POINTER(C.c_double)) for n in ("PHIG", "PHIT", "MGW")]
 
 
 def build(force: bool = False) -> str:
@@ -93,6 +96,12 @@ def lib():
         L.tlqo_gravity_source.argtypes = [P, D, D, D]
         L.tlqo_cool_coef.restype = C.c_double
         L.tlqo_cool_coef.argtypes = [P, C.c_double]
+        L.tlqo_mg_levels.restype = C.c_int
+        L.tlqo_mg_levels.argtypes = [P]
+        L.tlqo_mg_work_len.restype = C.c_long
+        L.tlqo_mg_work_len.argtypes = [P]
+        L.tlqo_multigrid.restype = C.c_int
+        L.tlqo_multigrid.argtypes = [P, D, D, C.c_int, D]
         L.tlqo_init.argtypes = [P, C.POINTER(_State)]
         L.tlqo_run.restype = C.c_int
         L.tlqo_run.argtypes = [P, C.POINTER(_State), C.c_int, C.c_double]
@@ -152,6 +161,8 @@ class Params:
     masses: np.ndarray | None = None  # (n, 4): x, y, z, M
     nthreads: int = 0
     plane_winds: list = field(default_factory=list)  # objects with plane, rho, vel, temp, mu
+    self_gravity: int = 0  # MultiGrid self-gravity (the reference's -DGRAV); nx = ny = nz = 2^L
+    grav_bc: int = GBC_ZERO
 
     @property
     def shape(self):
@@ -180,7 +191,8 @@ class Params:
         """Build the C parameter struct; returns (struct, keepalive)."""
         s = _Params()
         keep = []
-        for n in ("nx", "ny", "nz", "limiter", "solver", "cooling", "cool_max_sub", "nthreads"):
+        for n in ("nx", "ny", "nz", "limiter", "solver", "cooling", "cool_max_sub", "nthreads", "self_gravity",
+                  "grav_bc"):
             setattr(s, n, int(getattr(self, n)))
         for n in ("xl", "xr", "yl", "yr", "zl", "zr", "gamma", "cfl", "eta", "mu0", "cooling_limit", "cool_sub_frac"):
             setattr(s, n, float(getattr(self, n)))
@@ -230,6 +242,13 @@ class Oracle:
 
     def time_step(self, W) -> float:
         return self.L.tlqo_time_step(self._pp, _ptr(W))
+
+    def multigrid(self, U, phi, it: int):
+        """One MultiGrid call (sources.f90:99-193) on the density of U; phi
+        ((n+2)^3, Fortran order) is updated in place.  Returns the V-cycles."""
+        work = np.zeros(self.L.tlqo_mg_work_len(self._pp), dtype=np.float64)
+        assert work.size > 0, "self-gravity needs nx = ny = nz = 2^L"
+        return self.L.tlqo_multigrid(self._pp, _ptr(U), _ptr(phi), int(it), _ptr(work))
 
     def fluxes(self, U, W, choice, F=None, G=None, H=None):
         F = self.p.zeros() if F is None else F
@@ -286,11 +305,16 @@ class Run:
         self.arrays = {n: p.zeros() for n in ("U", "UP", "UPP", "UPrim", "F", "G", "H")}
         self.arrays["U"][...] = U0
         grav = p.masses is not None and len(p.masses) > 0
-        if grav:
+        if grav or p.self_gravity:
             self.arrays["S"] = p.zeros()
+        if grav:
             self.arrays["PHI"] = np.zeros(p.phi_shape, dtype=np.float64, order="F")
+        if p.self_gravity:
+            self.arrays["PHIG"] = np.zeros(p.phi_shape, dtype=np.float64, order="F")
+            self.arrays["PHIT"] = np.zeros(p.phi_shape, dtype=np.float64, order="F")
+            self.arrays["MGW"] = np.zeros(self.o.L.tlqo_mg_work_len(self.o._pp), dtype=np.float64)
         st = _State()
-        for n in ("U", "UP", "UPP", "UPrim", "F", "G", "H", "S", "PHI"):
+        for n in ("U", "UP", "UPP", "UPrim", "F", "G", "H", "S", "PHI", "PHIG", "PHIT", "MGW"):
             setattr(st, n, _ptr(self.arrays.get(n)))
         st.t, st.dt, st.it = 0.0, 0.0, 0
         self.st = st
@@ -340,6 +364,8 @@ def count_lib():
             subprocess.run(["make", "-s", "-C", HERE, "count"], check=True)
         L = C.CDLL(COUNT_LIB_PATH)
         L.tlqo_init.argtypes = [C.POINTER(_Params), C.POINTER(_State)]
+        L.tlqo_mg_work_len.restype = C.c_long
+        L.tlqo_mg_work_len.argtypes = [C.POINTER(_Params)]
         L.tlqo_run.restype = C.c_int
         L.tlqo_run.argtypes = [C.POINTER(_Params), C.POINTER(_State), C.c_int, C.c_double]
         L.tlqo_flops_reset.argtypes = []

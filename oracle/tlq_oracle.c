@@ -593,6 +593,368 @@ void tlqo_gravity_source(const tlqo_params* p, const double* W, const double* ph
 }
 
 /* ---------------------------------------------------------------------------
+ * Self-gravity: MultiGrid (source/sources.f90:99-193) with its restriction,
+ * prolongation, residual and smoother (:196-485), and the multipole boundary
+ * values (Moments, phi_*boundaries, :599-787).  Meshes are cubes of
+ * N = 2^L cells (parameters.f90:22-25, lvlm = size = L), so the coarsest
+ * level holds one cell.  Level arrays are (n+2)^3, index (i, j, k) with
+ * i in 0..n+1, i fastest -- the layout of the potential phi(0:nx+1, ...).
+ *
+ * Boundary modes (the reference's two builds, see TLQO_GBC_*): the serial
+ * build never sets its neighbour ranks (globals left..back stay 0), so its
+ * `left < 0` tests fail and the level-0 ghost values are never imposed; the
+ * MPI build on one rank has no neighbours (all < 0) and imposes multipole
+ * values every 10 steps, with each moment the single rank's sum (the serial
+ * build leaves those sums unassigned, sources.f90:634-641, 667-669).  The
+ * two builds also fill the error ghosts of the coarse levels in different
+ * statement orders (:262-283 vs :285-290), which the corner values show.
+ * ------------------------------------------------------------------------- */
+static inline long MG(int n, int i, int j, int k) {
+  return (long)i + (long)(n + 2) * ((long)j + (long)(n + 2) * (long)k);
+}
+static inline long mg_cells(int n) { return (long)(n + 2) * (n + 2) * (long)(n + 2); }
+
+int tlqo_mg_levels(const tlqo_params* p) {
+  if (p->nx != p->ny || p->nx != p->nz || p->nx < 1 || (p->nx & (p->nx - 1))) return -1;
+  int L = 0;
+  while ((1 << L) < p->nx) ++L;
+  return L;
+}
+
+long tlqo_mg_work_len(const tlqo_params* p) {
+  const int L = tlqo_mg_levels(p);
+  if (L < 0) return 0;
+  long len = 0;
+  for (int l = 0; l <= L; ++l) len += 3 * mg_cells(p->nx >> l);
+  return len;
+}
+
+/* Error, Residue and ret of level l inside the work array. */
+static void mg_level(const tlqo_params* p, double* work, int l, double** err, double** res, double** ret) {
+  long off = 0;
+  for (int q = 0; q < l; ++q) off += 3 * mg_cells(p->nx >> q);
+  const long c = mg_cells(p->nx >> l);
+  *err = work + off;
+  *res = work + off + c;
+  *ret = work + off + 2 * c;
+}
+
+/* x**n for a run-time integer n as gfortran evaluates it (exponentiation by
+ * squaring, the binary method). */
+static double powi(double x, int n) {
+  unsigned m = n < 0 ? (unsigned)(-n) : (unsigned)n;
+  double y = (m % 2) ? x : 1.0;
+  while (m >>= 1) {
+    x = x * x;
+    if (m % 2) y = y * x;
+  }
+  return n < 0 ? 1.0 / y : y;
+}
+
+/* Legendre and aLegendre, sources.f90:9-96 (x**2 as x*x, x**3 as x*x*x,
+ * x**4 as (x*x)*(x*x); real exponents through pow). */
+static double legendre(double x, int l) {
+  const double x2 = x * x;
+  switch (l) {
+    case 0: return 1.0;
+    case 1: return x;
+    case 2: return 0.5 * (3.0 * x2 - 1.0);
+    case 3: return 0.5 * (5.0 * (x2 * x) - 3.0 * x);
+    default: return (1.0 / 8.0) * ((35.0 * (x2 * x2) - 30.0 * x2) + 3.0);
+  }
+}
+
+static double alegendre(double x, int l, int m) {
+  const double x2 = x * x, s = 1.0 - x2;
+  switch (l) {
+    case 0: return 1.0;
+    case 1: return m == 0 ? x : -pow(s, 1.0 / 2.0);
+    case 2:
+      if (m == 0) return 0.50 * (3.0 * x2 - 1.0);
+      if (m == 1) return -(3.0 * x * pow(s, 1.0 / 2.0));
+      return 3.0 * s;
+    case 3:
+      if (m == 0) return 0.50 * (5.0 * (x2 * x) - 3.0 * x);
+      if (m == 1) return (3.0 / 2.0) * (1.0 - 5.0 * x2) * pow(s, 1.0 / 2.0);
+      if (m == 2) return 15.0 * x * s;
+      return -(15.0 * pow(s, 3.0 / 2.0));
+    default:
+      if (m == 0) return (1.0 / 8.0) * ((35.0 * (x2 * x2) - 30.0 * x2) + 3.0);
+      if (m == 1) return -((5.0 / 2.0) * (7.0 * (x2 * x) - 3.0 * x) * pow(s, 1.0 / 2.0));
+      if (m == 2) return (15.0 / 2.0) * (7.0 * x2 - 1.0) * s;
+      if (m == 3) return -(105.0 * x * pow(s, 3.0 / 2.0));
+      return 105.0 * (s * s);
+  }
+}
+
+/* pangle, aangle, distance (sources.f90:558-596) of a cell centre. */
+static void sph_coords(const tlqo_params* p, int i, int j, int k, double* coth, double* fi, double* r) {
+  const double x = xcoord(p, i), y = ycoord(p, j), z = zcoord(p, k);
+  const double thet = acos(z / sqrt((x * x + y * y) + z * z));
+  double f = atan2(y, x);
+  if (f < 0) f = f + 2. * PI_REF;
+  *r = sqrt((x * x + y * y) + z * z);
+  *coth = cos(thet);
+  *fi = f;
+}
+
+/* Moments, sources.f90:599-681 (one rank: each moment the rank's sum). */
+static void mg_moments(const tlqo_params* p, const double* U, double c0[5], double cm[5][5], double sm[5][5]) {
+  const int n = p->nx;
+  const double ddx = DX(p), ddy = DY(p), ddz = DZ(p);
+  for (int l = 0; l <= 4; ++l) {
+    c0[l] = 0.0;
+    for (int m = 0; m <= 4; ++m) cm[l][m] = sm[l][m] = 0.0;
+  }
+  for (int l = 1; l <= 4; ++l) {
+    double c0mp = 0.0;
+    for (int m = 1; m <= l; ++m) {
+      double cmp = 0.0, smp = 0.0;
+      c0mp = 0.0;
+      const double c = 2.0 * tgamma((double)(l - m) + 1.0) / tgamma((double)(l + m) + 1.0);
+      for (int i = 1; i <= n; ++i)
+        for (int j = 1; j <= n; ++j)
+          for (int k = 1; k <= n; ++k) {
+            double coth, fi, r;
+            sph_coords(p, i, j, k, &coth, &fi, &r);
+            const double rho = U[IX(p, 0, i, j, k)];
+            const double rl = powi(r, l);
+            c0mp = c0mp + legendre(coth, l) * rl * rho * ddx * ddy * ddz;
+            cmp = cmp + alegendre(coth, l, m) * cos((double)m * fi) * rl * rho * ddx * ddy * ddz;
+            smp = smp + alegendre(coth, l, m) * sin((double)m * fi) * rl * rho * ddx * ddy * ddz;
+          }
+      cm[l][m] = c * cmp;
+      sm[l][m] = c * smp;
+    }
+    c0[l] = c0mp;
+  }
+  double c0mp = 0.0;
+  for (int i = 1; i <= n; ++i)
+    for (int j = 1; j <= n; ++j)
+      for (int k = 1; k <= n; ++k) {
+        double coth, fi, r;
+        sph_coords(p, i, j, k, &coth, &fi, &r);
+        const double rho = U[IX(p, 0, i, j, k)];
+        c0mp = c0mp + legendre(coth, 0) * powi(r, 0) * rho * ddx * ddy * ddz;
+      }
+  c0[0] = c0mp;
+}
+
+/* phi_x/y/zboundaries, sources.f90:683-787: the multipole expansion at the
+ * centre of one ghost cell. */
+static double multipole_phi(const tlqo_params* p, int i, int j, int k, const double c0[5], double cm[5][5],
+                            double sm[5][5]) {
+  double coth, fi, rb;
+  sph_coords(p, i, j, k, &coth, &fi, &rb);
+  double phi = 0.0;
+  phi = phi - c0[0] / rb;
+  for (int l = 1; l <= 4; ++l) {
+    phi = phi - c0[l] * legendre(coth, l) / powi(rb, l + 1);
+    for (int m = 1; m <= l; ++m)
+      phi = phi - 2.0 * (cm[l][m] * cos((double)m * fi) + sm[l][m] * sin((double)m * fi)) * alegendre(coth, l, m) /
+                      powi(rb, l + 1);
+  }
+  return GR * phi;
+}
+
+static void mg_boundaries(const tlqo_params* p, const double* U, double* phi) {
+  const int n = p->nx;
+  double c0[5], cm[5][5], sm[5][5];
+  mg_moments(p, U, c0, cm, sm);
+  const int b[2] = {0, n + 1};
+  for (int f = 0; f < 2; ++f) /* x faces: j, k */
+    for (int j = 1; j <= n; ++j)
+      for (int k = 1; k <= n; ++k) phi[MG(n, b[f], j, k)] = multipole_phi(p, b[f], j, k, c0, cm, sm);
+  for (int f = 0; f < 2; ++f) /* y faces: i, k */
+    for (int i = 1; i <= n; ++i)
+      for (int k = 1; k <= n; ++k) phi[MG(n, i, b[f], k)] = multipole_phi(p, i, b[f], k, c0, cm, sm);
+  for (int f = 0; f < 2; ++f) /* z faces: i, j */
+    for (int i = 1; i <= n; ++i)
+      for (int j = 1; j <= n; ++j) phi[MG(n, i, j, b[f])] = multipole_phi(p, i, j, b[f], c0, cm, sm);
+}
+
+/* The error's ghost values on a coarse level: var = -(first interior layer)
+ * per face, in each build's statement order (sources.f90:262-290). */
+static void mg_ghosts(int n, double* v, int bc) {
+#define FACE_X(I, SRC) for (int k = 0; k <= n + 1; ++k) for (int j = 0; j <= n + 1; ++j) v[MG(n, I, j, k)] = -v[MG(n, SRC, j, k)]
+#define FACE_Y(J, SRC) for (int k = 0; k <= n + 1; ++k) for (int i = 0; i <= n + 1; ++i) v[MG(n, i, J, k)] = -v[MG(n, i, SRC, k)]
+#define FACE_Z(K, SRC) for (int j = 0; j <= n + 1; ++j) for (int i = 0; i <= n + 1; ++i) v[MG(n, i, j, K)] = -v[MG(n, i, j, SRC)]
+  if (bc == TLQO_GBC_MULTIPOLE) { /* MPI build: x-, x+, y-, y+, z-, z+ */
+    FACE_X(0, 1); FACE_X(n + 1, n); FACE_Y(0, 1); FACE_Y(n + 1, n); FACE_Z(0, 1); FACE_Z(n + 1, n);
+  } else { /* serial build: x-, y-, z-, x+, y+, z+ */
+    FACE_X(0, 1); FACE_Y(0, 1); FACE_Z(0, 1); FACE_X(n + 1, n); FACE_Y(n + 1, n); FACE_Z(n + 1, n);
+  }
+#undef FACE_X
+#undef FACE_Y
+#undef FACE_Z
+}
+
+/* One smoother update (sources.f90:447-449 and :378-379, w = 1). */
+static inline double mg_update(int n, const double* v, const double* src, int i, int j, int k, double dxl) {
+  const double w = 1.0;
+  double a = v[MG(n, i + 1, j, k)] + v[MG(n, i - 1, j, k)];
+  a = a + v[MG(n, i, j + 1, k)];
+  a = a + v[MG(n, i, j - 1, k)];
+  a = a + v[MG(n, i, j, k + 1)];
+  a = a + v[MG(n, i, j, k - 1)];
+  a = a - src[MG(n, i, j, k)] * (dxl * dxl);
+  return ((1.0 / 6.0) * a) * w + (1.0 - w) * v[MG(n, i, j, k)];
+}
+
+/* poisson_solver, sources.f90:218-485 (Solve: Gauss-Seidel in i, j, k order
+ * until the summed change is <= 0.001; Relax: it-1 = 5 passes of the two
+ * half-sweeps).  Returns Dif. */
+static double mg_poisson(const tlqo_params* p, const double* src, double* v, int n, int solve, int level) {
+  const double dxl = (p->xr - p->xl) / (double)n;
+  double Dif = 0.0;
+  if (level > 0) mg_ghosts(n, v, p->grav_bc);
+  if (solve) {
+    Dif = 1000.0;
+    while (Dif > 0.001) {
+      double difp = 0.0;
+      for (int i = 1; i <= n; ++i)
+        for (int j = 1; j <= n; ++j)
+          for (int k = 1; k <= n; ++k) {
+            const double d1 = v[MG(n, i, j, k)];
+            v[MG(n, i, j, k)] = mg_update(n, v, src, i, j, k, dxl);
+            difp = difp + fabs(v[MG(n, i, j, k)] - d1);
+          }
+      Dif = difp;
+    }
+    return Dif;
+  }
+  for (int iter = 1; iter <= 5; ++iter) {
+    double difp = 0.0;
+    for (int half = 0; half < 2; ++half)
+      for (int i = 1; i <= n; ++i)
+        for (int j = 1; j <= n; ++j) {
+          /* the reference's test repeats one condition: i even and j odd */
+          const int s = (i % 2 == 0) && (j % 2 == 1);
+          int start = s ? 1 : 2;
+          if (half) start = s ? 2 : 1;
+          for (int k = start; k <= n; k += 2) {
+            const double d1 = v[MG(n, i, j, k)];
+            v[MG(n, i, j, k)] = mg_update(n, v, src, i, j, k, dxl);
+            difp = difp + fabs(v[MG(n, i, j, k)] - d1);
+          }
+        }
+    Dif = difp;
+  }
+  return Dif;
+}
+
+/* resid, sources.f90:196-216 (fine level of n cells). */
+static void mg_resid(int n, double dxl, const double* v, const double* src, double* res) {
+  for (long q = 0; q < mg_cells(n); ++q) res[q] = src[q] - 0.0;
+  for (int k = 1; k <= n; ++k)
+    for (int j = 1; j <= n; ++j)
+      for (int i = 1; i <= n; ++i) {
+        double g = v[MG(n, i - 1, j, k)] + v[MG(n, i + 1, j, k)];
+        g = g + v[MG(n, i, j - 1, k)];
+        g = g + v[MG(n, i, j + 1, k)];
+        g = g + v[MG(n, i, j, k - 1)];
+        g = g + v[MG(n, i, j, k + 1)];
+        g = (g - 6.0 * v[MG(n, i, j, k)]) / (dxl * dxl);
+        res[MG(n, i, j, k)] = src[MG(n, i, j, k)] - g;
+      }
+}
+
+/* restriction, sources.f90:118-137: coarse (nc cells) from fine (2 nc). */
+static void mg_restrict(int nc, const double* f, double* c) {
+  const int nf = 2 * nc;
+  for (int k = 1; k <= nc; ++k)
+    for (int j = 1; j <= nc; ++j)
+      for (int i = 1; i <= nc; ++i) {
+        const int i1 = 2 * i - 1, j1 = 2 * j - 1, k1 = 2 * k - 1;
+        double a = f[MG(nf, i1, j1, k1)] + f[MG(nf, i1 + 1, j1, k1)];
+        a = a + f[MG(nf, i1, j1 + 1, k1)];
+        a = a + f[MG(nf, i1, j1, k1 + 1)];
+        a = a + f[MG(nf, i1 + 1, j1 + 1, k1)];
+        a = a + f[MG(nf, i1 + 1, j1, k1 + 1)];
+        a = a + f[MG(nf, i1, j1 + 1, k1 + 1)];
+        a = a + f[MG(nf, i1 + 1, j1 + 1, k1 + 1)];
+        c[MG(nc, i, j, k)] = (1.0 / 8.0) * a;
+      }
+}
+
+/* One child of prolongation (sources.f90:139-194): the coarse cell (i,j,k)
+ * and its neighbours toward the child, di/dj/dk = -1 or +1. */
+static inline double mg_child(int nc, const double* c, int i, int j, int k, int di, int dj, int dk) {
+  double a = 27.0 * c[MG(nc, i, j, k)] + 9.0 * c[MG(nc, i + di, j, k)];
+  a = a + 9.0 * c[MG(nc, i, j + dj, k)];
+  a = a + 9.0 * c[MG(nc, i, j, k + dk)];
+  a = a + 3.0 * c[MG(nc, i + di, j + dj, k)];
+  a = a + 3.0 * c[MG(nc, i + di, j, k + dk)];
+  a = a + 3.0 * c[MG(nc, i, j + dj, k + dk)];
+  a = a + c[MG(nc, i + di, j + dj, k + dk)];
+  return (1.0 / 64.0) * a;
+}
+
+static void mg_prolong(int nc, const double* c, double* f) {
+  const int nf = 2 * nc;
+  for (long q = 0; q < mg_cells(nf); ++q) f[q] = 0.0;
+  for (int k = 1; k <= nc; ++k)
+    for (int j = 1; j <= nc; ++j)
+      for (int i = 1; i <= nc; ++i) {
+        const int i1 = 2 * i - 1, j1 = 2 * j - 1, k1 = 2 * k - 1;
+        for (int dk = 0; dk < 2; ++dk)
+          for (int dj = 0; dj < 2; ++dj)
+            for (int di = 0; di < 2; ++di)
+              f[MG(nf, i1 + di, j1 + dj, k1 + dk)] = mg_child(nc, c, i, j, k, di ? 1 : -1, dj ? 1 : -1, dk ? 1 : -1);
+      }
+}
+
+int tlqo_multigrid(const tlqo_params* p, const double* U, double* phi, int it, double* work) {
+  const int L = tlqo_mg_levels(p);
+  if (L < 0) return -1;
+  const int n = p->nx;
+  if (it % 10 == 0 && p->grav_bc == TLQO_GBC_MULTIPOLE) mg_boundaries(p, U, phi);
+  double *E0, *R0, *T0;
+  mg_level(p, work, 0, &E0, &R0, &T0);
+  for (int k = 0; k <= n + 1; ++k)
+    for (int j = 0; j <= n + 1; ++j)
+      for (int i = 0; i <= n + 1; ++i) R0[MG(n, i, j, k)] = 4.0 * PI_REF * GR * U[IX(p, 0, i, j, k)];
+  memcpy(E0, phi, (size_t)mg_cells(n) * sizeof(double));
+  double Dif = 1.e28;
+  int iter = 0;
+  while (Dif > 10.0 && iter < 31) {
+    iter = iter + 1;
+    for (int lv = 1; lv <= L; ++lv) {
+      double *E, *R, *T;
+      mg_level(p, work, lv, &E, &R, &T);
+      memset(E, 0, (size_t)mg_cells(n >> lv) * sizeof(double));
+    }
+    Dif = mg_poisson(p, R0, E0, n, 0, 0);
+    for (int level = 1; level <= L; ++level) {
+      const int nl = n >> level;
+      double *Ef, *Rf, *Tf, *E, *R, *T;
+      mg_level(p, work, level - 1, &Ef, &Rf, &Tf);
+      mg_level(p, work, level, &E, &R, &T);
+      mg_resid(2 * nl, (p->xr - p->xl) / (double)(2 * nl), Ef, Rf, Tf);
+      mg_restrict(nl, Tf, R);
+      Dif = mg_poisson(p, R, E, nl, level == L, level);
+    }
+    for (int level = L - 1; level >= 0; --level) {
+      const int nl = n >> level;
+      double *E, *R, *T, *Ec, *Rc, *Tc;
+      mg_level(p, work, level, &E, &R, &T);
+      mg_level(p, work, level + 1, &Ec, &Rc, &Tc);
+      mg_prolong(nl / 2, Ec, T);
+      for (long q = 0; q < mg_cells(nl); ++q) E[q] = E[q] + T[q];
+      Dif = mg_poisson(p, R, E, nl, 0, level);
+    }
+  }
+  memcpy(phi, E0, (size_t)mg_cells(n) * sizeof(double));
+  return iter;
+}
+
+/* PHIT = PHIP + PHI (HLLC.f90:22), over the whole (n+2)^3 array. */
+static void mg_total(const tlqo_params* p, const tlqo_state* s) {
+  const long c = tlqo_phi_len(p);
+  for (long q = 0; q < c; ++q) s->PHIT[q] = (s->PHI ? s->PHI[q] : 0.0) + s->PHIG[q];
+}
+
+/* ---------------------------------------------------------------------------
  * Main loop, source/mainHD.f90:38-44 and :61-100.
  * ------------------------------------------------------------------------- */
 void tlqo_init(const tlqo_params* p, tlqo_state* s) {
@@ -602,21 +964,38 @@ void tlqo_init(const tlqo_params* p, tlqo_state* s) {
     memset(s->PHI, 0, (size_t)tlqo_phi_len(p) * sizeof(double));
     tlqo_point_potential(p, s->PHI);
   }
+  if (p->self_gravity && s->PHIG && s->MGW) { /* mainHD.f90:50-52, it = 0, PHI starting at 0 */
+    memset(s->PHIG, 0, (size_t)tlqo_phi_len(p) * sizeof(double));
+    tlqo_multigrid(p, s->U, s->PHIG, s->it, s->MGW);
+  }
+}
+
+/* Godunov's gravity (HLLC.f90:15-24): with self-gravity MultiGrid on the
+ * density of U (both stages pass U as UU), PHIT = PHIP + PHI, S from PHIT;
+ * with point masses alone S from their potential. */
+static void gravity(const tlqo_params* p, tlqo_state* s) {
+  if (p->self_gravity) {
+    tlqo_multigrid(p, s->U, s->PHIG, s->it, s->MGW);
+    mg_total(p, s);
+    tlqo_gravity_source(p, s->UPrim, s->PHIT, s->S);
+  } else {
+    tlqo_gravity_source(p, s->UPrim, s->PHI, s->S);
+  }
 }
 
 int tlqo_run(const tlqo_params* p, tlqo_state* s, int nsteps, double tfin) {
-  const int grav = p->nmasses > 0 && s->PHI && s->S;
+  const int grav = ((p->nmasses > 0 && s->PHI) || (p->self_gravity && s->PHIG && s->PHIT && s->MGW)) && s->S;
   int n = 0;
   while (n < nsteps && s->t < tfin) {
     s->dt = tlqo_time_step(p, s->UPrim);
     tlqo_fluxes(p, s->U, s->F, s->G, s->H, s->UPrim, 1);
     double dth = s->dt / 2.0;
-    if (grav) tlqo_gravity_source(p, s->UPrim, s->PHI, s->S);
+    if (grav) gravity(p, s);
     tlqo_godunov(p, s->UPP, s->U, s->F, s->G, s->H, dth, grav ? s->S : NULL);
     tlqo_borders(p, s->UPP, 2);
     tlqo_calc_prims(p, s->UPrim, s->UPP);
     tlqo_fluxes(p, s->UPP, s->F, s->G, s->H, s->UPrim, 2);
-    if (grav) tlqo_gravity_source(p, s->UPrim, s->PHI, s->S);
+    if (grav) gravity(p, s);
     tlqo_godunov(p, s->UP, s->U, s->F, s->G, s->H, s->dt, grav ? s->S : NULL);
     tlqo_borders(p, s->UP, 1);
     tlqo_step(p, s->U, s->UP, s->UPP, &s->t, &s->it, s->dt);

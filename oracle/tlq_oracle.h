@@ -34,6 +34,12 @@ enum { TLQO_SOLVER_HLLC = 0, TLQO_SOLVER_HLL = 1 };
  * (source/cooling.f90:47-119); the sub-cycled integrator built on it. */
 enum { TLQO_COOL_NONE = 0, TLQO_COOL_REF = 1, TLQO_COOL_SUBCYCLE = 2 };
 
+/* Boundary values of the self-gravity potential on the mesh faces: the
+ * reference's serial build never imposes any (they stay 0), its MPI build on
+ * one rank imposes the multipole expansion (source/sources.f90:683-787)
+ * every 10 steps.  The two also fill coarse-level ghosts in different orders. */
+enum { TLQO_GBC_ZERO = 0, TLQO_GBC_MULTIPOLE = 1 };
+
 /* spherical_wind_type, source/winds.f90:5-16 (same field order). */
 typedef struct tlqo_wind {
   double xc, yc, zc, vx, vy, vz, radius, mdot, vinf, temp, mu;
@@ -68,6 +74,8 @@ typedef struct tlqo_params {
   int nthreads;                         /* OpenMP threads (<=0: runtime default) */
   int nplanes;                          /* plane winds, imposed after the spherical ones */
   const tlqo_plane_wind* planes;
+  int self_gravity;                     /* -DGRAV: MultiGrid in every Godunov (HLLC.f90:15-24) */
+  int grav_bc;                          /* TLQO_GBC_*; nx = ny = nz = 2^L required */
 } tlqo_params;
 
 /* Size in doubles of one conserved/primitive array (5 vars incl. ghosts). */
@@ -88,6 +96,13 @@ void tlqo_step(const tlqo_params* p, double* U, const double* UP, double* UPP,
                double* t, int* it, double dt);
 void tlqo_cooling(const tlqo_params* p, double* UPrim, double* U, double dt);
 void tlqo_point_potential(const tlqo_params* p, double* phi);
+/* Self-gravity (source/sources.f90:99-485): levels L with nx = 2^L (-1 when
+ * the mesh is not such a cube); the work array's length in doubles; one
+ * MultiGrid call on the density U(1, 0:nx+1, ...) of the conserved array U,
+ * phi (nx+2)^3 in and out, it the step counter.  Returns the V-cycles run. */
+int tlqo_mg_levels(const tlqo_params* p);
+long tlqo_mg_work_len(const tlqo_params* p);
+int tlqo_multigrid(const tlqo_params* p, const double* U, double* phi, int it, double* work);
 void tlqo_gravity_source(const tlqo_params* p, const double* UPrim, const double* phi, double* S);
 double tlqo_cool_coef(const tlqo_params* p, double temp);
 
@@ -96,6 +111,7 @@ typedef struct tlqo_state {
   double *U, *UP, *UPP, *UPrim, *F, *G, *H, *S, *PHI;  /* PHI, S: NULL without gravity */
   double t, dt;
   int it;
+  double *PHIG, *PHIT, *MGW;  /* self-gravity potential, PHIP + PHIG, MultiGrid work (else NULL) */
 } tlqo_state;
 
 /* mainHD.f90:38-44: borders(U,1), calc_prims(UPrim,U) (+ point potential). */

@@ -12,8 +12,9 @@
  *
  * Categories: add (+ and - of two values, including compound assignment),
  * mul, div, sqrt, cmp (<, >, <=, >=, ==, !=, which also carry the Fortran
- * MIN/MAX), trans (exp, log10, pow); fabs, copysign, ceil, negation and
- * conversions are not counted.
+ * MIN/MAX), trans (exp, log10, pow, and the self-gravity's acos, atan2, cos,
+ * sin, Gamma); fabs, copysign, ceil, negation and conversions are not
+ * counted.
  */
 #include <cmath>
 #include <cstdlib>
@@ -57,6 +58,11 @@ inline fd pow(fd a, fd b) { ++g_trans; return fd(std::pow(a.v, b.v)); }
 inline fd fabs(fd a) { return fd(std::fabs(a.v)); }
 inline fd copysign(fd a, fd b) { return fd(std::copysign(a.v, b.v)); }
 inline fd ceil(fd a) { return fd(std::ceil(a.v)); }
+inline fd acos(fd a) { ++g_trans; return fd(std::acos(a.v)); }
+inline fd atan2(fd a, fd b) { ++g_trans; return fd(std::atan2(a.v, b.v)); }
+inline fd cos(fd a) { ++g_trans; return fd(std::cos(a.v)); }
+inline fd sin(fd a) { ++g_trans; return fd(std::sin(a.v)); }
+inline fd tgamma(fd a) { ++g_trans; return fd(std::tgamma(a.v)); }
 
 // Every header the oracle includes is included above, before the macro, so
 // that only the oracle's own code sees it.

@@ -15,6 +15,8 @@ def oracle_params(cfg, nthreads: int = 0) -> Params:
                                                     "temp", "mu")}) for w in cfg.winds]
     p.masses = None if cfg.masses is None else np.asarray(cfg.masses, float)
     p.plane_winds = list(getattr(cfg, "plane_winds", []))
+    p.self_gravity = int(getattr(cfg, "self_gravity", 0))
+    p.grav_bc = int(getattr(cfg, "grav_bc", 0))
     return p
 
 

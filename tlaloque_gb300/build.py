@@ -34,6 +34,7 @@ UNITS = [
     ("tlq_surrogate.cu", ["--use_fast_math"]),
     ("tlq_batch.cu", ["--use_fast_math"]),
     ("tlq_output.cu", []),
+    ("tlq_gravity.cu", ["-fmad=false"]),
 ]
 
 

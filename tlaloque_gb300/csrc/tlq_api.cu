@@ -97,6 +97,20 @@ int validate(const tlq_config* c, std::string& why) {
   }
   for (int q = 0; q < 6; ++q)
     if (c->bc[q] == TLQ_BC_INFLOW) { why = "inflow boundaries are an empty stub in the reference"; return TLQ_ERR_CONFIG; }
+  if (c->self_gravity) {
+    if (mg_levels_of(*c) < 0 || c->nx > 1024) {
+      why = "self-gravity needs nx = ny = nz = 2^L, 2 <= nx <= 1024 (parameters.f90:22-25)";
+      return TLQ_ERR_CONFIG;
+    }
+    if (c->grav_bc != TLQ_GBC_ZERO && c->grav_bc != TLQ_GBC_MULTIPOLE) { why = "unknown grav_bc"; return TLQ_ERR_CONFIG; }
+    if (c->grav_bc == TLQ_GBC_MULTIPOLE)
+      for (int q = 0; q < 6; ++q)
+        if (c->bc[q] == TLQ_BC_PERIODIC) {
+          why = "multipole self-gravity boundaries with periodic hydro boundaries (the reference exchanges the "
+                "potential's ghosts there instead)";
+          return TLQ_ERR_CONFIG;
+        }
+  }
   return TLQ_OK;
 }
 
@@ -179,7 +193,7 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.L = ctx->L;
   a.clk = ctx->clk;
   a.zlen = ctx->zlen;
-  a.phi = ctx->phi;
+  a.phi = ctx->cfg.self_gravity ? ctx->phit : ctx->phi;
   a.lapf = ctx->lapf;
   // stage 1: U[par] -> UPP
   a.uold = ctx->U[par];
@@ -188,12 +202,16 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   const bool mixed = ctx->cfg.precision == TLQ_PREC_MIXED;
   a.use_p = (!mixed && ctx->cfg.cooling != TLQ_COOL_NONE) ? 1 : 0;
   if (timed) CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+  // self-gravity: MultiGrid on U's density before each Godunov (both take U
+  // as UU, HLLC.f90:15-24 with mainHD.f90:79,87)
+  if (ctx->cfg.self_gravity) CK(enqueue_multigrid_soa(ctx, ctx->U[par], ctx->stream));
   if (mixed)
     CK(launch_stage_mixed(1, ctx->tm_U[par], a, ctx->grid, ctx->stream));
   else
     CK(launch_stage(1, ctx->cfg.precision, ctx->tm_U[par], ctx->tm_P, a, ctx->grid, ctx->stream));
   if (timed) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
   // stage 2: UPP (+ U[par]) -> U[par^1]
+  if (ctx->cfg.self_gravity) CK(enqueue_multigrid_soa(ctx, ctx->U[par], ctx->stream));
   a.out = ctx->U[par ^ 1];
   a.pout = ctx->Pc;
   a.use_p = 0;
@@ -362,6 +380,10 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   cudaMemset(ctx->UPP, 0, soa);
   cudaMemset(ctx->Pc, 0, (size_t)L.plane * 8);
   cudaMemset(ctx->phi, 0, (size_t)L.plane * 8);
+  if (cfg->self_gravity) {
+    if (mg_alloc(ctx) != cudaSuccess) return bail(TLQ_ERR_NOMEM);
+    ctx->P.gravity = 1;
+  }
   if (cfg->precision == TLQ_PREC_MIXED) {
     if (cudaMalloc(&ctx->lapf, (size_t)L.plane * 5 * sizeof(float))) return bail(TLQ_ERR_NOMEM);
     cudaMemset(ctx->lapf, 0, (size_t)L.plane * 5 * sizeof(float));
@@ -409,6 +431,7 @@ int tlq_destroy(tlq_ctx* ctx) {
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
+  mg_free(ctx);
   cudaFree(ctx->mlp_params); cudaFree(ctx->mlp_image); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
   cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_qcount);
   cudaFree(ctx->clk); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
@@ -522,7 +545,7 @@ int tlq_set_point_masses(tlq_ctx* ctx, const double* xyzm, int n) {
   cudaFree(ctx->dmasses);
   ctx->dmasses = nullptr;
   ctx->nmasses = 0;
-  ctx->P.gravity = 0;
+  ctx->P.gravity = ctx->cfg.self_gravity ? 1 : 0;
   CK(cudaMemsetAsync(ctx->phi, 0, (size_t)ctx->L.plane * 8, ctx->stream));
   if (n > 0) {
     CK(cudaMalloc(&ctx->dmasses, 4 * n * sizeof(double)));
@@ -570,6 +593,11 @@ int tlq_upload(tlq_ctx* ctx, const double* U) {
   CK(cudaMemcpyAsync(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
   CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], carries_pressure(ctx) ? ctx->Pc : nullptr, ctx->clk,
                           init_blocks(ctx->P), ctx->stream));
+  if (ctx->cfg.self_gravity) {  // mainHD.f90:50-52: the first MultiGrid, PHI starting at 0
+    const long long m = ctx->cfg.nx + 2;
+    CK(cudaMemsetAsync(ctx->phig, 0, (size_t)(m * m * m) * sizeof(double), ctx->stream));
+    CK(enqueue_multigrid_soa(ctx, ctx->U[0], ctx->stream));
+  }
   ctx->cur = 0;
   if (ctx->it_base != ctx->it0) invalidate_graphs(ctx);  // captured launches read it_base
   ctx->it_base = ctx->it0;
@@ -833,6 +861,30 @@ int tlq_cooling(tlq_ctx* ctx, double* W, double* U, double dt) {
   CK(cudaMemcpyAsync(W, ctx->rb[0], b, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(U, ctx->rb[1], b, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return TLQ_OK;
+}
+
+int tlq_multigrid(tlq_ctx* ctx, const double* U, double* phi, int it, int* cycles) {
+  if (!ctx) return TLQ_ERR_ARG;
+  NEED(U); NEED(phi);
+  if (!ctx->cfg.self_gravity) return fail(ctx, TLQ_ERR_STATE, "tlq_multigrid needs self_gravity in the configuration");
+  int rc = ensure_routine_scratch(ctx);
+  if (rc) return rc;
+  const long long m = ctx->cfg.nx + 2;
+  const size_t pb = (size_t)(m * m * m) * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->rb[0], U, array_bytes(ctx->cfg), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->phig, phi, pb, cudaMemcpyHostToDevice, ctx->stream));
+  Clock c{};
+  c.it = it;
+  c.tfin = std::numeric_limits<double>::infinity();
+  CK(cudaMemcpyAsync(ctx->rclk, &c, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
+  CK(enqueue_multigrid_aos(ctx, ctx->rb[0], ctx->rclk, ctx->stream));
+  CK(cudaMemcpyAsync(phi, ctx->phig, pb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int st = 0;
+  rc = mg_cycles_and_status(ctx, cycles, &st);
+  if (rc) return rc;
+  if (st) return fail(ctx, TLQ_ERR_TIMEOUT, "coarsest-level solve did not converge");
   return TLQ_OK;
 }
 

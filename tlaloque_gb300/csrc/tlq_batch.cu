@@ -364,7 +364,7 @@ int tlq_batch_create(const tlq_config* cfgs, int n, tlq_batch** out) {
   if (!cfgs || n < 1 || !out) return TLQ_ERR_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i)
-    if (cfgs[i].precision != TLQ_PREC_MIXED) return TLQ_ERR_CONFIG;
+    if (cfgs[i].precision != TLQ_PREC_MIXED || cfgs[i].self_gravity) return TLQ_ERR_CONFIG;
   tlq_batch* b = new tlq_batch();
   auto bail = [&](int code) {
     tlq_batch_destroy(b);

@@ -22,6 +22,14 @@ struct tlq_ctx {
   double* UPP = nullptr;
   double* Pc = nullptr;   // carried pressure plane (cooling)
   double* phi = nullptr;  // point-mass potential plane
+  // self-gravity (tlq_gravity.cu): multigrid levels, control block, moment
+  // partials, the self-gravity potential ((nx+2)^3) and the stages' total
+  // potential plane PHIP + PHI (SoA plane layout, like phi)
+  void* mg_work = nullptr;
+  void* mg_ctl = nullptr;
+  void* mg_mom = nullptr;
+  double* phig = nullptr;
+  double* phit = nullptr;
   float* lapf = nullptr;  // mixed form: eta * Laplacian of U between the stages
   Clock* clk = nullptr;
   Clock* clk_host = nullptr;  // pinned mirror
@@ -88,3 +96,17 @@ int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* log
 // Z-chunk length of the stage grid (>= 8 planes, or nz): regrids and drops
 // the captured graphs (tlq_api.cu).
 int ctx_set_zlen(tlq_ctx* ctx, int zlen);
+
+// Self-gravity (tlq_gravity.cu).  mg_levels_of: L with nx = ny = nz = 2^L,
+// else -1.  enqueue_multigrid_soa: one MultiGrid call on the density of the
+// state U (SoA planes) with the context's clock, then the stages' potential
+// plane phit = phi + phig.  enqueue_multigrid_aos: the same on a reference-
+// layout array and the given clock, leaving phig only.
+namespace tlq {
+int mg_levels_of(const tlq_config& c);
+cudaError_t mg_alloc(tlq_ctx* ctx);
+void mg_free(tlq_ctx* ctx);
+cudaError_t enqueue_multigrid_soa(tlq_ctx* ctx, const double* U, cudaStream_t s);
+cudaError_t enqueue_multigrid_aos(tlq_ctx* ctx, const double* U, const Clock* clk, cudaStream_t s);
+int mg_cycles_and_status(tlq_ctx* ctx, int* cycles, int* status);
+}  // namespace tlq

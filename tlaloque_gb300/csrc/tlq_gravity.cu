@@ -1,0 +1,793 @@
+// tlq_gravity.cu -- self-gravity: the reference's MultiGrid
+// (source/sources.f90:99-485) and its multipole boundary values (:531-787)
+// on the GPU, run before each stage like Godunov's (HLLC.f90:15-24):
+// MultiGrid on the density of the step's U, PHIT = PHIP + PHI, and the
+// stage's source term from PHIT.
+//
+// The mesh is a cube of N = 2^L cells (the reference's lvlm = size); level l
+// holds n = N/2^l cells and three arrays (the error E, the residue R and the
+// scratch T of the reference's Error/Residue/ret), each (n+2)^3 doubles with
+// one ghost layer, index i + (n+2) (j + (n+2) k), i in 0..n+1 -- the layout
+// of the reference's level arrays and of phi(0:nx+1, ...).
+//
+// The smoother is the reference's, in its order.  Its two half-sweeps split
+// the cells by k parity and s(i, j) = [i even and j odd] (the reference's
+// parity test states that one condition twice), so within a half-sweep a
+// cell with s = 0 reads the new value of its x neighbour in rows of even j
+// and of its y neighbour in columns of odd i: a Gauss-Seidel order along i
+// and j.  A block walks a plane's anti-diagonals i + j = d in order, one
+// thread per i, and every other neighbour (east, north, the k planes, the
+// source) still holds its value from before the half-sweep, so those loads
+// run ahead of the sweep.  Planes are independent within a half-sweep, one
+// block each.  With the order kept and FP64 without contraction, every
+// level is bit-identical to a sequential restatement; only the stopping
+// test's sum |dphi| is summed in another order (it decides only whether the
+// next V-cycle runs).
+//
+// The V-cycles are a fixed sequence of launches (31, the reference's cap),
+// each launch reading a device flag that the cycle's first kernel sets from
+// the reference's test (Dif > 10 and fewer than 31 cycles): the whole solve
+// is stream-ordered with no host round trip, so a CUDA graph captures it.
+// Levels of at most 32 cells run inside one block (one launch per cycle).
+//
+// Built with -fmad=false (FP64 as the restatement evaluates it).
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <string>
+
+#include "tlq_ctx.h"
+
+namespace tlq {
+namespace {
+
+constexpr int MG_MAXL = 11;         // levels 0..10: meshes up to 1024^3
+constexpr int MG_COARSE_N = 32;     // levels of at most this many cells run in the one-block kernel
+constexpr int MG_CYCLES = 31;       // the reference's V-cycle cap (sources.f90:140)
+constexpr int MG_PF = 4;            // diagonal steps the smoother's loads run ahead
+constexpr int MG_MOM_THREADS = 256;
+constexpr int MG_MOM_BLOCKS = 152 * 2;
+constexpr int MG_SOLVE_LIMIT = 100000;  // coarsest-level Gauss-Seidel passes before giving up
+constexpr int MG_ST_SOLVE = 1;
+
+struct MgLevel {
+  int n;
+  double* E;
+  double* R;
+  double* T;
+  double dxl;  // (xr - xl) / n (sources.f90:232; x extent for every axis, as there)
+};
+
+struct MgCtl {
+  int run;     // this MultiGrid call runs (the step runs: t < tfin)
+  int active;  // the current V-cycle runs
+  int iter;    // V-cycles started
+  int status;  // MG_ST_* bits
+  double dif;  // the last smoother pass's summed |change| (the reference's Dif)
+  double c0[5], cm[5][5], sm[5][5];  // multipole moments (sources.f90:599-681)
+  double part[2 * 1024];             // per-plane partial sums of the last pass's |change|
+};
+
+__host__ __device__ __forceinline__ long long mgi(int n, int i, int j, int k) {
+  return (long long)i + (long long)(n + 2) * ((long long)j + (long long)(n + 2) * (long long)k);
+}
+
+// Where the density of the step's state is read (U(1, 0:nx+1, ...)).
+struct DensSoA {
+  const double* U;
+  Layout L;
+  __device__ double operator()(int i, int j, int k) const { return U[L.at(i, j, k)]; }
+};
+struct DensAoS {
+  const double* U;
+  Aos A;
+  __device__ double operator()(int i, int j, int k) const { return U[A.at(i, j, k)]; }
+};
+
+// ---------------------------------------------------------------------------
+// Multipole boundary values (sources.f90:9-96, 558-787)
+// ---------------------------------------------------------------------------
+__device__ double powi(double x, int n) {  // x**n, run-time n: the binary method, as gfortran
+  unsigned m = n < 0 ? (unsigned)(-n) : (unsigned)n;
+  double y = (m % 2) ? x : 1.0;
+  while (m >>= 1) {
+    x = x * x;
+    if (m % 2) y = y * x;
+  }
+  return n < 0 ? 1.0 / y : y;
+}
+
+__device__ double legendre(double x, int l) {
+  const double x2 = x * x;
+  switch (l) {
+    case 0: return 1.0;
+    case 1: return x;
+    case 2: return 0.5 * (3.0 * x2 - 1.0);
+    case 3: return 0.5 * (5.0 * (x2 * x) - 3.0 * x);
+    default: return (1.0 / 8.0) * ((35.0 * (x2 * x2) - 30.0 * x2) + 3.0);
+  }
+}
+
+__device__ double alegendre(double x, int l, int m) {
+  const double x2 = x * x, s = 1.0 - x2;
+  switch (l) {
+    case 0: return 1.0;
+    case 1: return m == 0 ? x : -pow(s, 0.5);
+    case 2:
+      if (m == 0) return 0.50 * (3.0 * x2 - 1.0);
+      if (m == 1) return -(3.0 * x * pow(s, 0.5));
+      return 3.0 * s;
+    case 3:
+      if (m == 0) return 0.50 * (5.0 * (x2 * x) - 3.0 * x);
+      if (m == 1) return 1.5 * (1.0 - 5.0 * x2) * pow(s, 0.5);
+      if (m == 2) return 15.0 * x * s;
+      return -(15.0 * pow(s, 1.5));
+    default:
+      if (m == 0) return (1.0 / 8.0) * ((35.0 * (x2 * x2) - 30.0 * x2) + 3.0);
+      if (m == 1) return -(2.5 * (7.0 * (x2 * x) - 3.0 * x) * pow(s, 0.5));
+      if (m == 2) return 7.5 * (7.0 * x2 - 1.0) * s;
+      if (m == 3) return -(105.0 * x * pow(s, 1.5));
+      return 105.0 * (s * s);
+  }
+}
+
+// pangle, aangle, distance of the centre of cell (i, j, k) (one rank).
+__device__ void sph_coords(const Params& p, int i, int j, int k, double& coth, double& fi, double& r) {
+  const double x = (p.xl + p.dx * (double)i) - p.dx / 2.0;
+  const double y = (p.yl + p.dy * (double)j) - p.dy / 2.0;
+  const double z = (p.zl + p.dz * (double)k) - p.dz / 2.0;
+  const double thet = acos(z / sqrt((x * x + y * y) + z * z));
+  double f = atan2(y, x);
+  if (f < 0) f = f + 2. * 3.14159265358979;
+  r = sqrt((x * x + y * y) + z * z);
+  coth = cos(thet);
+  fi = f;
+}
+
+// 25 sums per block: c0 l = 0..4, then cm and sm for l = 1..4, m = 1..l.
+template <class Dens>
+__global__ void __launch_bounds__(MG_MOM_THREADS) k_mg_moments(const MgCtl* c, const Clock* clk, Params p, Dens rho,
+                                                             double* part) {
+  __shared__ double red[MG_MOM_THREADS / 32][25];
+  if (!c->run || clk->it % 10 != 0) return;
+  const int n = p.nx;
+  const double vol = p.dx, vy = p.dy, vz = p.dz;
+  double acc[25];
+#pragma unroll
+  for (int q = 0; q < 25; ++q) acc[q] = 0.0;
+  const long long cells = (long long)n * n * n;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < cells;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(q % n), j = 1 + (int)((q / n) % n), k = 1 + (int)(q / ((long long)n * n));
+    double coth, fi, r;
+    sph_coords(p, i, j, k, coth, fi, r);
+    const double d = rho(i, j, k);
+    acc[0] += legendre(coth, 0) * powi(r, 0) * d * vol * vy * vz;
+    int slot = 5;
+#pragma unroll
+    for (int l = 1; l <= 4; ++l) {
+      const double rl = powi(r, l);
+      acc[l] += legendre(coth, l) * rl * d * vol * vy * vz;
+#pragma unroll
+      for (int m = 1; m <= l; ++m, ++slot) {
+        const double al = alegendre(coth, l, m);
+        acc[slot] += al * cos((double)m * fi) * rl * d * vol * vy * vz;
+        acc[slot + 10] += al * sin((double)m * fi) * rl * d * vol * vy * vz;
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 25; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 25) {
+    double v = 0.0;
+    for (int q = 0; q < MG_MOM_THREADS / 32; ++q) v += red[q][threadIdx.x];
+    part[blockIdx.x * 25 + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_mg_moments_final(MgCtl* c, const Clock* clk, const double* part, int nblocks) {
+  // slots 5..14 (cm) and 15..24 (sm): (l, m) = (1,1) (2,1) (2,2) (3,1) .. (4,4)
+  constexpr int LS[10] = {1, 2, 2, 3, 3, 3, 4, 4, 4, 4}, MS[10] = {1, 1, 2, 1, 2, 3, 1, 2, 3, 4};
+  if (!c->run || clk->it % 10 != 0) return;
+  const int q = threadIdx.x;
+  if (q >= 25) return;
+  double v = 0.0;
+  for (int b = 0; b < nblocks; ++b) v += part[b * 25 + q];
+  if (q < 5) {
+    c->c0[q] = v;
+    return;
+  }
+  const int r = q < 15 ? q - 5 : q - 15, l = LS[r], m = MS[r];
+  const double cf = 2.0 * tgamma((double)(l - m) + 1.0) / tgamma((double)(l + m) + 1.0);
+  if (q < 15)
+    c->cm[l][m] = cf * v;
+  else
+    c->sm[l][m] = cf * v;
+}
+
+// phi_x/y/zboundaries: the six faces' ghost cells (edges untouched).
+__global__ void k_mg_faces(const MgCtl* c, const Clock* clk, Params p, double* phi) {
+  if (!c->run || clk->it % 10 != 0) return;
+  const int n = p.nx;
+  const long long per = (long long)n * n;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < 6 * per;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(q / per);
+    const int a = 1 + (int)((q % per) / n), b = 1 + (int)(q % n);
+    const int bnd = (f & 1) ? n + 1 : 0;
+    int i, j, k;
+    if (f < 2) { i = bnd; j = a; k = b; }
+    else if (f < 4) { i = a; j = bnd; k = b; }
+    else { i = a; j = b; k = bnd; }
+    double coth, fi, rb;
+    sph_coords(p, i, j, k, coth, fi, rb);
+    double v = 0.0;
+    v = v - c->c0[0] / rb;
+    for (int l = 1; l <= 4; ++l) {
+      v = v - c->c0[l] * legendre(coth, l) / powi(rb, l + 1);
+      for (int m = 1; m <= l; ++m)
+        v = v - 2.0 * (c->cm[l][m] * cos((double)m * fi) + c->sm[l][m] * sin((double)m * fi)) * alegendre(coth, l, m) /
+                    powi(rb, l + 1);
+    }
+    phi[mgi(n, i, j, k)] = 6.67430e-8 * v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cycle control
+// ---------------------------------------------------------------------------
+__global__ void k_mg_begin(MgCtl* c, const Clock* clk) {
+  c->run = clk->t < clk->tfin;  // the loop test of mainHD.f90:61 (the step's)
+  c->active = 0;
+  c->iter = 0;
+  c->dif = 1.e28;
+}
+
+// Residue(0) = 4 pi G dens, Error(0) = phi (sources.f90:136-137).
+template <class Dens>
+__global__ void k_mg_init(const MgCtl* c, Dens rho, int n, const double* phi, double* E0, double* R0) {
+  if (!c->run) return;
+  const long long cells = (long long)(n + 2) * (n + 2) * (n + 2);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < cells;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % (n + 2)), j = (int)((q / (n + 2)) % (n + 2)), k = (int)(q / ((long long)(n + 2) * (n + 2)));
+    R0[q] = 4.0 * 3.14159265358979 * 6.67430e-8 * rho(i, j, k);
+    E0[q] = phi[q];
+  }
+}
+
+// The loop test of the V-cycles (sources.f90:140): another cycle while
+// Dif > 10 and fewer than 31 ran; the error of every coarse level restarts
+// at 0 (:146-148).
+// (Every block decides from the same inputs; k_mg_cycle_flag updates them
+// after this launch.)
+__global__ void k_mg_cycle_begin(const MgCtl* c, double* Ecoarse, long long ncoarse) {
+  __shared__ int go;
+  if (threadIdx.x == 0) go = c->run && c->dif > 10.0 && c->iter < MG_CYCLES;
+  __syncthreads();
+  if (!go) return;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ncoarse;
+       q += (long long)gridDim.x * blockDim.x)
+    Ecoarse[q] = 0.0;
+}
+
+// The flag and the count, after every block of k_mg_cycle_begin has read
+// the previous values.
+__global__ void k_mg_cycle_flag(MgCtl* c) {
+  const int go = c->run && c->dif > 10.0 && c->iter < MG_CYCLES;
+  c->active = go;
+  if (go) c->iter = c->iter + 1;
+}
+
+__global__ void k_mg_cycle_end(MgCtl* c, int nparts) {
+  if (!c->active) return;
+  double v = 0.0;
+  for (int q = 0; q < nparts; ++q) v += c->part[q];
+  c->dif = v;
+}
+
+// phi = Error(0) (sources.f90:189); PHIT = PHIP + PHI into the stage's
+// potential plane (HLLC.f90:22).
+__global__ void k_mg_end(const MgCtl* c, int n, const double* E0, double* phig, const double* phip, double* phit,
+                         Layout L) {
+  if (!c->run) return;
+  const long long cells = (long long)(n + 2) * (n + 2) * (n + 2);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < cells;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % (n + 2)), j = (int)((q / (n + 2)) % (n + 2)), k = (int)(q / ((long long)(n + 2) * (n + 2)));
+    const double v = E0[q];
+    phig[q] = v;
+    if (phit) {
+      const long long o = L.at(i, j, k);
+      phit[o] = phip[o] + v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Level operators
+// ---------------------------------------------------------------------------
+// One smoother update (sources.f90:378-379, 447-449; w = 1).
+__device__ __forceinline__ double mg_new(double east, double west, double north, double south, double up, double down,
+                                         double src, double dxl2, double old) {
+  const double w = 1.0;
+  double a = east + west;
+  a = a + north;
+  a = a + south;
+  a = a + up;
+  a = a + down;
+  a = a - src * dxl2;
+  return ((1.0 / 6.0) * a) * w + (1.0 - w) * old;
+}
+
+// Cells (i even, j odd) of plane k: none of them shares a face with another,
+// so they update in any order (threads t of nt share them).
+__device__ double mg_parallel_plane(const MgLevel& lv, int k, int t, int nt) {
+  const int n = lv.n, h = n / 2;
+  const double dxl2 = lv.dxl * lv.dxl;
+  double acc = 0.0;
+  for (int q = t; q < h * h; q += nt) {
+    const int i = 2 * (q % h + 1), j = 2 * (q / h) + 1;
+    const long long o = mgi(n, i, j, k), s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
+    const double old = lv.E[o];
+    const double v = mg_new(lv.E[o + 1], lv.E[o - 1], lv.E[o + s1], lv.E[o - s1], lv.E[o + s2], lv.E[o - s2], lv.R[o],
+                            dxl2, old);
+    lv.E[o] = v;
+    acc += fabs(v - old);
+  }
+  return acc;
+}
+
+// The other cells of plane k (s = 0) in the reference's order: anti-diagonal
+// d = i + j after anti-diagonal, thread i of the plane's group.  West (i-1,
+// j) and south (i, j-1) lie on diagonal d-1: south is this thread's own last
+// value, west its neighbour's (pub, double-buffered by diagonal parity).
+// The loads of the other neighbours run MG_PF diagonals ahead.  Every thread
+// of the block calls this with the same n (uniform barriers); i > n idles.
+__device__ double mg_wave_plane(const MgLevel& lv, int k, int i, double* pub) {
+  const int n = lv.n;
+  const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
+  double* __restrict__ E = lv.E;
+  const double* __restrict__ R = lv.R;
+  const double dxl2 = lv.dxl * lv.dxl;
+  double rc[MG_PF], re[MG_PF], rn[MG_PF], ru[MG_PF], rd[MG_PF], rs[MG_PF];
+  const bool col = i >= 1 && i <= n;
+#pragma unroll
+  for (int q = 0; q < MG_PF; ++q) {
+    const int j = 2 + q - i;
+    if (col && j >= 1 && j <= n) {
+      const long long o = mgi(n, i, j, k);
+      rc[q] = E[o]; re[q] = E[o + 1]; rn[q] = E[o + s1]; ru[q] = E[o + s2]; rd[q] = E[o - s2]; rs[q] = R[o];
+    }
+  }
+  double prev = 0.0, acc = 0.0;
+  for (int d0 = 2; d0 <= 2 * n; d0 += MG_PF) {
+#pragma unroll
+    for (int q = 0; q < MG_PF; ++q) {
+      const int d = d0 + q;
+      if (d <= 2 * n) {
+        const int j = d - i;
+        if (col && j >= 1 && j <= n) {
+          const long long o = mgi(n, i, j, k);
+          const double west = i == 1 ? E[o - 1] : pub[((d - 1) & 1) * (n + 1) + i - 1];
+          const double south = j == 1 ? E[o - s1] : prev;
+          const double old = rc[q];
+          double cur = old;
+          if ((i & 1) || !(j & 1)) {  // s = 0: this half-sweep's cell
+            cur = mg_new(re[q], west, rn[q], south, ru[q], rd[q], rs[q], dxl2, old);
+            E[o] = cur;
+            acc += fabs(cur - old);
+          }
+          pub[(d & 1) * (n + 1) + i] = cur;
+          prev = cur;
+        }
+        const int jn = d + MG_PF - i;  // this slot's next diagonal
+        if (col && jn >= 1 && jn <= n) {
+          const long long o = mgi(n, i, jn, k);
+          rc[q] = E[o]; re[q] = E[o + 1]; rn[q] = E[o + s1]; ru[q] = E[o + s2]; rd[q] = E[o - s2]; rs[q] = R[o];
+        }
+        __syncthreads();
+      }
+    }
+  }
+  return acc;
+}
+
+// Sum over the block (blockDim.x a multiple of 32), in a fixed order; the
+// result in thread 0.
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+  return s;
+}
+
+// One half-sweep of a level above MG_COARSE_N cells: block b = plane k = b+1
+// (n threads).  half 0: cells with k parity = s; half 1: the others
+// (sources.f90:438-452 and :456-468).  part: where the plane's summed
+// |change| goes (null: not needed).
+template <int NT>
+__global__ void __launch_bounds__(NT) k_mg_half(const MgCtl* c, MgLevel lv, int half, double* part) {
+  __shared__ double pub[2 * 1025];
+  __shared__ double red[32];
+  if (!c->active) return;
+  const int k = blockIdx.x + 1;
+  const int sk = (k & 1) ^ half;  // the s of this half-sweep's cells in plane k
+  double acc;
+  if (sk)
+    acc = mg_parallel_plane(lv, k, threadIdx.x, blockDim.x);
+  else
+    acc = mg_wave_plane(lv, k, threadIdx.x + 1, pub);
+  if (part) {
+    const double s = block_sum(acc, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+  }
+}
+
+// The error's ghosts on a coarse level: -(first interior layer) per face in
+// each build's statement order (sources.f90:262-283, 285-290); one block.
+__device__ void mg_ghosts(const MgLevel& lv, int bc_multipole) {
+  const int n = lv.n, m = n + 2;
+  double* E = lv.E;
+  const int order_mpi[6] = {0, 1, 2, 3, 4, 5};  // x-, x+, y-, y+, z-, z+
+  const int order_ser[6] = {0, 2, 4, 1, 3, 5};  // x-, y-, z-, x+, y+, z+
+  for (int s = 0; s < 6; ++s) {
+    const int f = bc_multipole ? order_mpi[s] : order_ser[s];
+    const int axis = f >> 1, hi = f & 1;
+    const int g = hi ? n + 1 : 0, src = hi ? n : 1;
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+      const int a = q % m, b = q / m;
+      long long to, from;
+      if (axis == 0) { to = mgi(n, g, a, b); from = mgi(n, src, a, b); }
+      else if (axis == 1) { to = mgi(n, a, g, b); from = mgi(n, a, src, b); }
+      else { to = mgi(n, a, b, g); from = mgi(n, a, b, src); }
+      E[to] = -E[from];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_mg_ghosts(const MgCtl* c, MgLevel lv, int bc_multipole) {
+  if (!c->active) return;
+  mg_ghosts(lv, bc_multipole);
+}
+
+// resid on the fine level (sources.f90:196-216) and restriction onto the
+// coarse one (:118-137), fused: each coarse cell forms its 8 children's
+// residuals.  (The reference's ret array of the fine level is not kept: it
+// is overwritten before anything reads it.)
+__device__ __forceinline__ double mg_resid_cell(const MgLevel& f, int i, int j, int k) {
+  const int n = f.n;
+  const long long o = mgi(n, i, j, k), s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
+  const double* E = f.E;
+  double g = E[o - 1] + E[o + 1];
+  g = g + E[o - s1];
+  g = g + E[o + s1];
+  g = g + E[o - s2];
+  g = g + E[o + s2];
+  g = (g - 6.0 * E[o]) / (f.dxl * f.dxl);
+  return f.R[o] - g;
+}
+
+__device__ void mg_resid_restrict(const MgLevel& f, const MgLevel& c, long long t, long long nt) {
+  const int nc = c.n;
+  for (long long q = t; q < (long long)nc * nc * nc; q += nt) {
+    const int i = 1 + (int)(q % nc), j = 1 + (int)((q / nc) % nc), k = 1 + (int)(q / ((long long)nc * nc));
+    const int i1 = 2 * i - 1, j1 = 2 * j - 1, k1 = 2 * k - 1;
+    double a = mg_resid_cell(f, i1, j1, k1) + mg_resid_cell(f, i1 + 1, j1, k1);
+    a = a + mg_resid_cell(f, i1, j1 + 1, k1);
+    a = a + mg_resid_cell(f, i1, j1, k1 + 1);
+    a = a + mg_resid_cell(f, i1 + 1, j1 + 1, k1);
+    a = a + mg_resid_cell(f, i1 + 1, j1, k1 + 1);
+    a = a + mg_resid_cell(f, i1, j1 + 1, k1 + 1);
+    a = a + mg_resid_cell(f, i1 + 1, j1 + 1, k1 + 1);
+    c.R[mgi(nc, i, j, k)] = (1.0 / 8.0) * a;
+  }
+}
+
+__global__ void k_mg_resid_restrict(const MgCtl* c, MgLevel f, MgLevel co) {
+  if (!c->active) return;
+  mg_resid_restrict(f, co, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// prolongation (sources.f90:139-194) onto a zeroed ret, then
+// Error = Error + ret over the whole array (:181): interior cells add their
+// trilinear child value, ghosts add 0.
+__device__ void mg_prolong_add(const MgLevel& c, const MgLevel& f, long long t, long long nt) {
+  const int nf = f.n, nc = c.n, m = nf + 2;
+  const long long s1 = nc + 2, s2 = (long long)(nc + 2) * (nc + 2);
+  for (long long q = t; q < (long long)m * m * m; q += nt) {
+    const int fi = (int)(q % m), fj = (int)((q / m) % m), fk = (int)(q / ((long long)m * m));
+    double r = 0.0;
+    if (fi >= 1 && fi <= nf && fj >= 1 && fj <= nf && fk >= 1 && fk <= nf) {
+      const int i = (fi + 1) >> 1, j = (fj + 1) >> 1, k = (fk + 1) >> 1;
+      const long long di = (fi & 1) ? -1 : 1, dj = (fj & 1) ? -s1 : s1, dk = (fk & 1) ? -s2 : s2;
+      const long long o = mgi(nc, i, j, k);
+      const double* V = c.E;
+      double a = 27.0 * V[o] + 9.0 * V[o + di];
+      a = a + 9.0 * V[o + dj];
+      a = a + 9.0 * V[o + dk];
+      a = a + 3.0 * V[o + di + dj];
+      a = a + 3.0 * V[o + di + dk];
+      a = a + 3.0 * V[o + dj + dk];
+      a = a + V[o + di + dj + dk];
+      r = (1.0 / 64.0) * a;
+    }
+    f.E[q] = f.E[q] + r;
+  }
+}
+
+__global__ void k_mg_prolong_add(const MgCtl* c, MgLevel co, MgLevel f) {
+  if (!c->active) return;
+  mg_prolong_add(co, f, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// Levels lc..L (n <= MG_COARSE_N) of one V-cycle in one block
+// ---------------------------------------------------------------------------
+constexpr int MG_CT = 512;  // threads: (n/2 planes) x n <= 16 x 32
+
+// Relax (5 passes of 2 half-sweeps) on a level of at most 32 cells; the
+// wave planes of a half-sweep advance together, thread t <-> (plane slot
+// t / n, i = t % n + 1), the parallel planes' cells first (no plane of one
+// kind reads a cell of the other kind that the half-sweep writes).
+__device__ double mg_relax_block(const MgLevel& lv, double* pub, double* red, bool track) {
+  const int n = lv.n;
+  double last = 0.0;
+  for (int pass = 0; pass < 5; ++pass) {
+    double acc = 0.0;
+    for (int half = 0; half < 2; ++half) {
+      // parallel planes: (k & 1) != half
+      for (int k = 1; k <= n; ++k)
+        if (((k & 1) ^ half) == 1 && n >= 2) acc += mg_parallel_plane(lv, k, threadIdx.x, blockDim.x);
+      const int ps = threadIdx.x / n, i = threadIdx.x % n + 1;
+      const int k = 2 * ps + (half ? 1 : 2);  // (k & 1) == half
+      const bool mine = ps < n / 2 && k <= n;
+      // every thread runs the diagonal loop (uniform barriers); others idle
+      const double a = mg_wave_plane(lv, mine ? k : 1, mine ? i : n + 1, pub + (mine ? ps : 0) * 2 * (n + 1));
+      acc += mine ? a : 0.0;
+      __syncthreads();
+    }
+    if (track && pass == 4) last = block_sum(acc, red);
+  }
+  return last;  // (thread 0)
+}
+
+// Gauss-Seidel in i, j, k order until the summed change is <= 0.001
+// (sources.f90:337-396); one thread, the coarsest level is tiny.
+__device__ void mg_solve_block(const MgLevel& lv, MgCtl* c) {
+  if (threadIdx.x == 0) {
+    const int n = lv.n;
+    const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
+    const double dxl2 = lv.dxl * lv.dxl;
+    double Dif = 1000.0;
+    int passes = 0;
+    while (Dif > 0.001) {
+      if (++passes > MG_SOLVE_LIMIT) {
+        atomicOr(&c->status, MG_ST_SOLVE);
+        break;
+      }
+      double difp = 0.0;
+      for (int i = 1; i <= n; ++i)
+        for (int j = 1; j <= n; ++j)
+          for (int k = 1; k <= n; ++k) {
+            const long long o = mgi(n, i, j, k);
+            const double old = lv.E[o];
+            const double v = mg_new(lv.E[o + 1], lv.E[o - 1], lv.E[o + s1], lv.E[o - s1], lv.E[o + s2], lv.E[o - s2],
+                                    lv.R[o], dxl2, old);
+            lv.E[o] = v;
+            difp = difp + fabs(v - old);
+          }
+      Dif = difp;
+    }
+  }
+  __syncthreads();
+}
+
+struct MgLevels {
+  MgLevel lv[MG_MAXL];
+};
+
+// The part of one V-cycle on levels lc..L: down (relax lc; then per level
+// residual + restriction, ghosts, relax or, on L, solve) and up (per level
+// prolongation + add, ghosts, relax).  With lc = 0 it is the whole cycle
+// and also forms Dif.
+__global__ void __launch_bounds__(MG_CT) k_mg_coarse(MgCtl* c, MgLevels levels, int lc, int L, int bc_multipole) {
+  __shared__ double pub[16 * 2 * 33];
+  __shared__ double red[32];
+  if (!c->active) return;
+  const long long t = threadIdx.x, nt = blockDim.x;
+  // down
+  if (lc > 0) mg_ghosts(levels.lv[lc], bc_multipole);
+  if (lc == L)
+    mg_solve_block(levels.lv[L], c);
+  else
+    mg_relax_block(levels.lv[lc], pub, red, false);
+  for (int l = lc + 1; l <= L; ++l) {
+    mg_resid_restrict(levels.lv[l - 1], levels.lv[l], t, nt);
+    __syncthreads();
+    mg_ghosts(levels.lv[l], bc_multipole);
+    if (l == L)
+      mg_solve_block(levels.lv[l], c);
+    else
+      mg_relax_block(levels.lv[l], pub, red, false);
+  }
+  // up
+  for (int l = L - 1; l >= lc; --l) {
+    mg_prolong_add(levels.lv[l + 1], levels.lv[l], t, nt);
+    __syncthreads();
+    if (l > 0) mg_ghosts(levels.lv[l], bc_multipole);
+    const double d = mg_relax_block(levels.lv[l], pub, red, l == 0);
+    if (l == 0 && threadIdx.x == 0) c->part[0] = d;
+  }
+}
+
+// One half-sweep launch: a block per plane, a thread per i (n of them).
+void launch_half(const MgCtl* c, const MgLevel& lv, int half, double* part, cudaStream_t s) {
+  if (lv.n <= 256)
+    k_mg_half<256><<<lv.n, lv.n, 0, s>>>(c, lv, half, part);
+  else
+    k_mg_half<1024><<<lv.n, lv.n, 0, s>>>(c, lv, half, part);
+}
+
+int grid_for(long long work, int threads) {
+  return (int)std::max<long long>(1, std::min<long long>((work + threads - 1) / threads, 152LL * 8));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+// The solver's buffers: E of every level (contiguous, so that the coarse
+// ones zero in one pass), then R, then T; the control block; the moments'
+// block partials.
+int mg_levels_of(const tlq_config& c) {
+  if (c.nx != c.ny || c.nx != c.nz || c.nx < 2 || (c.nx & (c.nx - 1))) return -1;
+  int L = 0;
+  while ((1 << L) < c.nx) ++L;
+  return L;
+}
+
+cudaError_t mg_alloc(tlq_ctx* ctx) {
+  const int L = mg_levels_of(ctx->cfg);
+  long long cells = 0;
+  for (int l = 0; l <= L; ++l) {
+    const long long m = (ctx->cfg.nx >> l) + 2;
+    cells += m * m * m;
+  }
+  cudaError_t e = cudaMalloc(&ctx->mg_work, (size_t)cells * 3 * sizeof(double));
+  if (e != cudaSuccess) return e;
+  e = cudaMalloc(&ctx->mg_ctl, sizeof(MgCtl));
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(ctx->mg_ctl, 0, sizeof(MgCtl));
+  if (e != cudaSuccess) return e;
+  e = cudaMalloc(&ctx->mg_mom, (size_t)MG_MOM_BLOCKS * 25 * sizeof(double));
+  if (e != cudaSuccess) return e;
+  const long long m0 = ctx->cfg.nx + 2;
+  e = cudaMalloc(&ctx->phig, (size_t)(m0 * m0 * m0) * sizeof(double));
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(ctx->phig, 0, (size_t)(m0 * m0 * m0) * sizeof(double));
+  if (e != cudaSuccess) return e;
+  e = cudaMalloc(&ctx->phit, (size_t)ctx->L.plane * sizeof(double));
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(ctx->phit, 0, (size_t)ctx->L.plane * sizeof(double));
+  if (e != cudaSuccess) return e;
+  return cudaMemset(ctx->mg_work, 0, (size_t)cells * 3 * sizeof(double));
+}
+
+void mg_free(tlq_ctx* ctx) {
+  cudaFree(ctx->mg_work); cudaFree(ctx->mg_ctl); cudaFree(ctx->mg_mom); cudaFree(ctx->phig); cudaFree(ctx->phit);
+  ctx->mg_work = nullptr; ctx->mg_ctl = nullptr; ctx->mg_mom = nullptr; ctx->phig = nullptr; ctx->phit = nullptr;
+}
+
+namespace {
+
+MgLevels mg_plan(const tlq_ctx* ctx, int L) {
+  MgLevels v{};
+  long long total = 0;
+  for (int l = 0; l <= L; ++l) {
+    const long long m = (ctx->cfg.nx >> l) + 2;
+    total += m * m * m;
+  }
+  double* base = static_cast<double*>(ctx->mg_work);
+  long long off = 0;
+  for (int l = 0; l <= L; ++l) {
+    const int n = ctx->cfg.nx >> l;
+    const long long m = n + 2;
+    v.lv[l].n = n;
+    v.lv[l].E = base + off;
+    v.lv[l].R = base + total + off;
+    v.lv[l].T = base + 2 * total + off;
+    v.lv[l].dxl = (ctx->cfg.xr - ctx->cfg.xl) / (double)n;
+    off += m * m * m;
+  }
+  return v;
+}
+
+template <class Dens>
+cudaError_t enqueue_mg(tlq_ctx* ctx, Dens rho, const Clock* clk, double* phit, cudaStream_t s) {
+  const int L = mg_levels_of(ctx->cfg);
+  const MgLevels v = mg_plan(ctx, L);
+  MgCtl* c = static_cast<MgCtl*>(ctx->mg_ctl);
+  const int n = ctx->cfg.nx;
+  const bool multipole = ctx->cfg.grav_bc == TLQ_GBC_MULTIPOLE;
+  int lc = 0;
+  while (lc < L && v.lv[lc].n > MG_COARSE_N) ++lc;
+  long long ncoarse = 0;  // E of levels 1..L, contiguous after E of level 0
+  for (int l = 1; l <= L; ++l) {
+    const long long m = v.lv[l].n + 2;
+    ncoarse += m * m * m;
+  }
+  const long long m0 = n + 2;
+  k_mg_begin<<<1, 1, 0, s>>>(c, clk);
+  if (multipole) {
+    k_mg_moments<<<MG_MOM_BLOCKS, MG_MOM_THREADS, 0, s>>>(c, clk, ctx->P, rho, static_cast<double*>(ctx->mg_mom));
+    k_mg_moments_final<<<1, 32, 0, s>>>(c, clk, static_cast<const double*>(ctx->mg_mom), MG_MOM_BLOCKS);
+    k_mg_faces<<<grid_for(6LL * n * n, 256), 256, 0, s>>>(c, clk, ctx->P, ctx->phig);
+  }
+  k_mg_init<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, rho, n, ctx->phig, v.lv[0].E, v.lv[0].R);
+  double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(c) + offsetof(MgCtl, part));
+  for (int cyc = 0; cyc < MG_CYCLES; ++cyc) {
+    k_mg_cycle_begin<<<grid_for(ncoarse, 256), 256, 0, s>>>(c, v.lv[0].E + m0 * m0 * m0, ncoarse);
+    k_mg_cycle_flag<<<1, 1, 0, s>>>(c);
+    if (lc == 0) {
+      k_mg_coarse<<<1, MG_CT, 0, s>>>(c, v, 0, L, multipole ? 1 : 0);
+      k_mg_cycle_end<<<1, 1, 0, s>>>(c, 1);
+      continue;
+    }
+    // down: level 0 .. lc-1 on the large kernels
+    for (int l = 0; l < lc; ++l) {
+      if (l > 0) k_mg_ghosts<<<1, 1024, 0, s>>>(c, v.lv[l], multipole ? 1 : 0);
+      for (int h = 0; h < 10; ++h) launch_half(c, v.lv[l], h & 1, nullptr, s);
+      k_mg_resid_restrict<<<grid_for((long long)v.lv[l + 1].n * v.lv[l + 1].n * v.lv[l + 1].n, 256), 256, 0, s>>>(
+          c, v.lv[l], v.lv[l + 1]);
+    }
+    k_mg_coarse<<<1, MG_CT, 0, s>>>(c, v, lc, L, multipole ? 1 : 0);
+    // up: level lc-1 .. 0
+    for (int l = lc - 1; l >= 0; --l) {
+      const long long mf = v.lv[l].n + 2;
+      k_mg_prolong_add<<<grid_for(mf * mf * mf, 256), 256, 0, s>>>(c, v.lv[l + 1], v.lv[l]);
+      if (l > 0) k_mg_ghosts<<<1, 1024, 0, s>>>(c, v.lv[l], multipole ? 1 : 0);
+      for (int h = 0; h < 10; ++h) {
+        // the last pass of the level-0 relax forms Dif (sources.f90:465-471)
+        double* pp = (l == 0 && h >= 8) ? part + (h - 8) * v.lv[0].n : nullptr;
+        launch_half(c, v.lv[l], h & 1, pp, s);
+      }
+    }
+    k_mg_cycle_end<<<1, 1, 0, s>>>(c, 2 * n);
+  }
+  k_mg_end<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, n, v.lv[0].E, ctx->phig, ctx->phi, phit, ctx->L);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t enqueue_multigrid_soa(tlq_ctx* ctx, const double* U, cudaStream_t s) {
+  return enqueue_mg(ctx, DensSoA{U, ctx->L}, ctx->clk, ctx->phit, s);
+}
+
+cudaError_t enqueue_multigrid_aos(tlq_ctx* ctx, const double* U, const Clock* clk, cudaStream_t s) {
+  return enqueue_mg(ctx, DensAoS{U, ctx->A}, clk, nullptr, s);
+}
+
+int mg_cycles_and_status(tlq_ctx* ctx, int* cycles, int* status) {
+  MgCtl h;
+  if (cudaMemcpy(&h, ctx->mg_ctl, sizeof(MgCtl), cudaMemcpyDeviceToHost) != cudaSuccess) return TLQ_ERR_CUDA;
+  if (cycles) *cycles = h.iter;
+  if (status) *status = h.status;
+  return TLQ_OK;
+}
+
+}  // namespace tlq

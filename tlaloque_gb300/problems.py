@@ -11,7 +11,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .tlq import (BC_OUTFLOW, BC_PERIODIC, COOL_SUBCYCLE, LIMITER_VANLEER, SOLVER_HLL, SOLVER_HLLC, Config, Wind)
+from .tlq import (BC_OUTFLOW, BC_PERIODIC, COOL_SUBCYCLE, GBC_MULTIPOLE, LIMITER_VANLEER, SOLVER_HLL, SOLVER_HLLC,
+                  Config, Wind)
 
 # source/constants.f90:6-15 (cgs)
 AMU = 1.660538782e-24
@@ -145,6 +146,33 @@ def wind_bubble(n: int = 256, cooling: int = COOL_SUBCYCLE, T_wind: float = 1.0e
     # the last bit of its pressure.  1e-9 above the edge gives the
     # exact-arithmetic decision (cooled) robustly in every precision.
     p = n_amb * KB * 1.0e4 * (1.0 + 1e-9)
+    return cfg, conserved(cfg, rho, 0.0, 0.0, 0.0, p)
+
+
+def gravitating_cloud(n: int = 128, grav_bc: int = GBC_MULTIPOLE, box_pc: float = 4.0, radius_pc: float = 1.0,
+                      n_cloud: float = 500.0, T_cloud: float = 50.0, contrast: float = 100.0, seed: int = 7,
+                      mass_msun: float = 0.0):
+    """A self-gravitating cloud (the reference's -DGRAV physics): a uniform
+    sphere of radius 1 pc, n = 500 cm^-3 (mu 1.3), T = 50 K, in a 100 times
+    thinner medium at the same pressure, in a (4 pc)^3 box of n^3 cells
+    (n = 2^L, as MultiGrid needs); a 1 % seeded density perturbation breaks
+    the symmetry; gamma 5/3, HLLC + van Leer, outflow, no cooling; optional
+    point mass at the centre.  Free-fall time ~2 Myr."""
+    L = box_pc * PC
+    mu = 1.3
+    cfg = Config(nx=n, ny=n, nz=n, xl=-L / 2, xr=L / 2, yl=-L / 2, yr=L / 2, zl=-L / 2, zr=L / 2, gamma=5.0 / 3.0,
+                 cfl=0.4, eta=0.5e-2, mu0=mu, limiter=LIMITER_VANLEER, solver=SOLVER_HLLC, bc=(BC_OUTFLOW,) * 6,
+                 self_gravity=1, grav_bc=grav_bc)
+    if mass_msun > 0.0:
+        cfg.masses = np.array([[0.0, 0.0, 0.0, mass_msun * MSUN]])
+    x, y, z = cell_centres(cfg)
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    r = np.sqrt(X * X + Y * Y + Z * Z)
+    rng = np.random.default_rng(seed)
+    rho_c = n_cloud * mu * AMU
+    inside = r < radius_pc * PC
+    rho = np.where(inside, rho_c * (1.0 + 0.01 * rng.standard_normal(r.shape)), rho_c / contrast)
+    p = n_cloud * KB * T_cloud  # pressure balance across the cloud's edge
     return cfg, conserved(cfg, rho, 0.0, 0.0, 0.0, p)
 
 

@@ -23,6 +23,7 @@ SOLVER_HLLC, SOLVER_HLL = 0, 1
 COOL_NONE, COOL_REF, COOL_SUBCYCLE, COOL_MLP = 0, 1, 2, 3
 MLP_NPARAM = 8641
 PREC_FP64, PREC_MIXED = 0, 1
+GBC_ZERO, GBC_MULTIPOLE = 0, 1
 OUT_DAT, OUT_VTK, OUT_BIN = 1, 2, 3
 
 # Every function the header declares (checked by the CPU test suite).
@@ -31,7 +32,8 @@ EXPORTS = (
     "tlq_set_point_masses", "tlq_upload", "tlq_download", "tlq_set_time", "tlq_get_time", "tlq_step", "tlq_advance",
     "tlq_run_until", "tlq_synchronize", "tlq_stats_get", "tlq_enable_timing", "tlq_last_error", "tlq_status_string",
     "tlq_conserved_sums", "tlq_calc_prims", "tlq_time_step", "tlq_fluxes", "tlq_godunov", "tlq_borders",
-    "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_time_step_noalloc",
+    "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_multigrid",
+    "tlq_time_step_noalloc",
     "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
     "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
     "tlq_set_tfin", "tlq_set_plane_winds", "tlq_output", "tlq_output_wait", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
@@ -56,6 +58,7 @@ class CConfig(C.Structure):
         ("limiter", C.c_int), ("solver", C.c_int), ("bc", C.c_int * 6), ("cooling", C.c_int),
         ("cool_max_sub", C.c_int), ("cool_sub_frac", C.c_double), ("precision", C.c_int), ("device", C.c_int),
         ("cool_mlp_tol", C.c_double),
+        ("self_gravity", C.c_int), ("grav_bc", C.c_int),
     ]
 
 
@@ -159,6 +162,7 @@ def load_library(path: str = LIB_PATH):
         "tlq_cooling": (I, [V, D, D, C.c_double]),
         "tlq_point_potential": (I, [V, D]),
         "tlq_gravity_source": (I, [V, D, D, D]),
+        "tlq_multigrid": (I, [V, D, D, I, C.POINTER(I)]),
         "tlq_time_step_noalloc": (I, [V, I, I, I, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, V, V]),
         "tlq_surrogate_opts_default": (None, [C.POINTER(CSurrogateOpts)]),
         "tlq_train_cooling_surrogate": (I, [V, C.POINTER(CSurrogateOpts), C.POINTER(CSurrogateReport)]),
@@ -236,6 +240,8 @@ class Config:
     cool_max_sub: int = 1
     cool_sub_frac: float = 0.1
     cool_mlp_tol: float = 1e-3
+    self_gravity: int = 0  # the reference's -DGRAV MultiGrid; nx = ny = nz = 2^L
+    grav_bc: int = GBC_ZERO  # GBC_ZERO (its serial build) or GBC_MULTIPOLE (its MPI build on one rank)
     precision: int = PREC_FP64
     device: int = 0
     # run-time tables (not part of tlq_config; set through their own calls)
@@ -274,7 +280,8 @@ class Config:
 
     def to_c(self) -> CConfig:
         c = CConfig()
-        for n in ("nx", "ny", "nz", "limiter", "solver", "cooling", "cool_max_sub", "precision", "device"):
+        for n in ("nx", "ny", "nz", "limiter", "solver", "cooling", "cool_max_sub", "precision", "device",
+                  "self_gravity", "grav_bc"):
             setattr(c, n, int(getattr(self, n)))
         for n in ("xl", "xr", "yl", "yr", "zl", "zr", "gamma", "cfl", "eta", "mu0", "cooling_limit", "cool_sub_frac",
                   "cool_mlp_tol"):
@@ -473,6 +480,13 @@ class Context:
         S = self.cfg.zeros()
         self._check(self.L.tlq_gravity_source(self.h, _dp(W), _dp(phi), _dp(S)), "gravity_source")
         return S
+
+    def multigrid(self, U, phi, it: int) -> int:
+        """One MultiGrid call on U's density; phi ((n+2)^3, Fortran order) is
+        updated in place.  Returns the V-cycles run."""
+        cyc = C.c_int(0)
+        self._check(self.L.tlq_multigrid(self.h, _dp(U), _dp(phi), int(it), C.byref(cyc)), "multigrid")
+        return cyc.value
 
     # -- learned cooling surrogate (TLQ_COOL_MLP) -----------------------------
     def train_cooling_surrogate(self, **opts) -> dict:
