@@ -1,7 +1,7 @@
 """Benchmark of tlaloque's hydrodynamic step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tlq|reference]
-                    [--workload wind256|wind128|sedov128|sod|clumpy384|ensemble48]
+                    [--workload wind256|wind128|sedov128|sod|clumpy384|cloud128|cloud256|ensemble48]
 
 A "step" is one full iteration of the reference's main loop
 (source/mainHD.f90:74-99: CFL dt, two HLLC stages, ghost fill, winds, point
@@ -88,6 +88,12 @@ def make_workload(name: str):
     elif name == "sod":
         cfg, U0 = problems.sod_tube()
         desc = "Sod shock tube 256x4x4, HLL, gamma 1.4, outflow"
+    elif name in ("cloud128", "cloud256"):
+        n = int(name[5:])
+        cfg, U0 = problems.gravitating_cloud(n)
+        desc = (f"self-gravitating cloud {n}^3 (the reference's -DGRAV MultiGrid before each stage, multipole faces "
+                "every 10 steps): (4 pc)^3, 1 pc sphere n = 500 cm^-3, T = 50 K, pressure-matched medium 100x "
+                "thinner, HLLC + van Leer, outflow")
     else:
         raise SystemExit(f"unknown workload {name}")
     return cfg, U0, desc
@@ -421,7 +427,7 @@ def main():
         sums = ctx.conserved_sums()
         ms_max = allmax(dist, ms)
         return {"ctx": ctx, "ms": ms_max, "value": world * cfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
-                "k2": st.ms_stage2, "kc": st.ms_cool, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
+                "k2": st.ms_stage2, "kc": st.ms_cool, "kg": st.ms_grav, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
                 "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks,
                 "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback,
                          st.cool_single - st0.cool_single), "zlen": zlen}
@@ -431,6 +437,8 @@ def main():
              "zlen": m["zlen"]}
         if m["kc"] > 0:
             d["ms_cool_passes"] = m["kc"]
+        if m["kg"] > 0:
+            d["ms_multigrid"] = m["kg"]  # both solves of a step (ms_stage1/2: the stage kernels alone)
         return d
 
     def accuracy(a, b):
@@ -508,6 +516,8 @@ def main():
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if peak_kind == "measured"
                 else peak_kind,
                 "traffic": None, "bytes_per_zone": bpz_m, "ms_stage1": k1, "ms_stage2": k2}
+    if mix["kg"] > 0:
+        roofline["ms_multigrid"] = mix["kg"]
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             tr = json.load(f).get(args.workload, {}).get("mixed_" + dom)

@@ -163,6 +163,8 @@ typedef struct tlq_stats {
   double ms_cool;          /* TLQ_COOL_MLP: average device time of the timed cooling passes */
   long long cool_single;   /* TLQ_COOL_MLP: cell-steps with tau <= cool_sub_frac, cooled by the exact
                               integrator's single exponential step (the network has nothing to gain) */
+  double ms_grav;          /* self-gravity: average device time of the timed steps' two MultiGrid solves
+                              (ms_stage1/ms_stage2 then time the stage kernels alone) */
 } tlq_stats;
 
 typedef struct tlq_ctx tlq_ctx;

@@ -32,9 +32,9 @@ def one_call(cfg, U0, phi0, it):
 
 @pytest.mark.parametrize("n", [8, 16, 32, 64, 128])
 def test_multigrid_bit_exact_zero_faces(gpu_lib, n):
-    """One call from phi = 0 and one from a perturbed potential: every level
-    through the one-block coarse kernel (n <= 32) or the per-plane
-    half-sweep kernels (n = 64, 128) bit for bit."""
+    """One call from phi = 0 and one from a perturbed potential, bit for bit:
+    n = 8 runs in the one-block coarse kernel, larger meshes relax their
+    levels of 16 cells and more in the pipelined cooperative kernel."""
     cfg, U0 = problems.gravitating_cloud(n, grav_bc=tlq.GBC_ZERO)
     g, gc, o, oc = one_call(cfg, U0, np.zeros(cfg.phi_shape, order="F"), 0)
     assert gc == oc and gc >= 2
@@ -45,6 +45,18 @@ def test_multigrid_bit_exact_zero_faces(gpu_lib, n):
     start[:, 0] = start[:, -1] = 0.0
     start[:, :, 0] = start[:, :, -1] = 0.0
     g, gc, o, oc = one_call(cfg, U0, start, 3)
+    assert gc == oc
+    np.testing.assert_array_equal(g, o)
+
+
+@pytest.mark.parametrize("n", [32, 128])
+def test_multigrid_per_half_sweep_path(gpu_lib, n, monkeypatch):
+    """The relax without the pipelined cooperative kernel (one launch per
+    half-sweep, the path for levels whose planes cannot all be resident)
+    gives the same bits too."""
+    monkeypatch.setenv("TLQ_MG_PIPELINE", "0")
+    cfg, U0 = problems.gravitating_cloud(n, grav_bc=tlq.GBC_ZERO)
+    g, gc, o, oc = one_call(cfg, U0, np.zeros(cfg.phi_shape, order="F"), 0)
     assert gc == oc
     np.testing.assert_array_equal(g, o)
 

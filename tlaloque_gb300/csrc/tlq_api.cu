@@ -138,11 +138,17 @@ void fill_params(tlq_ctx* c) {
   p.f_cooling_limit = (float)p.cooling_limit;
 }
 
+}  // namespace
+
 void invalidate_graphs(tlq_ctx* c) {
   c->gen += 1;
-  for (int q = 0; q < 2; ++q)
+  for (int q = 0; q < 2; ++q) {
     if (c->graph[q]) { cudaGraphExecDestroy(c->graph[q]); c->graph[q] = nullptr; }
+    if (c->tgraph[q]) { cudaGraphExecDestroy(c->tgraph[q]); c->tgraph[q] = nullptr; }
+  }
 }
+
+namespace {
 
 int ensure_routine_scratch(tlq_ctx* ctx) {
   if (ctx->rb[0]) return TLQ_OK;
@@ -186,7 +192,8 @@ int status_from_bits(int bits) {
   return TLQ_OK;
 }
 
-// Enqueue one step (stage 1 + stage 2) on buffer parity `par`.
+// Enqueue one step (stage 1 + stage 2) on buffer parity `par`; timed: with
+// the timing events, recorded as event nodes when the stream is captured.
 int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   StageArgs a{};
   a.p = ctx->P;
@@ -201,17 +208,19 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.pout = nullptr;
   const bool mixed = ctx->cfg.precision == TLQ_PREC_MIXED;
   a.use_p = (!mixed && ctx->cfg.cooling != TLQ_COOL_NONE) ? 1 : 0;
-  if (timed) CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+  if (timed) CK(cudaEventRecordWithFlags(ctx->ev[0], ctx->stream, cudaEventRecordExternal));
   // self-gravity: MultiGrid on U's density before each Godunov (both take U
   // as UU, HLLC.f90:15-24 with mainHD.f90:79,87)
   if (ctx->cfg.self_gravity) CK(enqueue_multigrid_soa(ctx, ctx->U[par], ctx->stream));
+  if (timed) CK(cudaEventRecordWithFlags(ctx->ev[4], ctx->stream, cudaEventRecordExternal));
   if (mixed)
     CK(launch_stage_mixed(1, ctx->tm_U[par], a, ctx->grid, ctx->stream));
   else
     CK(launch_stage(1, ctx->cfg.precision, ctx->tm_U[par], ctx->tm_P, a, ctx->grid, ctx->stream));
-  if (timed) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+  if (timed) CK(cudaEventRecordWithFlags(ctx->ev[1], ctx->stream, cudaEventRecordExternal));
   // stage 2: UPP (+ U[par]) -> U[par^1]
   if (ctx->cfg.self_gravity) CK(enqueue_multigrid_soa(ctx, ctx->U[par], ctx->stream));
+  if (timed) CK(cudaEventRecordWithFlags(ctx->ev[5], ctx->stream, cudaEventRecordExternal));
   a.out = ctx->U[par ^ 1];
   a.pout = ctx->Pc;
   a.use_p = 0;
@@ -221,23 +230,24 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
     CK(launch_stage_mixed(2, ctx->tm_UPP, a, ctx->grid, ctx->stream));
   else
     CK(launch_stage(2, ctx->cfg.precision, ctx->tm_UPP, ctx->tm_P, a, ctx->grid, ctx->stream));
-  if (timed) CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+  if (timed) CK(cudaEventRecordWithFlags(ctx->ev[2], ctx->stream, cudaEventRecordExternal));
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
     CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->mlp_image, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
                           ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->stream));
-  if (timed) CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+  if (timed) CK(cudaEventRecordWithFlags(ctx->ev[3], ctx->stream, cudaEventRecordExternal));
   return TLQ_OK;
 }
 
-int build_graph(tlq_ctx* ctx, int par) {
+// The step on parity par as a graph (timed: with the timing events).
+int build_graph(tlq_ctx* ctx, int par, bool timed = false) {
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_step(ctx, par, false);
+  int rc = enqueue_step(ctx, par, timed);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   if (rc != TLQ_OK) { if (g) cudaGraphDestroy(g); return rc; }
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
-  e = cudaGraphInstantiate(&ctx->graph[par], g, 0);
+  e = cudaGraphInstantiate(timed ? &ctx->tgraph[par] : &ctx->graph[par], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
   return TLQ_OK;
@@ -248,17 +258,23 @@ int run_steps(tlq_ctx* ctx, int n) {
     return fail(ctx, TLQ_ERR_STATE, "surrogate cooling on but no network (train or set one first)");
   for (int q = 0; q < n; ++q) {
     const int par = ctx->cur;
-    if (ctx->timing) {
-      int rc = enqueue_step(ctx, par, true);
-      if (rc) return rc;
+    if (ctx->timing) {  // the same step graph with its events recorded
+      if (!ctx->tgraph[par]) {
+        int rc = build_graph(ctx, par, true);
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(ctx->tgraph[par], ctx->stream));
       CK(cudaEventSynchronize(ctx->ev[3]));
-      float a = 0.f, b = 0.f, c = 0.f;
-      cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
-      cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+      float a = 0.f, b = 0.f, c = 0.f, g1 = 0.f, g2 = 0.f;
+      cudaEventElapsedTime(&a, ctx->ev[4], ctx->ev[1]);
+      cudaEventElapsedTime(&b, ctx->ev[5], ctx->ev[2]);
       cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]);
+      cudaEventElapsedTime(&g1, ctx->ev[0], ctx->ev[4]);
+      cudaEventElapsedTime(&g2, ctx->ev[1], ctx->ev[5]);
       ctx->ms1_acc += a;
       ctx->ms2_acc += b;
       ctx->mscool_acc += c;
+      ctx->msgrav_acc += (double)g1 + (double)g2;
       ctx->ntimed += 1;
     } else {
       if (!ctx->graph[par]) {
@@ -416,7 +432,7 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   if (!r) r = make_map(ctx, &ctx->tm_UPP, ctx->UPP, 5);
   if (!r) r = make_map(ctx, &ctx->tm_P, ctx->Pc, 1);
   if (r) return bail(r);
-  for (int q = 0; q < 4; ++q) cudaEventCreate(&ctx->ev[q]);
+  for (int q = 0; q < 6; ++q) cudaEventCreate(&ctx->ev[q]);
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(TLQ_ERR_CUDA);
   *out = ctx;
   return TLQ_OK;
@@ -427,7 +443,7 @@ int tlq_destroy(tlq_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   output_free(ctx);
   invalidate_graphs(ctx);
-  for (int q = 0; q < 4; ++q)
+  for (int q = 0; q < 6; ++q)
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
@@ -695,7 +711,7 @@ int tlq_synchronize(tlq_ctx* ctx) {
 int tlq_enable_timing(tlq_ctx* ctx, int on) {
   if (!ctx) return TLQ_ERR_ARG;
   ctx->timing = on != 0;
-  ctx->ms1_acc = ctx->ms2_acc = ctx->mscool_acc = 0.0;
+  ctx->ms1_acc = ctx->ms2_acc = ctx->mscool_acc = ctx->msgrav_acc = 0.0;
   ctx->ntimed = 0;
   return TLQ_OK;
 }
@@ -716,6 +732,7 @@ int tlq_stats_get(tlq_ctx* ctx, tlq_stats* s) {
   s->ms_stage1 = ctx->ntimed ? ctx->ms1_acc / ctx->ntimed : 0.0;
   s->ms_stage2 = ctx->ntimed ? ctx->ms2_acc / ctx->ntimed : 0.0;
   s->ms_cool = ctx->ntimed ? ctx->mscool_acc / ctx->ntimed : 0.0;
+  s->ms_grav = ctx->ntimed ? ctx->msgrav_acc / ctx->ntimed : 0.0;
   s->bytes_state = (double)ctx->L.plane * 8.0 * 17.0;
   if (ctx->cool_counts) {
     unsigned long long cc[3] = {0, 0, 0};

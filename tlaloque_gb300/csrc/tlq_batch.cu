@@ -634,11 +634,16 @@ int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen) {
     const bool carried = c.cooling != TLQ_COOL_NONE && c.precision == TLQ_PREC_FP64;
     const size_t bytes = (size_t)ctx->L.plane * 5 * sizeof(double);
     const size_t pbytes = carried ? (size_t)ctx->L.plane * sizeof(double) : 0;
+    // and the self-gravity potential (each solve starts from the last one)
+    const long long mg = c.self_gravity ? (long long)(c.nx + 2) * (c.nx + 2) * (c.nx + 2) : 0;
+    const size_t gbytes = (size_t)mg * sizeof(double);
     double* snap = nullptr;
     tlq::Clock clk{};
-    if (cudaMalloc(&snap, bytes + pbytes) != cudaSuccess) return TLQ_ERR_NOMEM;
+    if (cudaMalloc(&snap, bytes + pbytes + gbytes) != cudaSuccess) return TLQ_ERR_NOMEM;
+    double* gsnap = snap + (bytes + pbytes) / sizeof(double);
     cudaMemcpyAsync(snap, ctx->U[cur], bytes, cudaMemcpyDeviceToDevice, ctx->stream);
     if (carried) cudaMemcpyAsync(snap + ctx->L.plane * 5, ctx->Pc, pbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (mg) cudaMemcpyAsync(gsnap, ctx->phig, gbytes, cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(&clk, ctx->clk, sizeof(clk), cudaMemcpyDeviceToHost, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     const long long steps0 = ctx->steps;
@@ -656,7 +661,7 @@ int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen) {
         cudaFree(snap);
         return rc;
       }
-      const double ms = s.ms_stage1 + s.ms_stage2 + s.ms_cool;
+      const double ms = s.ms_stage1 + s.ms_stage2 + s.ms_cool + s.ms_grav;
       if (ms < best_ms) {
         best_ms = ms;
         best = std::min(z, c.nz);
@@ -664,6 +669,7 @@ int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen) {
       // back to the snapshot
       cudaMemcpyAsync(ctx->U[cur], snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
       if (carried) cudaMemcpyAsync(ctx->Pc, snap + ctx->L.plane * 5, pbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (mg) cudaMemcpyAsync(ctx->phig, gsnap, gbytes, cudaMemcpyDeviceToDevice, ctx->stream);
       cudaMemcpyAsync(ctx->clk, &clk, sizeof(clk), cudaMemcpyHostToDevice, ctx->stream);
       if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         cudaFree(snap);

@@ -58,10 +58,13 @@ struct tlq_ctx {
   double t0 = 0.0;
   int it0 = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t tgraph[2] = {nullptr, nullptr};  // the same steps with the timing events recorded
   unsigned gen = 0;  // bumped whenever set-up changes what a captured step does
   bool timing = false;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  double ms1_acc = 0.0, ms2_acc = 0.0, mscool_acc = 0.0;
+  // timing events: stage-1 start, stage-2 start, stage-2 end, cooling end,
+  // and the ends of the two self-gravity solves
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double ms1_acc = 0.0, ms2_acc = 0.0, mscool_acc = 0.0, msgrav_acc = 0.0;
   long long ntimed = 0;
   long long steps = 0;
   // learned cooling surrogate (TLQ_COOL_MLP)
@@ -92,6 +95,9 @@ void output_free(tlq_ctx* ctx);  // waits for a pending output, frees its buffer
 // Closed-form cooling-time integral of the table for the surrogate's
 // residual check (tlq_surrogate.cu); called by tlq_set_cooling_table.
 int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* logL, int n);
+
+// Drops the captured step graphs and bumps the set-up generation (tlq_api.cu).
+void invalidate_graphs(tlq_ctx* c);
 
 // Z-chunk length of the stage grid (>= 8 planes, or nz): regrids and drops
 // the captured graphs (tlq_api.cu).

@@ -34,6 +34,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -43,19 +44,22 @@ namespace tlq {
 namespace {
 
 constexpr int MG_MAXL = 11;         // levels 0..10: meshes up to 1024^3
-constexpr int MG_COARSE_N = 32;     // levels of at most this many cells run in the one-block kernel
+constexpr int MG_COARSE_N = 8;      // levels of at most this many cells run in the one-block kernel
 constexpr int MG_CYCLES = 31;       // the reference's V-cycle cap (sources.f90:140)
 constexpr int MG_PF = 4;            // diagonal steps the smoother's loads run ahead
 constexpr int MG_MOM_THREADS = 256;
 constexpr int MG_MOM_BLOCKS = 152 * 2;
 constexpr int MG_SOLVE_LIMIT = 100000;  // coarsest-level Gauss-Seidel passes before giving up
+constexpr int MG_CHUNK = 4;             // diagonals between progress publications (pipelined relax)
+constexpr long long MG_WAIT_LIMIT = 1LL << 24;  // polls of a neighbour's progress before giving up (~1 s)
 constexpr int MG_ST_SOLVE = 1;
+constexpr int MG_ST_TIMEOUT = 2;
 
 struct MgLevel {
   int n;
   double* E;
   double* R;
-  double* T;
+  double* T;   // source(i,j,k)*dxl**2 of the smoother, formed once with R
   double dxl;  // (xr - xl) / n (sources.f90:232; x extent for every axis, as there)
 };
 
@@ -67,6 +71,8 @@ struct MgCtl {
   double dif;  // the last smoother pass's summed |change| (the reference's Dif)
   double c0[5], cm[5][5], sm[5][5];  // multipole moments (sources.f90:599-681)
   double part[2 * 1024];             // per-plane partial sums of the last pass's |change|
+  int abort;                         // a pipelined relax gave up waiting (sticky for the call)
+  int prog[1026];                    // pipelined relax: plane k's last finished diagonal, hs*(2n+2) + d
 };
 
 __host__ __device__ __forceinline__ long long mgi(int n, int i, int j, int k) {
@@ -248,17 +254,21 @@ __global__ void k_mg_begin(MgCtl* c, const Clock* clk) {
   c->active = 0;
   c->iter = 0;
   c->dif = 1.e28;
+  c->abort = 0;
 }
 
 // Residue(0) = 4 pi G dens, Error(0) = phi (sources.f90:136-137).
 template <class Dens>
-__global__ void k_mg_init(const MgCtl* c, Dens rho, int n, const double* phi, double* E0, double* R0) {
+__global__ void k_mg_init(const MgCtl* c, Dens rho, int n, const double* phi, double* E0, double* R0, double* T0,
+                          double dxl) {
   if (!c->run) return;
   const long long cells = (long long)(n + 2) * (n + 2) * (n + 2);
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < cells;
        q += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(q % (n + 2)), j = (int)((q / (n + 2)) % (n + 2)), k = (int)(q / ((long long)(n + 2) * (n + 2)));
-    R0[q] = 4.0 * 3.14159265358979 * 6.67430e-8 * rho(i, j, k);
+    const double r = 4.0 * 3.14159265358979 * 6.67430e-8 * rho(i, j, k);
+    R0[q] = r;
+    T0[q] = r * (dxl * dxl);
     E0[q] = phi[q];
   }
 }
@@ -295,9 +305,12 @@ __global__ void k_mg_cycle_end(MgCtl* c, int nparts) {
 
 // phi = Error(0) (sources.f90:189); PHIT = PHIP + PHI into the stage's
 // potential plane (HLLC.f90:22).
-__global__ void k_mg_end(const MgCtl* c, int n, const double* E0, double* phig, const double* phip, double* phit,
-                         Layout L) {
+// A solve that gave up (a bounded wait or the coarsest solve) marks the
+// step's status as timed out.
+__global__ void k_mg_end(const MgCtl* c, Clock* clk, int n, const double* E0, double* phig, const double* phip,
+                         double* phit, Layout L) {
   if (!c->run) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && c->status) atomicOr(&clk->status, ST_TIMEOUT);
   const long long cells = (long long)(n + 2) * (n + 2) * (n + 2);
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < cells;
        q += (long long)gridDim.x * blockDim.x) {
@@ -314,33 +327,43 @@ __global__ void k_mg_end(const MgCtl* c, int n, const double* E0, double* phig, 
 // ---------------------------------------------------------------------------
 // Level operators
 // ---------------------------------------------------------------------------
-// One smoother update (sources.f90:378-379, 447-449; w = 1).
+// One smoother update (sources.f90:378-379, 447-449), sdx = source*dxl**2.
+// The reference's tail ((1/6) a) w + (1-w) old with w = 1 equals (1/6) a
+// bit for bit unless that is a signed zero or old is not finite (then the
+// 0*old term can change the sign or give a NaN): those take the literal
+// expression, every other update saves its three FP64 operations (the FP64
+// pipe bounds the smoother).
 __device__ __forceinline__ double mg_new(double east, double west, double north, double south, double up, double down,
-                                         double src, double dxl2, double old) {
-  const double w = 1.0;
+                                         double sdx, double old) {
   double a = east + west;
   a = a + north;
   a = a + south;
   a = a + up;
   a = a + down;
-  a = a - src * dxl2;
-  return ((1.0 / 6.0) * a) * w + (1.0 - w) * old;
+  a = a - sdx;
+  double v = (1.0 / 6.0) * a;
+  const long long vb = __double_as_longlong(v), ob = __double_as_longlong(old);
+  if ((vb & 0x7fffffffffffffffLL) == 0 || ((ob >> 52) & 0x7ff) == 0x7ff) {
+    const double w = 1.0;
+    v = v * w + (1.0 - w) * old;
+  }
+  return v;
 }
 
 // Cells (i even, j odd) of plane k: none of them shares a face with another,
 // so they update in any order (threads t of nt share them).
+template <bool TRACK>
 __device__ double mg_parallel_plane(const MgLevel& lv, int k, int t, int nt) {
   const int n = lv.n, h = n / 2;
-  const double dxl2 = lv.dxl * lv.dxl;
   double acc = 0.0;
   for (int q = t; q < h * h; q += nt) {
     const int i = 2 * (q % h + 1), j = 2 * (q / h) + 1;
     const long long o = mgi(n, i, j, k), s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
     const double old = lv.E[o];
-    const double v = mg_new(lv.E[o + 1], lv.E[o - 1], lv.E[o + s1], lv.E[o - s1], lv.E[o + s2], lv.E[o - s2], lv.R[o],
-                            dxl2, old);
+    const double v = mg_new(lv.E[o + 1], lv.E[o - 1], lv.E[o + s1], lv.E[o - s1], lv.E[o + s2], lv.E[o - s2], lv.T[o],
+                            old);
     lv.E[o] = v;
-    acc += fabs(v - old);
+    if (TRACK) acc += fabs(v - old);
   }
   return acc;
 }
@@ -351,12 +374,12 @@ __device__ double mg_parallel_plane(const MgLevel& lv, int k, int t, int nt) {
 // value, west its neighbour's (pub, double-buffered by diagonal parity).
 // The loads of the other neighbours run MG_PF diagonals ahead.  Every thread
 // of the block calls this with the same n (uniform barriers); i > n idles.
+template <bool TRACK>
 __device__ double mg_wave_plane(const MgLevel& lv, int k, int i, double* pub) {
   const int n = lv.n;
   const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
   double* __restrict__ E = lv.E;
-  const double* __restrict__ R = lv.R;
-  const double dxl2 = lv.dxl * lv.dxl;
+  const double* __restrict__ R = lv.T;
   double rc[MG_PF], re[MG_PF], rn[MG_PF], ru[MG_PF], rd[MG_PF], rs[MG_PF];
   const bool col = i >= 1 && i <= n;
 #pragma unroll
@@ -381,9 +404,9 @@ __device__ double mg_wave_plane(const MgLevel& lv, int k, int i, double* pub) {
           const double old = rc[q];
           double cur = old;
           if ((i & 1) || !(j & 1)) {  // s = 0: this half-sweep's cell
-            cur = mg_new(re[q], west, rn[q], south, ru[q], rd[q], rs[q], dxl2, old);
+            cur = mg_new(re[q], west, rn[q], south, ru[q], rd[q], rs[q], old);
             E[o] = cur;
-            acc += fabs(cur - old);
+            if (TRACK) acc += fabs(cur - old);
           }
           pub[(d & 1) * (n + 1) + i] = cur;
           prev = cur;
@@ -417,7 +440,7 @@ __device__ double block_sum(double v, double* red) {
 // (n threads).  half 0: cells with k parity = s; half 1: the others
 // (sources.f90:438-452 and :456-468).  part: where the plane's summed
 // |change| goes (null: not needed).
-template <int NT>
+template <int NT, bool TRACK>
 __global__ void __launch_bounds__(NT) k_mg_half(const MgCtl* c, MgLevel lv, int half, double* part) {
   __shared__ double pub[2 * 1025];
   __shared__ double red[32];
@@ -426,13 +449,169 @@ __global__ void __launch_bounds__(NT) k_mg_half(const MgCtl* c, MgLevel lv, int 
   const int sk = (k & 1) ^ half;  // the s of this half-sweep's cells in plane k
   double acc;
   if (sk)
-    acc = mg_parallel_plane(lv, k, threadIdx.x, blockDim.x);
+    acc = mg_parallel_plane<TRACK>(lv, k, threadIdx.x, blockDim.x);
   else
-    acc = mg_wave_plane(lv, k, threadIdx.x + 1, pub);
-  if (part) {
+    acc = mg_wave_plane<TRACK>(lv, k, threadIdx.x + 1, pub);
+  if (TRACK) {
     const double s = block_sum(acc, red);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
   }
+}
+
+// ---------------------------------------------------------------------------
+// A whole relax (5 passes of 2 half-sweeps) in one cooperative launch: block
+// b owns plane k = b+1 through all ten half-sweeps, so the half-sweeps of
+// neighbouring planes overlap instead of running one after another.  Plane
+// k may start diagonals d0..d1 of half-sweep hs once planes k-1 and k+1 have
+// finished diagonal d1+1 of half-sweep hs-1: every value it reads from them
+// (the cells (i, j, k+-1), i + j <= d1) then holds its hs-1 value, and every
+// cell of theirs that reads one of plane k's cells it is about to change
+// (the same (i, j)) has read it.  The waits are bounded; a block that gives
+// up sets the status and the abort flag and every block leaves.  Values of
+// other planes are loaded around L1 (ld.global.cg: L1 is not coherent
+// between the SMs of one launch).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+
+// Thread 0 waits until planes k-1, k+1 (those in 1..n) reach `need`; false
+// when it gave up (the block then leaves the relax).
+__device__ bool mg_wait(MgCtl* c, int k, int n, int need, int* s_ok) {
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile int* prog = c->prog;
+    volatile int* abort = &c->abort;
+    for (int nb = k - 1; nb <= k + 1 && ok; nb += 2) {
+      if (nb < 1 || nb > n) continue;
+      long long tries = 0;
+      while (prog[nb] < need) {
+        if (*abort || ++tries > MG_WAIT_LIMIT) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (!ok) {
+      atomicOr(&c->status, MG_ST_TIMEOUT);
+      atomicExch(&c->abort, 1);
+    }
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+__device__ __forceinline__ void mg_publish(MgCtl* c, int k, int value) {
+  __syncthreads();  // every thread's stores of the chunk are issued
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicExch(&c->prog[k], value);
+  }
+}
+
+// Time step t of a block processes diagonal d = t - MG_SKEW hs of every
+// half-sweep hs at once: a cell of half-sweep hs reads its own plane's
+// cells of half-sweep hs-1 on diagonals d-1..d+1 (processed MG_SKEW-1 steps
+// or more earlier) and its neighbour planes' cells of hs-1 on diagonal d
+// (their step t + 1 - MG_SKEW), so the ten half-sweeps of a relax take
+// 2n + 9 MG_SKEW steps instead of 20n.  A plane checks its neighbours once
+// per MG_CHUNK steps, which MG_SKEW = MG_CHUNK + 1 allows.
+constexpr int MG_SKEW = MG_CHUNK + 1;
+
+size_t pipe_smem(int n) { return (size_t)10 * 2 * (n + 1) * sizeof(double); }
+
+// NT threads, MINB blocks per SM at least, loads of G half-sweeps at a time.
+template <int NT, int MINB, int G, bool TRACK>
+__global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv, double* part) {
+  extern __shared__ double pub[];  // per half-sweep, per diagonal parity: the diagonal's values by i
+  __shared__ double red[32];
+  __shared__ int s_ok;
+  if (!c->active) return;
+  const int n = lv.n, k = blockIdx.x + 1, i = threadIdx.x + 1;
+  const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
+  double* __restrict__ E = lv.E;
+  const double* __restrict__ Sd = lv.T;
+  const bool col = i <= n;
+  const int tmax = 2 * n + 9 * MG_SKEW;
+  double prev[10];
+#pragma unroll
+  for (int hs = 0; hs < 10; ++hs) prev[hs] = 0.0;
+  double acc8 = 0.0, acc9 = 0.0;
+  for (int t0 = 2; t0 <= tmax; t0 += MG_CHUNK) {
+    const int t1 = min(t0 + MG_CHUNK - 1, tmax);
+    const int need = t1 + 1 - MG_SKEW;  // the neighbours' last step this chunk reads
+    if (need >= 2 && !mg_wait(c, k, n, need, &s_ok)) return;
+    for (int t = t0; t <= t1; ++t) {
+      // The loads of G half-sweeps before their stores: the cells a step
+      // reads and the cells it writes lie MG_SKEW diagonals or more apart,
+      // so these loads need not wait behind those stores.
+#pragma unroll
+      for (int g = 0; g < 10; g += G) {
+      double rc[10], re[10], rn[10], ru[10], rd[10], rs[10], rw[10], rv[10];
+#pragma unroll
+      for (int hs = g; hs < (g + G < 10 ? g + G : 10); ++hs) {
+        const int d = t - MG_SKEW * hs, j = d - i;
+        if (d >= 2 && d <= 2 * n && col && j >= 1 && j <= n) {
+          const long long o = mgi(n, i, j, k);
+          rc[hs] = E[o]; re[hs] = E[o + 1]; rn[hs] = E[o + s1];
+          ru[hs] = ldcg(E + o + s2); rd[hs] = ldcg(E + o - s2); rs[hs] = Sd[o];
+          // west and south from memory: the parallel cells' (other colour,
+          // this plane, hs-1) and the ghosts; the wave cells' others come
+          // from this half-sweep's previous diagonal
+          const bool par = ((k & 1) ^ (hs & 1)) != 0;
+          rw[hs] = (par || i == 1) ? E[o - 1] : 0.0;
+          rv[hs] = (par || j == 1) ? E[o - s1] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int hs = g; hs < (g + G < 10 ? g + G : 10); ++hs) {
+        const int d = t - MG_SKEW * hs;
+        if (d < 2 || d > 2 * n) continue;  // (uniform)
+        const int j = d - i;
+        if (!col || j < 1 || j > n) continue;
+        const long long o = mgi(n, i, j, k);
+        const bool par = ((k & 1) ^ (hs & 1)) != 0;  // cells (i even, j odd) of this plane
+        const double old = rc[hs];
+        if (par) {
+          if (!(i & 1) && (j & 1)) {
+            const double v = mg_new(re[hs], rw[hs], rn[hs], rv[hs], ru[hs], rd[hs], rs[hs], old);
+            E[o] = v;
+            if (TRACK && hs == 8) acc8 += fabs(v - old);
+            if (TRACK && hs == 9) acc9 += fabs(v - old);
+          }
+        } else {
+          double* pb = pub + hs * 2 * (n + 1);
+          const double west = i == 1 ? rw[hs] : pb[((d - 1) & 1) * (n + 1) + i - 1];
+          const double south = j == 1 ? rv[hs] : prev[hs];
+          double cur = old;
+          if ((i & 1) || !(j & 1)) {
+            cur = mg_new(re[hs], west, rn[hs], south, ru[hs], rd[hs], rs[hs], old);
+            E[o] = cur;
+            if (TRACK && hs == 8) acc8 += fabs(cur - old);
+            if (TRACK && hs == 9) acc9 += fabs(cur - old);
+          }
+          pb[(d & 1) * (n + 1) + i] = cur;
+          prev[hs] = cur;
+        }
+      }
+      }
+      __syncthreads();
+    }
+    mg_publish(c, k, t1);
+  }
+  if (TRACK) {
+    const double a = block_sum(acc8, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+    const double b = block_sum(acc9, red);
+    if (threadIdx.x == 0) part[n + blockIdx.x] = b;
+  }
+}
+
+// Progress of every plane (and its two ghost planes) to "nothing done".
+__global__ void k_mg_prog_reset(MgCtl* c, int n) {
+  if (!c->active) return;
+  for (int q = threadIdx.x; q <= n + 1; q += blockDim.x) c->prog[q] = -1;
 }
 
 // The error's ghosts on a coarse level: -(first interior layer) per face in
@@ -492,7 +671,9 @@ __device__ void mg_resid_restrict(const MgLevel& f, const MgLevel& c, long long 
     a = a + mg_resid_cell(f, i1 + 1, j1, k1 + 1);
     a = a + mg_resid_cell(f, i1, j1 + 1, k1 + 1);
     a = a + mg_resid_cell(f, i1 + 1, j1 + 1, k1 + 1);
-    c.R[mgi(nc, i, j, k)] = (1.0 / 8.0) * a;
+    const double r = (1.0 / 8.0) * a;
+    c.R[mgi(nc, i, j, k)] = r;
+    c.T[mgi(nc, i, j, k)] = r * (c.dxl * c.dxl);
   }
 }
 
@@ -536,7 +717,7 @@ __global__ void k_mg_prolong_add(const MgCtl* c, MgLevel co, MgLevel f) {
 // ---------------------------------------------------------------------------
 // Levels lc..L (n <= MG_COARSE_N) of one V-cycle in one block
 // ---------------------------------------------------------------------------
-constexpr int MG_CT = 512;  // threads: (n/2 planes) x n <= 16 x 32
+constexpr int MG_CT = 128;  // threads: (n/2 planes) x n <= 4 x 8, and the level-wide loops
 
 // Relax (5 passes of 2 half-sweeps) on a level of at most 32 cells; the
 // wave planes of a half-sweep advance together, thread t <-> (plane slot
@@ -550,12 +731,12 @@ __device__ double mg_relax_block(const MgLevel& lv, double* pub, double* red, bo
     for (int half = 0; half < 2; ++half) {
       // parallel planes: (k & 1) != half
       for (int k = 1; k <= n; ++k)
-        if (((k & 1) ^ half) == 1 && n >= 2) acc += mg_parallel_plane(lv, k, threadIdx.x, blockDim.x);
+        if (((k & 1) ^ half) == 1 && n >= 2) acc += mg_parallel_plane<true>(lv, k, threadIdx.x, blockDim.x);
       const int ps = threadIdx.x / n, i = threadIdx.x % n + 1;
       const int k = 2 * ps + (half ? 1 : 2);  // (k & 1) == half
       const bool mine = ps < n / 2 && k <= n;
       // every thread runs the diagonal loop (uniform barriers); others idle
-      const double a = mg_wave_plane(lv, mine ? k : 1, mine ? i : n + 1, pub + (mine ? ps : 0) * 2 * (n + 1));
+      const double a = mg_wave_plane<true>(lv, mine ? k : 1, mine ? i : n + 1, pub + (mine ? ps : 0) * 2 * (n + 1));
       acc += mine ? a : 0.0;
       __syncthreads();
     }
@@ -585,7 +766,7 @@ __device__ void mg_solve_block(const MgLevel& lv, MgCtl* c) {
             const long long o = mgi(n, i, j, k);
             const double old = lv.E[o];
             const double v = mg_new(lv.E[o + 1], lv.E[o - 1], lv.E[o + s1], lv.E[o - s1], lv.E[o + s2], lv.E[o - s2],
-                                    lv.R[o], dxl2, old);
+                                    lv.R[o] * dxl2, old);
             lv.E[o] = v;
             difp = difp + fabs(v - old);
           }
@@ -635,10 +816,71 @@ __global__ void __launch_bounds__(MG_CT) k_mg_coarse(MgCtl* c, MgLevels levels, 
 
 // One half-sweep launch: a block per plane, a thread per i (n of them).
 void launch_half(const MgCtl* c, const MgLevel& lv, int half, double* part, cudaStream_t s) {
-  if (lv.n <= 256)
-    k_mg_half<256><<<lv.n, lv.n, 0, s>>>(c, lv, half, part);
-  else
-    k_mg_half<1024><<<lv.n, lv.n, 0, s>>>(c, lv, half, part);
+  const int nt = lv.n < 32 ? 32 : lv.n;  // whole warps (threads past n idle)
+  if (lv.n <= 256) {
+    if (part)
+      k_mg_half<256, true><<<lv.n, nt, 0, s>>>(c, lv, half, part);
+    else
+      k_mg_half<256, false><<<lv.n, nt, 0, s>>>(c, lv, half, part);
+  } else {
+    if (part)
+      k_mg_half<1024, true><<<lv.n, nt, 0, s>>>(c, lv, half, part);
+    else
+      k_mg_half<1024, false><<<lv.n, nt, 0, s>>>(c, lv, half, part);
+  }
+}
+
+// Whether a level's relax runs as one cooperative launch: every plane's
+// block resident at once (checked with the occupancy calculator, once per
+// level size; levels of at most 256 cells), unless TLQ_MG_PIPELINE=0 asks
+// for the per-half-sweep kernels.
+template <int NT, int MINB, int G, bool TRACK>
+bool pipe_fits(int n, int nt) {
+  static int cached[2048] = {0};  // 0 unknown, 1 fits, 2 does not
+  if (n >= 2048) return false;
+  if (!cached[n]) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mg_relax_pipe<NT, MINB, G, TRACK>, nt, pipe_smem(n));
+    cached[n] = (long long)per * sms >= n ? 1 : 2;
+  }
+  return cached[n] == 1;
+}
+
+template <int NT, int MINB, int G, bool TRACK>
+bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, int nt, cudaStream_t s) {
+  if (!pipe_fits<NT, MINB, G, TRACK>(lv.n, nt)) return false;
+  k_mg_prog_reset<<<1, 256, 0, s>>>(c, lv.n);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(lv.n);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = pipe_smem(lv.n);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_mg_relax_pipe<NT, MINB, G, TRACK>, c, lv, part) == cudaSuccess;
+}
+
+// One relax of a level above MG_COARSE_N cells (sources.f90:398-471); part:
+// where the last pass's per-plane |change| sums go (null: not needed).
+// Levels of up to 152 planes run one block per SM with every half-sweep's
+// loads ahead; 256-cell levels need two blocks per SM and load three
+// half-sweeps at a time.
+void launch_relax(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
+  const int nt = lv.n < 32 ? 32 : lv.n;
+  const char* env = std::getenv("TLQ_MG_PIPELINE");
+  const bool pipe = !(env && env[0] == '0');
+  bool done = false;
+  if (pipe && lv.n <= 128)
+    done = part ? launch_pipe<128, 1, 10, true>(c, lv, part, nt, s) : launch_pipe<128, 1, 10, false>(c, lv, part, nt, s);
+  else if (pipe && lv.n <= 256)
+    done = part ? launch_pipe<256, 2, 3, true>(c, lv, part, nt, s) : launch_pipe<256, 2, 3, false>(c, lv, part, nt, s);
+  if (done) return;
+  for (int h = 0; h < 10; ++h) launch_half(c, lv, h & 1, (part && h >= 8) ? part + (h - 8) * lv.n : nullptr, s);
 }
 
 int grid_for(long long work, int threads) {
@@ -737,7 +979,8 @@ cudaError_t enqueue_mg(tlq_ctx* ctx, Dens rho, const Clock* clk, double* phit, c
     k_mg_moments_final<<<1, 32, 0, s>>>(c, clk, static_cast<const double*>(ctx->mg_mom), MG_MOM_BLOCKS);
     k_mg_faces<<<grid_for(6LL * n * n, 256), 256, 0, s>>>(c, clk, ctx->P, ctx->phig);
   }
-  k_mg_init<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, rho, n, ctx->phig, v.lv[0].E, v.lv[0].R);
+  k_mg_init<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, rho, n, ctx->phig, v.lv[0].E, v.lv[0].R, v.lv[0].T,
+                                                        v.lv[0].dxl);
   double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(c) + offsetof(MgCtl, part));
   for (int cyc = 0; cyc < MG_CYCLES; ++cyc) {
     k_mg_cycle_begin<<<grid_for(ncoarse, 256), 256, 0, s>>>(c, v.lv[0].E + m0 * m0 * m0, ncoarse);
@@ -750,7 +993,7 @@ cudaError_t enqueue_mg(tlq_ctx* ctx, Dens rho, const Clock* clk, double* phit, c
     // down: level 0 .. lc-1 on the large kernels
     for (int l = 0; l < lc; ++l) {
       if (l > 0) k_mg_ghosts<<<1, 1024, 0, s>>>(c, v.lv[l], multipole ? 1 : 0);
-      for (int h = 0; h < 10; ++h) launch_half(c, v.lv[l], h & 1, nullptr, s);
+      launch_relax(c, v.lv[l], nullptr, s);
       k_mg_resid_restrict<<<grid_for((long long)v.lv[l + 1].n * v.lv[l + 1].n * v.lv[l + 1].n, 256), 256, 0, s>>>(
           c, v.lv[l], v.lv[l + 1]);
     }
@@ -760,15 +1003,13 @@ cudaError_t enqueue_mg(tlq_ctx* ctx, Dens rho, const Clock* clk, double* phit, c
       const long long mf = v.lv[l].n + 2;
       k_mg_prolong_add<<<grid_for(mf * mf * mf, 256), 256, 0, s>>>(c, v.lv[l + 1], v.lv[l]);
       if (l > 0) k_mg_ghosts<<<1, 1024, 0, s>>>(c, v.lv[l], multipole ? 1 : 0);
-      for (int h = 0; h < 10; ++h) {
-        // the last pass of the level-0 relax forms Dif (sources.f90:465-471)
-        double* pp = (l == 0 && h >= 8) ? part + (h - 8) * v.lv[0].n : nullptr;
-        launch_half(c, v.lv[l], h & 1, pp, s);
-      }
+      // the last pass of the level-0 relax forms Dif (sources.f90:465-471)
+      launch_relax(c, v.lv[l], l == 0 ? part : nullptr, s);
     }
     k_mg_cycle_end<<<1, 1, 0, s>>>(c, 2 * n);
   }
-  k_mg_end<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, n, v.lv[0].E, ctx->phig, ctx->phi, phit, ctx->L);
+  k_mg_end<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, const_cast<Clock*>(clk), n, v.lv[0].E, ctx->phig, ctx->phi,
+                                                       phit, ctx->L);
   return cudaGetLastError();
 }
 

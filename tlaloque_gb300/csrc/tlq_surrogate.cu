@@ -651,9 +651,7 @@ int tlq_train_cooling_surrogate(tlq_ctx* ctx, const tlq_surrogate_opts* opts, tl
     ctx->mlp_box[q] = o.box[q];
   }
   ctx->mlp_ready = true;
-  ctx->gen += 1;
-  for (int q = 0; q < 2; ++q)
-    if (ctx->graph[q]) { cudaGraphExecDestroy(ctx->graph[q]); ctx->graph[q] = nullptr; }
+  invalidate_graphs(ctx);
   if (rep) {
     rep->loss_first = lfirst;
     rep->loss_last = llast;
@@ -690,9 +688,7 @@ int tlq_set_cooling_surrogate(tlq_ctx* ctx, const float* params, const float* no
   std::memcpy(ctx->mlp_norm, norm6, 6 * sizeof(float));
   std::memcpy(ctx->mlp_box, box6, 6 * sizeof(double));
   ctx->mlp_ready = true;
-  ctx->gen += 1;
-  for (int q = 0; q < 2; ++q)
-    if (ctx->graph[q]) { cudaGraphExecDestroy(ctx->graph[q]); ctx->graph[q] = nullptr; }
+  invalidate_graphs(ctx);
   return TLQ_OK;
 }
 

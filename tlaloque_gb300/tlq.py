@@ -76,7 +76,7 @@ class CStats(C.Structure):
         ("steps", C.c_longlong), ("t", C.c_double), ("dt", C.c_double), ("status", C.c_int), ("graph", C.c_int),
         ("ms_stage1", C.c_double), ("ms_stage2", C.c_double), ("timed", C.c_longlong), ("bytes_state", C.c_double),
         ("cool_mlp", C.c_longlong), ("cool_fallback", C.c_longlong), ("ms_cool", C.c_double),
-        ("cool_single", C.c_longlong),
+        ("cool_single", C.c_longlong), ("ms_grav", C.c_double),
     ]
 
 
