@@ -49,6 +49,15 @@ def test_multigrid_bit_exact_zero_faces(gpu_lib, n):
     np.testing.assert_array_equal(g, o)
 
 
+def test_multigrid_bit_exact_256(gpu_lib):
+    """A 256^3 mesh: its finest level relaxes in the 512-thread, two blocks
+    per SM variant of the pipelined kernel (256 planes resident at once)."""
+    cfg, U0 = problems.gravitating_cloud(256, grav_bc=tlq.GBC_ZERO)
+    g, gc, o, oc = one_call(cfg, U0, np.zeros(cfg.phi_shape, order="F"), 0)
+    assert gc == oc and gc >= 2
+    np.testing.assert_array_equal(g, o)
+
+
 @pytest.mark.parametrize("n", [32, 128])
 def test_multigrid_per_half_sweep_path(gpu_lib, n, monkeypatch):
     """The relax without the pipelined cooperative kernel (one launch per

@@ -522,21 +522,27 @@ constexpr int MG_SKEW = MG_CHUNK + 1;
 size_t pipe_smem(int n) { return (size_t)10 * 2 * (n + 1) * sizeof(double); }
 
 // NT threads, MINB blocks per SM at least, loads of G half-sweeps at a time.
-template <int NT, int MINB, int G, bool TRACK>
+// NT threads at most, MINB blocks per SM at least; the block is n x HG
+// threads: thread t works on column i = t % n + 1 for the K = 10/HG
+// half-sweeps g K .. g K + K-1 of group g = t / n (more warps per plane to
+// hide the FP64 latency), loading G of them at a time.
+template <int NT, int MINB, int HG, int G, bool TRACK>
 __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv, double* part) {
+  constexpr int K = 10 / HG;
+  static_assert(K * HG == 10, "HG divides the ten half-sweeps");
   extern __shared__ double pub[];  // per half-sweep, per diagonal parity: the diagonal's values by i
   __shared__ double red[32];
   __shared__ int s_ok;
   if (!c->active) return;
-  const int n = lv.n, k = blockIdx.x + 1, i = threadIdx.x + 1;
+  const int n = lv.n, k = blockIdx.x + 1;
+  const int i = (int)(threadIdx.x % n) + 1, h0 = (int)(threadIdx.x / n) * K;
   const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
   double* __restrict__ E = lv.E;
   const double* __restrict__ Sd = lv.T;
-  const bool col = i <= n;
   const int tmax = 2 * n + 9 * MG_SKEW;
-  double prev[10];
+  double prev[K];
 #pragma unroll
-  for (int hs = 0; hs < 10; ++hs) prev[hs] = 0.0;
+  for (int q = 0; q < K; ++q) prev[q] = 0.0;
   double acc8 = 0.0, acc9 = 0.0;
   for (int t0 = 2; t0 <= tmax; t0 += MG_CHUNK) {
     const int t1 = min(t0 + MG_CHUNK - 1, tmax);
@@ -547,52 +553,54 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
       // reads and the cells it writes lie MG_SKEW diagonals or more apart,
       // so these loads need not wait behind those stores.
 #pragma unroll
-      for (int g = 0; g < 10; g += G) {
-      double rc[10], re[10], rn[10], ru[10], rd[10], rs[10], rw[10], rv[10];
+      for (int g = 0; g < K; g += G) {
+      double rc[K], re[K], rn[K], ru[K], rd[K], rs[K], rw[K], rv[K];
 #pragma unroll
-      for (int hs = g; hs < (g + G < 10 ? g + G : 10); ++hs) {
+      for (int q = g; q < (g + G < K ? g + G : K); ++q) {
+        const int hs = h0 + q;
         const int d = t - MG_SKEW * hs, j = d - i;
-        if (d >= 2 && d <= 2 * n && col && j >= 1 && j <= n) {
+        if (d >= 2 && d <= 2 * n && j >= 1 && j <= n) {
           const long long o = mgi(n, i, j, k);
-          rc[hs] = E[o]; re[hs] = E[o + 1]; rn[hs] = E[o + s1];
-          ru[hs] = ldcg(E + o + s2); rd[hs] = ldcg(E + o - s2); rs[hs] = Sd[o];
+          rc[q] = E[o]; re[q] = E[o + 1]; rn[q] = E[o + s1];
+          ru[q] = ldcg(E + o + s2); rd[q] = ldcg(E + o - s2); rs[q] = Sd[o];
           // west and south from memory: the parallel cells' (other colour,
           // this plane, hs-1) and the ghosts; the wave cells' others come
           // from this half-sweep's previous diagonal
           const bool par = ((k & 1) ^ (hs & 1)) != 0;
-          rw[hs] = (par || i == 1) ? E[o - 1] : 0.0;
-          rv[hs] = (par || j == 1) ? E[o - s1] : 0.0;
+          rw[q] = (par || i == 1) ? E[o - 1] : 0.0;
+          rv[q] = (par || j == 1) ? E[o - s1] : 0.0;
         }
       }
 #pragma unroll
-      for (int hs = g; hs < (g + G < 10 ? g + G : 10); ++hs) {
+      for (int q = g; q < (g + G < K ? g + G : K); ++q) {
+        const int hs = h0 + q;
         const int d = t - MG_SKEW * hs;
-        if (d < 2 || d > 2 * n) continue;  // (uniform)
+        if (d < 2 || d > 2 * n) continue;  // (uniform within the group)
         const int j = d - i;
-        if (!col || j < 1 || j > n) continue;
+        if (j < 1 || j > n) continue;
         const long long o = mgi(n, i, j, k);
         const bool par = ((k & 1) ^ (hs & 1)) != 0;  // cells (i even, j odd) of this plane
-        const double old = rc[hs];
+        const double old = rc[q];
         if (par) {
           if (!(i & 1) && (j & 1)) {
-            const double v = mg_new(re[hs], rw[hs], rn[hs], rv[hs], ru[hs], rd[hs], rs[hs], old);
+            const double v = mg_new(re[q], rw[q], rn[q], rv[q], ru[q], rd[q], rs[q], old);
             E[o] = v;
             if (TRACK && hs == 8) acc8 += fabs(v - old);
             if (TRACK && hs == 9) acc9 += fabs(v - old);
           }
         } else {
           double* pb = pub + hs * 2 * (n + 1);
-          const double west = i == 1 ? rw[hs] : pb[((d - 1) & 1) * (n + 1) + i - 1];
-          const double south = j == 1 ? rv[hs] : prev[hs];
+          const double west = i == 1 ? rw[q] : pb[((d - 1) & 1) * (n + 1) + i - 1];
+          const double south = j == 1 ? rv[q] : prev[q];
           double cur = old;
           if ((i & 1) || !(j & 1)) {
-            cur = mg_new(re[hs], west, rn[hs], south, ru[hs], rd[hs], rs[hs], old);
+            cur = mg_new(re[q], west, rn[q], south, ru[q], rd[q], rs[q], old);
             E[o] = cur;
             if (TRACK && hs == 8) acc8 += fabs(cur - old);
             if (TRACK && hs == 9) acc9 += fabs(cur - old);
           }
           pb[(d & 1) * (n + 1) + i] = cur;
-          prev[hs] = cur;
+          prev[q] = cur;
         }
       }
       }
@@ -834,7 +842,7 @@ void launch_half(const MgCtl* c, const MgLevel& lv, int half, double* part, cuda
 // block resident at once (checked with the occupancy calculator, once per
 // level size; levels of at most 256 cells), unless TLQ_MG_PIPELINE=0 asks
 // for the per-half-sweep kernels.
-template <int NT, int MINB, int G, bool TRACK>
+template <int NT, int MINB, int HG, int G, bool TRACK>
 bool pipe_fits(int n, int nt) {
   static int cached[2048] = {0};  // 0 unknown, 1 fits, 2 does not
   if (n >= 2048) return false;
@@ -842,15 +850,16 @@ bool pipe_fits(int n, int nt) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mg_relax_pipe<NT, MINB, G, TRACK>, nt, pipe_smem(n));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mg_relax_pipe<NT, MINB, HG, G, TRACK>, nt, pipe_smem(n));
     cached[n] = (long long)per * sms >= n ? 1 : 2;
   }
   return cached[n] == 1;
 }
 
-template <int NT, int MINB, int G, bool TRACK>
-bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, int nt, cudaStream_t s) {
-  if (!pipe_fits<NT, MINB, G, TRACK>(lv.n, nt)) return false;
+template <int NT, int MINB, int HG, int G, bool TRACK>
+bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
+  const int nt = lv.n * HG;
+  if (!pipe_fits<NT, MINB, HG, G, TRACK>(lv.n, nt)) return false;
   k_mg_prog_reset<<<1, 256, 0, s>>>(c, lv.n);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(lv.n);
@@ -862,24 +871,30 @@ bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, int nt, cudaStream_t
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_mg_relax_pipe<NT, MINB, G, TRACK>, c, lv, part) == cudaSuccess;
+  return cudaLaunchKernelEx(&cfg, k_mg_relax_pipe<NT, MINB, HG, G, TRACK>, c, lv, part) == cudaSuccess;
 }
 
 // One relax of a level above MG_COARSE_N cells (sources.f90:398-471); part:
 // where the last pass's per-plane |change| sums go (null: not needed).
-// Levels of up to 152 planes run one block per SM with every half-sweep's
-// loads ahead; 256-cell levels need two blocks per SM and load three
-// half-sweeps at a time.
+// Threads per plane: 128-cell levels 2 x 128 (five half-sweeps each), 64:
+// 5 x 64, 32 and 16: 10 x n; 256-cell levels need two blocks per SM and
+// run 256 threads loading three half-sweeps at a time.
+template <bool TRACK>
+bool launch_pipe_any(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
+  switch (lv.n) {
+    case 16: return launch_pipe<160, 1, 10, 1, TRACK>(c, lv, part, s);
+    case 32: return launch_pipe<320, 1, 10, 1, TRACK>(c, lv, part, s);
+    case 64: return launch_pipe<320, 1, 5, 1, TRACK>(c, lv, part, s);
+    case 128: return launch_pipe<256, 1, 2, 5, TRACK>(c, lv, part, s);
+    case 256: return launch_pipe<512, 2, 2, 1, TRACK>(c, lv, part, s);
+    default: return false;
+  }
+}
+
 void launch_relax(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
-  const int nt = lv.n < 32 ? 32 : lv.n;
   const char* env = std::getenv("TLQ_MG_PIPELINE");
   const bool pipe = !(env && env[0] == '0');
-  bool done = false;
-  if (pipe && lv.n <= 128)
-    done = part ? launch_pipe<128, 1, 10, true>(c, lv, part, nt, s) : launch_pipe<128, 1, 10, false>(c, lv, part, nt, s);
-  else if (pipe && lv.n <= 256)
-    done = part ? launch_pipe<256, 2, 3, true>(c, lv, part, nt, s) : launch_pipe<256, 2, 3, false>(c, lv, part, nt, s);
-  if (done) return;
+  if (pipe && (part ? launch_pipe_any<true>(c, lv, part, s) : launch_pipe_any<false>(c, lv, part, s))) return;
   for (int h = 0; h < 10; ++h) launch_half(c, lv, h & 1, (part && h >= 8) ? part + (h - 8) * lv.n : nullptr, s);
 }
 
