@@ -884,8 +884,8 @@ bool launch_pipe_any(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) 
   switch (lv.n) {
     case 16: return launch_pipe<160, 1, 10, 1, TRACK>(c, lv, part, s);
     case 32: return launch_pipe<320, 1, 10, 1, TRACK>(c, lv, part, s);
-    case 64: return launch_pipe<320, 1, 5, 1, TRACK>(c, lv, part, s);
-    case 128: return launch_pipe<256, 1, 2, 5, TRACK>(c, lv, part, s);
+    case 64: return launch_pipe<640, 1, 10, 1, TRACK>(c, lv, part, s);
+    case 128: return launch_pipe<640, 1, 5, 1, TRACK>(c, lv, part, s);
     case 256: return launch_pipe<512, 2, 2, 1, TRACK>(c, lv, part, s);
     default: return false;
   }
