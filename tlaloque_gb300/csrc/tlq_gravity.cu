@@ -50,7 +50,6 @@ constexpr int MG_PF = 4;            // diagonal steps the smoother's loads run a
 constexpr int MG_MOM_THREADS = 256;
 constexpr int MG_MOM_BLOCKS = 152 * 2;
 constexpr int MG_SOLVE_LIMIT = 100000;  // coarsest-level Gauss-Seidel passes before giving up
-constexpr int MG_CHUNK = 4;             // diagonals between progress publications (pipelined relax)
 constexpr long long MG_WAIT_LIMIT = 1LL << 24;  // polls of a neighbour's progress before giving up (~1 s)
 constexpr int MG_ST_SOLVE = 1;
 constexpr int MG_ST_TIMEOUT = 2;
@@ -510,25 +509,26 @@ __device__ __forceinline__ void mg_publish(MgCtl* c, int k, int value) {
   }
 }
 
-// Time step t of a block processes diagonal d = t - MG_SKEW hs of every
+// Time step t of a block processes diagonal d = t - SKEW hs of every
 // half-sweep hs at once: a cell of half-sweep hs reads its own plane's
-// cells of half-sweep hs-1 on diagonals d-1..d+1 (processed MG_SKEW-1 steps
-// or more earlier) and its neighbour planes' cells of hs-1 on diagonal d
-// (their step t + 1 - MG_SKEW), so the ten half-sweeps of a relax take
-// 2n + 9 MG_SKEW steps instead of 20n.  A plane checks its neighbours once
-// per MG_CHUNK steps, which MG_SKEW = MG_CHUNK + 1 allows.
-constexpr int MG_SKEW = MG_CHUNK + 1;
+// cells of half-sweep hs-1 on diagonals d-1..d+1 (processed SKEW-1 steps or
+// more earlier) and its neighbour planes' cells of hs-1 on diagonal d
+// (their step t + 1 - SKEW), so the ten half-sweeps of a relax take
+// 2n + 9 SKEW steps instead of 20n.  A plane checks its neighbours once per
+// CH steps, which SKEW = CH + 1 allows.
 
 size_t pipe_smem(int n) { return (size_t)10 * 2 * (n + 1) * sizeof(double); }
 
 // NT threads, MINB blocks per SM at least, loads of G half-sweeps at a time.
-// NT threads at most, MINB blocks per SM at least; the block is n x HG
+// NT threads at most, MINB blocks per SM at least, neighbour checks every
+// CH steps; the block is n x HG
 // threads: thread t works on column i = t % n + 1 for the K = 10/HG
 // half-sweeps g K .. g K + K-1 of group g = t / n (more warps per plane to
 // hide the FP64 latency), loading G of them at a time.
-template <int NT, int MINB, int HG, int G, bool TRACK>
+template <int NT, int MINB, int HG, int G, int CH, bool TRACK>
 __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv, double* part) {
   constexpr int K = 10 / HG;
+  constexpr int SKEW = CH + 1;  // steps between consecutive half-sweeps: a neighbour check per CH steps
   static_assert(K * HG == 10, "HG divides the ten half-sweeps");
   extern __shared__ double pub[];  // per half-sweep, per diagonal parity: the diagonal's values by i
   __shared__ double red[32];
@@ -539,18 +539,18 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
   const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
   double* __restrict__ E = lv.E;
   const double* __restrict__ Sd = lv.T;
-  const int tmax = 2 * n + 9 * MG_SKEW;
+  const int tmax = 2 * n + 9 * SKEW;
   double prev[K];
 #pragma unroll
   for (int q = 0; q < K; ++q) prev[q] = 0.0;
   double acc8 = 0.0, acc9 = 0.0;
-  for (int t0 = 2; t0 <= tmax; t0 += MG_CHUNK) {
-    const int t1 = min(t0 + MG_CHUNK - 1, tmax);
-    const int need = t1 + 1 - MG_SKEW;  // the neighbours' last step this chunk reads
+  for (int t0 = 2; t0 <= tmax; t0 += CH) {
+    const int t1 = min(t0 + CH - 1, tmax);
+    const int need = t1 + 1 - SKEW;  // the neighbours' last step this chunk reads
     if (need >= 2 && !mg_wait(c, k, n, need, &s_ok)) return;
     for (int t = t0; t <= t1; ++t) {
       // The loads of G half-sweeps before their stores: the cells a step
-      // reads and the cells it writes lie MG_SKEW diagonals or more apart,
+      // reads and the cells it writes lie SKEW diagonals or more apart,
       // so these loads need not wait behind those stores.
 #pragma unroll
       for (int g = 0; g < K; g += G) {
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
 #pragma unroll
       for (int q = g; q < (g + G < K ? g + G : K); ++q) {
         const int hs = h0 + q;
-        const int d = t - MG_SKEW * hs, j = d - i;
+        const int d = t - SKEW * hs, j = d - i;
         if (d >= 2 && d <= 2 * n && j >= 1 && j <= n) {
           const long long o = mgi(n, i, j, k);
           rc[q] = E[o]; re[q] = E[o + 1]; rn[q] = E[o + s1];
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
 #pragma unroll
       for (int q = g; q < (g + G < K ? g + G : K); ++q) {
         const int hs = h0 + q;
-        const int d = t - MG_SKEW * hs;
+        const int d = t - SKEW * hs;
         if (d < 2 || d > 2 * n) continue;  // (uniform within the group)
         const int j = d - i;
         if (j < 1 || j > n) continue;
@@ -842,7 +842,7 @@ void launch_half(const MgCtl* c, const MgLevel& lv, int half, double* part, cuda
 // block resident at once (checked with the occupancy calculator, once per
 // level size; levels of at most 256 cells), unless TLQ_MG_PIPELINE=0 asks
 // for the per-half-sweep kernels.
-template <int NT, int MINB, int HG, int G, bool TRACK>
+template <int NT, int MINB, int HG, int G, int CH, bool TRACK>
 bool pipe_fits(int n, int nt) {
   static int cached[2048] = {0};  // 0 unknown, 1 fits, 2 does not
   if (n >= 2048) return false;
@@ -850,16 +850,16 @@ bool pipe_fits(int n, int nt) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mg_relax_pipe<NT, MINB, HG, G, TRACK>, nt, pipe_smem(n));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mg_relax_pipe<NT, MINB, HG, G, CH, TRACK>, nt, pipe_smem(n));
     cached[n] = (long long)per * sms >= n ? 1 : 2;
   }
   return cached[n] == 1;
 }
 
-template <int NT, int MINB, int HG, int G, bool TRACK>
+template <int NT, int MINB, int HG, int G, int CH, bool TRACK>
 bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
   const int nt = lv.n * HG;
-  if (!pipe_fits<NT, MINB, HG, G, TRACK>(lv.n, nt)) return false;
+  if (!pipe_fits<NT, MINB, HG, G, CH, TRACK>(lv.n, nt)) return false;
   k_mg_prog_reset<<<1, 256, 0, s>>>(c, lv.n);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(lv.n);
@@ -871,22 +871,23 @@ bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_mg_relax_pipe<NT, MINB, HG, G, TRACK>, c, lv, part) == cudaSuccess;
+  return cudaLaunchKernelEx(&cfg, k_mg_relax_pipe<NT, MINB, HG, G, CH, TRACK>, c, lv, part) == cudaSuccess;
 }
 
 // One relax of a level above MG_COARSE_N cells (sources.f90:398-471); part:
 // where the last pass's per-plane |change| sums go (null: not needed).
-// Threads per plane: 128-cell levels 2 x 128 (five half-sweeps each), 64:
-// 5 x 64, 32 and 16: 10 x n; 256-cell levels need two blocks per SM and
-// run 256 threads loading three half-sweeps at a time.
+// Threads per plane (measured on the gravitating cloud): 128-cell levels
+// 5 x 128 (two half-sweeps each), 64, 32 and 16: 10 x n, neighbour checks
+// every 8 steps; 256-cell levels need two blocks per SM: 2 x 256, checks
+// every 4 steps.
 template <bool TRACK>
 bool launch_pipe_any(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
   switch (lv.n) {
-    case 16: return launch_pipe<160, 1, 10, 1, TRACK>(c, lv, part, s);
-    case 32: return launch_pipe<320, 1, 10, 1, TRACK>(c, lv, part, s);
-    case 64: return launch_pipe<640, 1, 10, 1, TRACK>(c, lv, part, s);
-    case 128: return launch_pipe<640, 1, 5, 1, TRACK>(c, lv, part, s);
-    case 256: return launch_pipe<512, 2, 2, 1, TRACK>(c, lv, part, s);
+    case 16: return launch_pipe<160, 1, 10, 1, 8, TRACK>(c, lv, part, s);
+    case 32: return launch_pipe<320, 1, 10, 1, 8, TRACK>(c, lv, part, s);
+    case 64: return launch_pipe<640, 1, 10, 1, 8, TRACK>(c, lv, part, s);
+    case 128: return launch_pipe<640, 1, 5, 1, 8, TRACK>(c, lv, part, s);
+    case 256: return launch_pipe<512, 2, 2, 1, 4, TRACK>(c, lv, part, s);
     default: return false;
   }
 }
