@@ -44,7 +44,7 @@ namespace tlq {
 namespace {
 
 constexpr int MG_MAXL = 11;         // levels 0..10: meshes up to 1024^3
-constexpr int MG_COARSE_N = 8;      // levels of at most this many cells run in the one-block kernel
+constexpr int MG_COARSE_N = 4;      // levels of at most this many cells run in the one-block kernel
 constexpr int MG_CYCLES = 31;       // the reference's V-cycle cap (sources.f90:140)
 constexpr int MG_PF = 4;            // diagonal steps the smoother's loads run ahead
 constexpr int MG_MOM_THREADS = 256;
@@ -535,7 +535,9 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
   __shared__ int s_ok;
   if (!c->active) return;
   const int n = lv.n, k = blockIdx.x + 1;
-  const int i = (int)(threadIdx.x % n) + 1, h0 = (int)(threadIdx.x / n) * K;
+  // threads past n x HG (whole warps) only take part in the barriers
+  const bool live = (int)threadIdx.x < n * HG;
+  const int i = (int)(threadIdx.x % n) + 1, h0 = live ? (int)(threadIdx.x / n) * K : 0;
   const long long s1 = n + 2, s2 = (long long)(n + 2) * (n + 2);
   double* __restrict__ E = lv.E;
   const double* __restrict__ Sd = lv.T;
@@ -559,7 +561,7 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
       for (int q = g; q < (g + G < K ? g + G : K); ++q) {
         const int hs = h0 + q;
         const int d = t - SKEW * hs, j = d - i;
-        if (d >= 2 && d <= 2 * n && j >= 1 && j <= n) {
+        if (live && d >= 2 && d <= 2 * n && j >= 1 && j <= n) {
           const long long o = mgi(n, i, j, k);
           rc[q] = E[o]; re[q] = E[o + 1]; rn[q] = E[o + s1];
           ru[q] = ldcg(E + o + s2); rd[q] = ldcg(E + o - s2); rs[q] = Sd[o];
@@ -575,7 +577,7 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
       for (int q = g; q < (g + G < K ? g + G : K); ++q) {
         const int hs = h0 + q;
         const int d = t - SKEW * hs;
-        if (d < 2 || d > 2 * n) continue;  // (uniform within the group)
+        if (!live || d < 2 || d > 2 * n) continue;  // (uniform within the group)
         const int j = d - i;
         if (j < 1 || j > n) continue;
         const long long o = mgi(n, i, j, k);
@@ -858,7 +860,7 @@ bool pipe_fits(int n, int nt) {
 
 template <int NT, int MINB, int HG, int G, int CH, bool TRACK>
 bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
-  const int nt = lv.n * HG;
+  const int nt = (lv.n * HG + 31) / 32 * 32;
   if (!pipe_fits<NT, MINB, HG, G, CH, TRACK>(lv.n, nt)) return false;
   k_mg_prog_reset<<<1, 256, 0, s>>>(c, lv.n);
   cudaLaunchConfig_t cfg = {};
@@ -877,14 +879,16 @@ bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
 // One relax of a level above MG_COARSE_N cells (sources.f90:398-471); part:
 // where the last pass's per-plane |change| sums go (null: not needed).
 // Threads per plane (measured on the gravitating cloud): 128-cell levels
-// 5 x 128 (two half-sweeps each), 64, 32 and 16: 10 x n, neighbour checks
-// every 8 steps; 256-cell levels need two blocks per SM: 2 x 256, checks
-// every 4 steps.
+// 5 x 128 (two half-sweeps each), 64 down to 8: 10 x n; neighbour checks
+// every 8 steps on 128 and 64 cells, 4 on 32, 2 below (a relax takes
+// 2n + 9 (CH + 1) steps); 256-cell levels need two blocks per SM: 2 x 256,
+// checks every 4 steps.
 template <bool TRACK>
 bool launch_pipe_any(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
   switch (lv.n) {
-    case 16: return launch_pipe<160, 1, 10, 1, 8, TRACK>(c, lv, part, s);
-    case 32: return launch_pipe<320, 1, 10, 1, 8, TRACK>(c, lv, part, s);
+    case 8: return launch_pipe<96, 1, 10, 1, 2, TRACK>(c, lv, part, s);
+    case 16: return launch_pipe<160, 1, 10, 1, 2, TRACK>(c, lv, part, s);
+    case 32: return launch_pipe<320, 1, 10, 1, 4, TRACK>(c, lv, part, s);
     case 64: return launch_pipe<640, 1, 10, 1, 8, TRACK>(c, lv, part, s);
     case 128: return launch_pipe<640, 1, 5, 1, 8, TRACK>(c, lv, part, s);
     case 256: return launch_pipe<512, 2, 2, 1, 4, TRACK>(c, lv, part, s);
