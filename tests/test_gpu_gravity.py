@@ -5,9 +5,11 @@ With the serial build's boundary values (zero) every level of the GPU solver
 runs the reference's smoother in its order with FP64 arithmetic as the
 restatement evaluates it, so one MultiGrid call and whole steps with
 self-gravity are bit-identical to the oracle.  With the multipole faces the
-moments are sums over all cells in another order and use CUDA's acos,
-atan2, cos, sin and pow, so the bar is 1e-10 of the potential (one call) and
-1e-10 relative L1 per conserved variable after the steps (the step's bar)."""
+moments are sums over all cells in another order, and the angles' cosines
+and sines come from algebra (z/r, the Chebyshev recurrence, square roots)
+instead of the reference's acos, atan2, cos, sin and real powers, so the bar
+is 1e-10 of the potential (one call) and 1e-10 relative L1 per conserved
+variable after the steps (the step's bar)."""
 import numpy as np
 import pytest
 

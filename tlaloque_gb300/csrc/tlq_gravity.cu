@@ -114,40 +114,62 @@ __device__ double legendre(double x, int l) {
   }
 }
 
+// aLegendre with its (1 - x^2)^(1/2) and ^(3/2) as square roots (the
+// reference raises to the real powers 1/2 and 3/2; equal up to rounding).
+// |x| <= 1 here (x = z/r with r >= |z| in rounded arithmetic), so 1 - x^2 >= 0.
 __device__ double alegendre(double x, int l, int m) {
-  const double x2 = x * x, s = 1.0 - x2;
+  const double x2 = x * x, s = 1.0 - x2, q = sqrt(s);
   switch (l) {
     case 0: return 1.0;
-    case 1: return m == 0 ? x : -pow(s, 0.5);
+    case 1: return m == 0 ? x : -q;
     case 2:
       if (m == 0) return 0.50 * (3.0 * x2 - 1.0);
-      if (m == 1) return -(3.0 * x * pow(s, 0.5));
+      if (m == 1) return -(3.0 * x * q);
       return 3.0 * s;
     case 3:
       if (m == 0) return 0.50 * (5.0 * (x2 * x) - 3.0 * x);
-      if (m == 1) return 1.5 * (1.0 - 5.0 * x2) * pow(s, 0.5);
+      if (m == 1) return 1.5 * (1.0 - 5.0 * x2) * q;
       if (m == 2) return 15.0 * x * s;
-      return -(15.0 * pow(s, 1.5));
+      return -(15.0 * (s * q));
     default:
       if (m == 0) return (1.0 / 8.0) * ((35.0 * (x2 * x2) - 30.0 * x2) + 3.0);
-      if (m == 1) return -(2.5 * (7.0 * (x2 * x) - 3.0 * x) * pow(s, 0.5));
+      if (m == 1) return -(2.5 * (7.0 * (x2 * x) - 3.0 * x) * q);
       if (m == 2) return 7.5 * (7.0 * x2 - 1.0) * s;
-      if (m == 3) return -(105.0 * x * pow(s, 1.5));
+      if (m == 3) return -(105.0 * x * (s * q));
       return 105.0 * (s * s);
   }
 }
 
-// pangle, aangle, distance of the centre of cell (i, j, k) (one rank).
-__device__ void sph_coords(const Params& p, int i, int j, int k, double& coth, double& fi, double& r) {
+// The spherical quantities of the multipole terms at the centre of cell
+// (i, j, k) (pangle, aangle, distance; one rank), by algebra instead of the
+// reference's transcendental round trips: cos(theta) = z/r (it forms
+// cos(acos(z/r))), and cos(m phi), sin(m phi) from cos phi = x/rho, sin phi
+// = y/rho, rho = |(x, y)|, by the Chebyshev recurrence (it takes cos and sin
+// of m atan2(y, x)).  Equal up to rounding; on the FP64 pipe these are a few
+// operations instead of eleven transcendental functions per cell.
+struct Sph {
+  double coth, r, c[5], s[5];
+};
+__device__ Sph sph_terms(const Params& p, int i, int j, int k) {
   const double x = (p.xl + p.dx * (double)i) - p.dx / 2.0;
   const double y = (p.yl + p.dy * (double)j) - p.dy / 2.0;
   const double z = (p.zl + p.dz * (double)k) - p.dz / 2.0;
-  const double thet = acos(z / sqrt((x * x + y * y) + z * z));
-  double f = atan2(y, x);
-  if (f < 0) f = f + 2. * 3.14159265358979;
-  r = sqrt((x * x + y * y) + z * z);
-  coth = cos(thet);
-  fi = f;
+  Sph o;
+  const double rho2 = x * x + y * y;
+  o.r = sqrt(rho2 + z * z);
+  o.coth = z / o.r;
+  const double rho = sqrt(rho2);
+  const double c1 = rho > 0.0 ? x / rho : 1.0, s1 = rho > 0.0 ? y / rho : 0.0;
+  o.c[0] = 1.0;
+  o.s[0] = 0.0;
+  o.c[1] = c1;
+  o.s[1] = s1;
+#pragma unroll
+  for (int m = 2; m <= 4; ++m) {
+    o.c[m] = 2.0 * c1 * o.c[m - 1] - o.c[m - 2];
+    o.s[m] = 2.0 * c1 * o.s[m - 1] - o.s[m - 2];
+  }
+  return o;
 }
 
 // 25 sums per block: c0 l = 0..4, then cm and sm for l = 1..4, m = 1..l.
@@ -165,20 +187,24 @@ __global__ void __launch_bounds__(MG_MOM_THREADS) k_mg_moments(const MgCtl* c, c
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < cells;
        q += (long long)gridDim.x * blockDim.x) {
     const int i = 1 + (int)(q % n), j = 1 + (int)((q / n) % n), k = 1 + (int)(q / ((long long)n * n));
-    double coth, fi, r;
-    sph_coords(p, i, j, k, coth, fi, r);
-    const double d = rho(i, j, k);
-    acc[0] += legendre(coth, 0) * powi(r, 0) * d * vol * vy * vz;
+    const Sph sp = sph_terms(p, i, j, k);
+    const double coth = sp.coth, r = sp.r;
+    // the cell's mass once (the reference multiplies rho dx dy dz into every
+    // term; the order of the products only changes the rounding)
+    const double dm = rho(i, j, k) * vol * vy * vz;
+    acc[0] += dm;  // Legendre(.,0) r**0 = 1
     int slot = 5;
+    double rl = 1.0;
 #pragma unroll
     for (int l = 1; l <= 4; ++l) {
-      const double rl = powi(r, l);
-      acc[l] += legendre(coth, l) * rl * d * vol * vy * vz;
+      rl = rl * r;
+      const double w = rl * dm;
+      acc[l] += legendre(coth, l) * w;
 #pragma unroll
       for (int m = 1; m <= l; ++m, ++slot) {
-        const double al = alegendre(coth, l, m);
-        acc[slot] += al * cos((double)m * fi) * rl * d * vol * vy * vz;
-        acc[slot + 10] += al * sin((double)m * fi) * rl * d * vol * vy * vz;
+        const double t = alegendre(coth, l, m) * w;
+        acc[slot] += t * sp.c[m];
+        acc[slot + 10] += t * sp.s[m];
       }
     }
   }
@@ -231,15 +257,14 @@ __global__ void k_mg_faces(const MgCtl* c, const Clock* clk, Params p, double* p
     if (f < 2) { i = bnd; j = a; k = b; }
     else if (f < 4) { i = a; j = bnd; k = b; }
     else { i = a; j = b; k = bnd; }
-    double coth, fi, rb;
-    sph_coords(p, i, j, k, coth, fi, rb);
+    const Sph sp = sph_terms(p, i, j, k);
+    const double coth = sp.coth, rb = sp.r;
     double v = 0.0;
     v = v - c->c0[0] / rb;
     for (int l = 1; l <= 4; ++l) {
       v = v - c->c0[l] * legendre(coth, l) / powi(rb, l + 1);
       for (int m = 1; m <= l; ++m)
-        v = v - 2.0 * (c->cm[l][m] * cos((double)m * fi) + c->sm[l][m] * sin((double)m * fi)) * alegendre(coth, l, m) /
-                    powi(rb, l + 1);
+        v = v - 2.0 * (c->cm[l][m] * sp.c[m] + c->sm[l][m] * sp.s[m]) * alegendre(coth, l, m) / powi(rb, l + 1);
     }
     phi[mgi(n, i, j, k)] = 6.67430e-8 * v;
   }
