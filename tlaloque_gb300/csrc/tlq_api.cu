@@ -607,8 +607,11 @@ int tlq_upload(tlq_ctx* ctx, const double* U) {
   c.tfin = std::numeric_limits<double>::infinity();
   *ctx->clk_host = c;
   CK(cudaMemcpyAsync(ctx->clk, ctx->clk_host, sizeof(Clock), cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], carries_pressure(ctx) ? ctx->Pc : nullptr, ctx->clk,
-                          init_blocks(ctx->P), ctx->stream));
+  if (ctx->cfg.precision == TLQ_PREC_MIXED)
+    CK(launch_init_dt_mixed(ctx->P, ctx->L, ctx->U[0], ctx->clk, init_blocks(ctx->P), ctx->stream));
+  else
+    CK(launch_init_prims_dt(ctx->P, ctx->L, ctx->U[0], carries_pressure(ctx) ? ctx->Pc : nullptr, ctx->clk,
+                            init_blocks(ctx->P), ctx->stream));
   if (ctx->cfg.self_gravity) {  // mainHD.f90:50-52: the first MultiGrid, PHI starting at 0
     const long long m = ctx->cfg.nx + 2;
     CK(cudaMemsetAsync(ctx->phig, 0, (size_t)(m * m * m) * sizeof(double), ctx->stream));

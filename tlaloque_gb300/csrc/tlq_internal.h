@@ -41,6 +41,9 @@ cudaError_t prepare_mixed_kernels();
 cudaError_t prepare_batch_kernels();  // tlq_batch.cu
 size_t mixed_smem_bytes();
 cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageArgs& a, dim3 grid, cudaStream_t s);
+// The first dt of the mixed form (its FP32 signal speeds; tlq_mixed.cu).
+cudaError_t launch_init_dt_mixed(const Params& p, const Layout& L, const double* U, Clock* clk, int nblocks,
+                                 cudaStream_t s);
 
 // Layout conversions and per-step helpers (SoA device state).
 cudaError_t launch_aos_to_soa(const Aos& A, const Layout& L, const double* src, double* dst, cudaStream_t s);

@@ -42,4 +42,42 @@ cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageA
   return cudaGetLastError();
 }
 
+// calc_prims + time_step on an uploaded state (mainHD.f90:44,74) in the
+// mixed form's arithmetic: FP32 primitives and signal speeds as stage 2 forms
+// them for every later dt, the maxima and dt in FP64.  (The plain form's
+// FP64 division and square root per cell take ~1.6 ms at 256^3 on the FP64
+// pipe; this pass is bound by reading U.)
+__global__ void __launch_bounds__(RED_THREADS) k_init_dt_mixed(Params p, Layout L, const double* __restrict__ U,
+                                                               Clock* clk) {
+  __shared__ double red[96];
+  __shared__ int flag;
+  const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
+  const long long n = (long long)p.nx * p.ny * p.nz;
+  float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(c % p.nx);
+    const long long r = c / p.nx;
+    const int j = 1 + (int)(r % p.ny);
+    const int k = 1 + (int)(r / p.ny);
+    const long long o = L.at(i, j, k);
+    double u[5];
+#pragma unroll
+    for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
+    float cf[5], w[5];
+    mixed_cell(gm1, u, 1, cf, w);
+    const float cs = sqrtf(gf * w[4] / w[0]);
+    const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
+    m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
+    m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
+    m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
+  }
+  cfl_reduce_finalize<RED_THREADS>(f2d(m0), f2d(m1), f2d(m2), clk, p, false, red, &flag);
+}
+
+cudaError_t launch_init_dt_mixed(const Params& p, const Layout& L, const double* U, Clock* clk, int nblocks,
+                                 cudaStream_t s) {
+  k_init_dt_mixed<<<nblocks, RED_THREADS, 0, s>>>(p, L, U, clk);
+  return cudaGetLastError();
+}
+
 }  // namespace tlq
