@@ -35,8 +35,9 @@ def one_call(cfg, U0, phi0, it):
 @pytest.mark.parametrize("n", [8, 16, 32, 64, 128])
 def test_multigrid_bit_exact_zero_faces(gpu_lib, n):
     """One call from phi = 0 and one from a perturbed potential, bit for bit:
-    n = 8 runs in the one-block coarse kernel, larger meshes relax their
-    levels of 16 cells and more in the pipelined cooperative kernel."""
+    levels of 8 to 128 cells relax in the cooperative kernel that holds each
+    plane in shared memory, levels of 4 cells and fewer in the one-block
+    coarse kernel."""
     cfg, U0 = problems.gravitating_cloud(n, grav_bc=tlq.GBC_ZERO)
     g, gc, o, oc = one_call(cfg, U0, np.zeros(cfg.phi_shape, order="F"), 0)
     assert gc == oc and gc >= 2
@@ -66,6 +67,18 @@ def test_multigrid_per_half_sweep_path(gpu_lib, n, monkeypatch):
     half-sweep, the path for levels whose planes cannot all be resident)
     gives the same bits too."""
     monkeypatch.setenv("TLQ_MG_PIPELINE", "0")
+    cfg, U0 = problems.gravitating_cloud(n, grav_bc=tlq.GBC_ZERO)
+    g, gc, o, oc = one_call(cfg, U0, np.zeros(cfg.phi_shape, order="F"), 0)
+    assert gc == oc
+    np.testing.assert_array_equal(g, o)
+
+
+@pytest.mark.parametrize("n", [32, 128])
+def test_multigrid_global_plane_path(gpu_lib, n, monkeypatch):
+    """The skewed cooperative relax that reads every plane from the level
+    arrays (the kernel of 256-cell levels) on levels that otherwise hold
+    their planes in shared memory: the same bits."""
+    monkeypatch.setenv("TLQ_MG_PLANE", "0")
     cfg, U0 = problems.gravitating_cloud(n, grav_bc=tlq.GBC_ZERO)
     g, gc, o, oc = one_call(cfg, U0, np.zeros(cfg.phi_shape, order="F"), 0)
     assert gc == oc

@@ -658,6 +658,109 @@ __global__ void __launch_bounds__(NT, MINB) k_mg_relax_pipe(MgCtl* c, MgLevel lv
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same skewed relax with the block's plane held in shared memory (levels
+// up to 128 cells: (n+2)^2 doubles, 135 KB at 128).  Only plane k's block
+// writes plane k during a relax, so its copy in shared memory is the current
+// one: an update reads its old value and its four in-plane neighbours there
+// (no L2 round trip per step and no diagonal buffers; the values are the
+// same ones the reference's order gives, by the argument above), and
+// writes the new value there and to the level array, where the neighbour
+// planes read it.  The ghost rows and columns (i or j = 0, n+1) do not
+// change during a relax.  Layout: column parity, row, column / 2, so that a
+// warp's cells of one diagonal (consecutive columns of one parity) fall on
+// distinct banks.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int plane_slot(int n, int i, int j) {
+  return ((i & 1) * (n + 2) + j) * ((n >> 1) + 1) + (i >> 1);
+}
+size_t plane_smem(int n) { return (size_t)(n + 2) * (n + 2) * sizeof(double); }
+
+template <int NT, int HG, int CH, bool TRACK>
+__global__ void __launch_bounds__(NT, 1) k_mg_relax_plane(MgCtl* c, MgLevel lv, double* part) {
+  constexpr int K = 10 / HG;
+  constexpr int SKEW = CH + 1;
+  static_assert(K * HG == 10, "HG divides the ten half-sweeps");
+  extern __shared__ double P[];
+  __shared__ double red[32];
+  __shared__ int s_ok;
+  if (!c->active) return;
+  const int n = lv.n, k = blockIdx.x + 1;
+  const long long s2 = (long long)(n + 2) * (n + 2), base = s2 * k;
+  double* __restrict__ E = lv.E;
+  const double* __restrict__ Sd = lv.T;
+  for (int q = threadIdx.x; q < (n + 2) * (n + 2); q += blockDim.x)
+    P[plane_slot(n, q % (n + 2), q / (n + 2))] = E[base + q];
+  __syncthreads();
+  const bool live = (int)threadIdx.x < n * HG;
+  const int col = (int)(threadIdx.x % n), hn = n >> 1;
+  const int i = col < hn ? 2 * col + 1 : 2 * (col - hn) + 2;  // odd columns first (whole idle warps)
+  const int h0 = live ? (int)(threadIdx.x / n) * K : 0;
+  const int R = hn + 1, PS = (n + 2) * R;  // row stride and size of one parity's array
+  const int de = (i & 1) ? 1 - PS : PS, dw = (i & 1) ? -PS : PS - 1;  // east, west: the other parity
+  const int tmax = 2 * n + 9 * SKEW;
+  // one half-sweep's cell of a step: whether it changes, where it lies, and
+  // its values from the level arrays (the planes above and below, the source)
+  struct Fetch {
+    double ru, rd, rs;
+    long long og;
+    int os;
+    bool up;
+  };
+  auto fetch = [&](int t, Fetch* f) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      const int hs = h0 + q, d = t - SKEW * hs, j = d - i;
+      const bool par = ((k & 1) ^ (hs & 1)) != 0;  // cells (i even, j odd) of this plane
+      f[q].up = live && d >= 2 && d <= 2 * n && j >= 1 && j <= n &&
+                (par ? (!(i & 1) && (j & 1)) : ((i & 1) || !(j & 1)));
+      if (f[q].up) {
+        f[q].og = base + i + (long long)(n + 2) * j;
+        f[q].os = plane_slot(n, i, j);
+        f[q].ru = ldcg(E + f[q].og + s2);
+        f[q].rd = ldcg(E + f[q].og - s2);
+        f[q].rs = Sd[f[q].og];
+      }
+    }
+  };
+  double acc8 = 0.0, acc9 = 0.0;
+  for (int t0 = 2; t0 <= tmax; t0 += CH) {
+    const int t1 = min(t0 + CH - 1, tmax);
+    const int need = t1 + 1 - SKEW;  // the neighbours' last step this chunk reads
+    if (need >= 2 && !mg_wait(c, k, n, need, &s_ok)) return;
+    // The other planes' values and the source of step t + 1 load while step
+    // t computes: the chunk's wait covers every step of the chunk, and a
+    // neighbour cannot get SKEW steps ahead of this plane's published
+    // progress, so none of them changes before its use.
+    Fetch cur[K], nxt[K];
+    fetch(t0, cur);
+    for (int t = t0; t <= t1; ++t) {
+      if (t < t1) fetch(t + 1, nxt);
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        if (!cur[q].up) continue;
+        const int hs = h0 + q, o = cur[q].os;
+        const double old = P[o];
+        const double v = mg_new(P[o + de], P[o + dw], P[o + R], P[o - R], cur[q].ru, cur[q].rd, cur[q].rs, old);
+        P[o] = v;
+        E[cur[q].og] = v;
+        if (TRACK && hs == 8) acc8 += fabs(v - old);
+        if (TRACK && hs == 9) acc9 += fabs(v - old);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < K; ++q) cur[q] = nxt[q];
+    }
+    mg_publish(c, k, t1);
+  }
+  if (TRACK) {
+    const double a = block_sum(acc8, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+    const double b = block_sum(acc9, red);
+    if (threadIdx.x == 0) part[n + blockIdx.x] = b;
+  }
+}
+
 // Progress of every plane (and its two ghost planes) to "nothing done".
 __global__ void k_mg_prog_reset(MgCtl* c, int n) {
   if (!c->active) return;
@@ -916,15 +1019,66 @@ bool launch_pipe(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
   return cudaLaunchKernelEx(&cfg, k_mg_relax_pipe<NT, MINB, HG, G, CH, TRACK>, c, lv, part) == cudaSuccess;
 }
 
+// The shared-memory-plane relax: one block of NT threads per plane, all
+// resident at once (with the plane's dynamic shared memory).
+template <int NT, int HG, int CH, bool TRACK>
+bool launch_plane(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
+  const int n = lv.n;
+  const int nt = (n * HG + 31) / 32 * 32;
+  static int state = 0;  // 0 unknown, 1 fits, 2 does not (one level size per instantiation)
+  if (!state) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    bool ok = cudaFuncSetAttribute(k_mg_relax_plane<NT, HG, CH, TRACK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)plane_smem(n)) == cudaSuccess;
+    ok = ok && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mg_relax_plane<NT, HG, CH, TRACK>, nt,
+                                                             plane_smem(n)) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+    state = (ok && (long long)per * sms >= n) ? 1 : 2;
+  }
+  if (state != 1) return false;
+  k_mg_prog_reset<<<1, 256, 0, s>>>(c, n);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = plane_smem(n);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_mg_relax_plane<NT, HG, CH, TRACK>, c, lv, part) == cudaSuccess;
+}
+
+template <bool TRACK>
+bool launch_plane_any(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
+  switch (lv.n) {
+    case 8: return launch_plane<96, 10, 2, TRACK>(c, lv, part, s);
+    case 16: return launch_plane<160, 10, 2, TRACK>(c, lv, part, s);
+    case 32: return launch_plane<320, 10, 4, TRACK>(c, lv, part, s);
+    case 64: return launch_plane<640, 10, 8, TRACK>(c, lv, part, s);
+    case 128: return launch_plane<640, 5, 8, TRACK>(c, lv, part, s);
+    default: return false;
+  }
+}
+
 // One relax of a level above MG_COARSE_N cells (sources.f90:398-471); part:
 // where the last pass's per-plane |change| sums go (null: not needed).
-// Threads per plane (measured on the gravitating cloud): 128-cell levels
+// Levels up to 128 cells hold their planes in shared memory
+// (k_mg_relax_plane) unless TLQ_MG_PLANE=0; the others, and those, then use
+// k_mg_relax_pipe.  Its threads per plane (measured on the gravitating
+// cloud): 128-cell levels
 // 5 x 128 (two half-sweeps each), 64 down to 8: 10 x n; neighbour checks
 // every 8 steps on 128 and 64 cells, 4 on 32, 2 below (a relax takes
 // 2n + 9 (CH + 1) steps); 256-cell levels need two blocks per SM: 2 x 256,
 // checks every 4 steps.
 template <bool TRACK>
 bool launch_pipe_any(MgCtl* c, const MgLevel& lv, double* part, cudaStream_t s) {
+  const char* env = std::getenv("TLQ_MG_PLANE");
+  const bool plane = !(env && env[0] == '0');
+  if (plane && launch_plane_any<TRACK>(c, lv, part, s)) return true;
   switch (lv.n) {
     case 8: return launch_pipe<96, 1, 10, 1, 2, TRACK>(c, lv, part, s);
     case 16: return launch_pipe<160, 1, 10, 1, 2, TRACK>(c, lv, part, s);
