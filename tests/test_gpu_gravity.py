@@ -127,6 +127,29 @@ def test_step_self_gravity_bit_exact(gpu_lib, n):
     assert t == run.t and dt == run.dt
 
 
+def test_step_graph_loop_node(gpu_lib, monkeypatch):
+    """The step's graph runs the V-cycles as the body of a while node (only
+    the cycles the loop test asks for are launched); with TLQ_MG_GRAPH_LOOP=0
+    it holds the fixed sequence of 31 cycle slots instead.  Both give the
+    same bits over twelve steps across a multipole refresh."""
+    cfg, U0 = problems.gravitating_cloud(32)
+    out = []
+    for loop in ("1", "0"):
+        monkeypatch.setenv("TLQ_MG_GRAPH_LOOP", loop)
+        U1 = U0.copy(order="F")
+        with tlq.Context(cfg) as ctx:
+            ctx.borders(U1, 1)
+            ctx.upload(U1)
+            ctx.advance(12)
+            ctx.synchronize()
+            Ug, _ = ctx.state()
+            out.append((Ug, ctx.time()))
+    (Ua, ta), (Ub, tb) = out
+    assert ta[3] == tlq.OK and ta[1] == 12
+    np.testing.assert_array_equal(Ua, Ub)
+    assert ta == tb
+
+
 def test_step_self_gravity_multipole(gpu_lib):
     """Twelve steps across a multipole refresh (it = 0 and 10): relative L1
     <= 1e-10 per conserved variable."""

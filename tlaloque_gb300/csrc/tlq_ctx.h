@@ -28,6 +28,7 @@ struct tlq_ctx {
   void* mg_work = nullptr;
   void* mg_ctl = nullptr;
   void* mg_mom = nullptr;
+  cudaStream_t mg_body = nullptr;  // captures a V-cycle into a graph's loop body
   double* phig = nullptr;
   double* phit = nullptr;
   float* lapf = nullptr;  // mixed form: eta * Laplacian of U between the stages

@@ -320,6 +320,13 @@ __global__ void k_mg_cycle_flag(MgCtl* c) {
   if (go) c->iter = c->iter + 1;
 }
 
+// The same loop test as the condition of a graph's loop node: the step's
+// graph runs the V-cycles as the body of a while node, so that cycles after
+// convergence are not launched at all.
+__global__ void k_mg_loop_test(const MgCtl* c, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, (c->run && c->dif > 10.0 && c->iter < MG_CYCLES) ? 1u : 0u);
+}
+
 __global__ void k_mg_cycle_end(MgCtl* c, int nparts) {
   if (!c->active) return;
   double v = 0.0;
@@ -1131,6 +1138,8 @@ cudaError_t mg_alloc(tlq_ctx* ctx) {
   if (e != cudaSuccess) return e;
   e = cudaMalloc(&ctx->mg_mom, (size_t)MG_MOM_BLOCKS * 25 * sizeof(double));
   if (e != cudaSuccess) return e;
+  e = cudaStreamCreateWithFlags(&ctx->mg_body, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
   const long long m0 = ctx->cfg.nx + 2;
   e = cudaMalloc(&ctx->phig, (size_t)(m0 * m0 * m0) * sizeof(double));
   if (e != cudaSuccess) return e;
@@ -1145,7 +1154,9 @@ cudaError_t mg_alloc(tlq_ctx* ctx) {
 
 void mg_free(tlq_ctx* ctx) {
   cudaFree(ctx->mg_work); cudaFree(ctx->mg_ctl); cudaFree(ctx->mg_mom); cudaFree(ctx->phig); cudaFree(ctx->phit);
+  if (ctx->mg_body) cudaStreamDestroy(ctx->mg_body);
   ctx->mg_work = nullptr; ctx->mg_ctl = nullptr; ctx->mg_mom = nullptr; ctx->phig = nullptr; ctx->phit = nullptr;
+  ctx->mg_body = nullptr;
 }
 
 namespace {
@@ -1196,31 +1207,72 @@ cudaError_t enqueue_mg(tlq_ctx* ctx, Dens rho, const Clock* clk, double* phit, c
   k_mg_init<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, rho, n, ctx->phig, v.lv[0].E, v.lv[0].R, v.lv[0].T,
                                                         v.lv[0].dxl);
   double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(c) + offsetof(MgCtl, part));
-  for (int cyc = 0; cyc < MG_CYCLES; ++cyc) {
-    k_mg_cycle_begin<<<grid_for(ncoarse, 256), 256, 0, s>>>(c, v.lv[0].E + m0 * m0 * m0, ncoarse);
-    k_mg_cycle_flag<<<1, 1, 0, s>>>(c);
+  // One V-cycle slot (sources.f90:140-187): its first kernels evaluate the
+  // loop test, and every later kernel of a slot that does not run returns.
+  auto cycle = [&](cudaStream_t st) {
+    k_mg_cycle_begin<<<grid_for(ncoarse, 256), 256, 0, st>>>(c, v.lv[0].E + m0 * m0 * m0, ncoarse);
+    k_mg_cycle_flag<<<1, 1, 0, st>>>(c);
     if (lc == 0) {
-      k_mg_coarse<<<1, MG_CT, 0, s>>>(c, v, 0, L, multipole ? 1 : 0);
-      k_mg_cycle_end<<<1, 1, 0, s>>>(c, 1);
-      continue;
+      k_mg_coarse<<<1, MG_CT, 0, st>>>(c, v, 0, L, multipole ? 1 : 0);
+      k_mg_cycle_end<<<1, 1, 0, st>>>(c, 1);
+      return;
     }
     // down: level 0 .. lc-1 on the large kernels
     for (int l = 0; l < lc; ++l) {
-      if (l > 0) k_mg_ghosts<<<1, 1024, 0, s>>>(c, v.lv[l], multipole ? 1 : 0);
-      launch_relax(c, v.lv[l], nullptr, s);
-      k_mg_resid_restrict<<<grid_for((long long)v.lv[l + 1].n * v.lv[l + 1].n * v.lv[l + 1].n, 256), 256, 0, s>>>(
+      if (l > 0) k_mg_ghosts<<<1, 1024, 0, st>>>(c, v.lv[l], multipole ? 1 : 0);
+      launch_relax(c, v.lv[l], nullptr, st);
+      k_mg_resid_restrict<<<grid_for((long long)v.lv[l + 1].n * v.lv[l + 1].n * v.lv[l + 1].n, 256), 256, 0, st>>>(
           c, v.lv[l], v.lv[l + 1]);
     }
-    k_mg_coarse<<<1, MG_CT, 0, s>>>(c, v, lc, L, multipole ? 1 : 0);
+    k_mg_coarse<<<1, MG_CT, 0, st>>>(c, v, lc, L, multipole ? 1 : 0);
     // up: level lc-1 .. 0
     for (int l = lc - 1; l >= 0; --l) {
       const long long mf = v.lv[l].n + 2;
-      k_mg_prolong_add<<<grid_for(mf * mf * mf, 256), 256, 0, s>>>(c, v.lv[l + 1], v.lv[l]);
-      if (l > 0) k_mg_ghosts<<<1, 1024, 0, s>>>(c, v.lv[l], multipole ? 1 : 0);
+      k_mg_prolong_add<<<grid_for(mf * mf * mf, 256), 256, 0, st>>>(c, v.lv[l + 1], v.lv[l]);
+      if (l > 0) k_mg_ghosts<<<1, 1024, 0, st>>>(c, v.lv[l], multipole ? 1 : 0);
       // the last pass of the level-0 relax forms Dif (sources.f90:465-471)
-      launch_relax(c, v.lv[l], l == 0 ? part : nullptr, s);
+      launch_relax(c, v.lv[l], l == 0 ? part : nullptr, st);
     }
-    k_mg_cycle_end<<<1, 1, 0, s>>>(c, 2 * n);
+    k_mg_cycle_end<<<1, 1, 0, st>>>(c, 2 * n);
+  };
+  // Captured into a graph: the cycles are the body of a while node whose
+  // condition the loop test sets on the device (before the node and at the
+  // end of each cycle), captured on the context's second stream.  Run
+  // directly (or with TLQ_MG_GRAPH_LOOP=0): the fixed sequence of 31 slots.
+  cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cg, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return e;
+  const char* env = std::getenv("TLQ_MG_GRAPH_LOOP");
+  if (cst == cudaStreamCaptureStatusActive && ctx->mg_body && !(env && env[0] == '0')) {
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, cg, 0, 0);
+    if (e != cudaSuccess) return e;
+    k_mg_loop_test<<<1, 1, 0, s>>>(c, h);
+    e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cg, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(ctx->mg_body, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cycle(ctx->mg_body);
+    k_mg_loop_test<<<1, 1, 0, ctx->mg_body>>>(c, h);
+    cudaGraph_t body = nullptr;
+    e = cudaStreamEndCapture(ctx->mg_body, &body);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+  } else {
+    for (int cyc = 0; cyc < MG_CYCLES; ++cyc) cycle(s);
   }
   k_mg_end<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, const_cast<Clock*>(clk), n, v.lv[0].E, ctx->phig, ctx->phi,
                                                        phit, ctx->L);
