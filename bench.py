@@ -561,7 +561,7 @@ def main():
                    "l2": "inputs larger than L2 (each state array 0.7 GB; 3 arrays touched per step)",
                    "sim": mix["sim"]},
         "forms": forms, "surrogate": surrogate, "e2e": e2e, "roofline": roofline, "clocks": mix["clocks"],
-        "gpu_launches": (4 if surrogate else 2) * args.steps,
+        "gpu_launches": (5 if surrogate else 2) * args.steps,
         "hbm_gbs_step": bpz_m["step"] * cfg.cells * args.steps / (ms_max / 1e3) / 1e9,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -272,7 +272,7 @@ int tlq_autotune(tlq_ctx* ctx, const char* cache_path, int steps, int* chosen);
  * by one persistent launch per stage over all members' tiles, the step
  * replayed from one CUDA graph.  Members run the mixed-precision step
  * (TLQ_PREC_MIXED; any cooling; a member with the cooling surrogate adds its
- * two cooling passes to the captured step).  Member i is a tlq_ctx
+ * three cooling passes to the captured step).  Member i is a tlq_ctx
  * (tlq_batch_member) for every set-up and I/O call (tables, winds, masses,
  * upload, download, get_time); it must not be destroyed on its own.  A
  * member's failure (non-finite dt, non-positive density) stops that member

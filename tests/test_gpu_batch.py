@@ -178,7 +178,7 @@ def test_context_autotune_restores_state(gpu_lib, tmp_path, precision):
 
 
 def test_batch_with_surrogate_members(gpu_lib):
-    """Members with the learned cooling surrogate (their two cooling passes
+    """Members with the learned cooling surrogate (their three cooling passes
     join the captured batched step) advance exactly like their single runs;
     a plain member beside them is unaffected."""
     cfg_a, U_a = problems.wind_bubble(32)
@@ -209,7 +209,7 @@ def test_batch_with_surrogate_members(gpu_lib):
         load(b, members)
         b.run(n)
         assert b.status() == [tlq.OK] * 3
-        assert b.stats().launches_per_step == 2 + 2  # both surrogate members share the two cooling launches
+        assert b.stats().launches_per_step == 2 + 3  # both surrogate members share the three cooling launches
         got = [(m.state()[0], m.time(), (m.stats().cool_mlp, m.stats().cool_fallback)) for m in b.members]
     for (cfg, U0), (U, tm, cc) in zip(members, got):
         ref, tr, rc = single_mlp(cfg, U0)

@@ -234,7 +234,8 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
     CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->mlp_image, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
-                          ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->stream));
+                          ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->mlp_nqueue,
+                          ctx->mlp_qcount + 2, ctx->stream));
   if (timed) CK(cudaEventRecordWithFlags(ctx->ev[3], ctx->stream, cudaEventRecordExternal));
   return TLQ_OK;
 }
@@ -407,9 +408,9 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   if (cfg->cooling == TLQ_COOL_MLP) {
     const size_t ncell = (size_t)cfg->nx * cfg->ny * cfg->nz;
     if (cudaMalloc(&ctx->mlp_queue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_cqueue, ncell * sizeof(unsigned)) ||
-        cudaMalloc(&ctx->mlp_qcount, 2 * sizeof(unsigned)))
+        cudaMalloc(&ctx->mlp_nqueue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_qcount, 3 * sizeof(unsigned)))
       return bail(TLQ_ERR_NOMEM);
-    cudaMemset(ctx->mlp_qcount, 0, 2 * sizeof(unsigned));
+    cudaMemset(ctx->mlp_qcount, 0, 3 * sizeof(unsigned));
   }
   if (cudaMalloc(&ctx->clk, sizeof(Clock)) || cudaMallocHost(&ctx->clk_host, sizeof(Clock))) return bail(TLQ_ERR_NOMEM);
   std::memset(ctx->clk_host, 0, sizeof(Clock));
@@ -449,7 +450,7 @@ int tlq_destroy(tlq_ctx* ctx) {
   cudaFree(ctx->lapf);
   mg_free(ctx);
   cudaFree(ctx->mlp_params); cudaFree(ctx->mlp_image); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
-  cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_qcount);
+  cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_nqueue); cudaFree(ctx->mlp_qcount);
   cudaFree(ctx->clk); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);

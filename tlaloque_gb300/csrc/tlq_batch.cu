@@ -224,7 +224,7 @@ int refresh_desc(tlq_batch* b, const std::vector<int>& which = {}) {
   for (int i = 0; i < (int)b->m.size(); ++i) fill_desc(b, i);
   BCK(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), b->h_desc.size() * sizeof(MemberDesc), cudaMemcpyHostToDevice,
                       b->stream));
-  // each surrogate member gets its own blocks of the two cooling passes: one
+  // each surrogate member gets its own blocks of the three cooling passes: one
   // resident wave of the network pass (152 SMs x 3 blocks) shared in
   // proportion to the cells
   const size_t jb = tlq::cool_job_bytes();
@@ -247,7 +247,8 @@ int refresh_desc(tlq_batch* b, const std::vector<int>& which = {}) {
     const MemberDesc& d = b->h_desc[i];
     tlq::fill_cool_job(b->h_cool.data() + b->ncool * jb, c->P, c->L, c->U[0], c->U[1], c->it_base, c->clk,
                        c->mlp_image, c->mlp_norm, c->mlp_box, c->gcum, c->gslope, c->cool_counts, c->mlp_cqueue,
-                       c->mlp_qcount + 1, c->mlp_queue, c->mlp_qcount, b->cool_blocks, nblk);
+                       c->mlp_qcount + 1, c->mlp_queue, c->mlp_qcount, c->mlp_nqueue, c->mlp_qcount + 2,
+                       b->cool_blocks, nblk);
     b->cool_blocks += nblk;
     ++b->ncool;
   }
@@ -256,7 +257,7 @@ int refresh_desc(tlq_batch* b, const std::vector<int>& which = {}) {
 }
 
 // One batched step of the members the item list holds: the two persistent
-// stage launches, then the surrogate's two cooling passes over the members
+// stage launches, then the surrogate's three cooling passes over the members
 // that use it (their stage 2 queued the cooling cells and left the dt
 // reduction to them; refresh_desc wrote their arguments).
 int enqueue_batch_step(tlq_batch* b) {
@@ -495,10 +496,10 @@ int tlq_batch_stats_get(tlq_batch* b, tlq_batch_stats* s) {
   s->ms_per_step = b->steps_timed ? b->ms_acc / (double)b->steps_timed : 0.0;
   s->items = b->nitems;
   s->blocks = b->blocks;
-  s->launches_per_step = 2;  // the two stages, and the two cooling passes when a member uses the surrogate
+  s->launches_per_step = 2;  // the two stages, and the three cooling passes when a member uses the surrogate
   for (tlq_ctx* c : b->m)
     if (c->cfg.cooling == TLQ_COOL_MLP) {
-      s->launches_per_step = 4;
+      s->launches_per_step = 5;
       break;
     }
   long long cells = 0;

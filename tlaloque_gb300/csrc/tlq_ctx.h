@@ -80,7 +80,9 @@ struct tlq_ctx {
   double cool_tmin = 0.0;                  // the table's first temperature
   unsigned* mlp_cqueue = nullptr;          // cells that cool, queued by stage 2 (capacity nx ny nz)
   unsigned* mlp_queue = nullptr;           // cells handed to the exact integrator (capacity nx ny nz)
-  unsigned* mlp_qcount = nullptr;          // [0]: fallback queue length, [1]: cooling queue length (zero between steps)
+  unsigned* mlp_nqueue = nullptr;          // cells for the network (capacity nx ny nz)
+  unsigned* mlp_qcount = nullptr;          // [0]: fallback queue length, [1]: cooling queue length,
+                                           // [2]: network queue length (zero between steps)
   // output path (tlq_output.cu): device snapshot, page-locked copy, writer thread
   double* out_dev = nullptr;
   double* out_host = nullptr;

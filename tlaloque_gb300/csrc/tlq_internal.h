@@ -81,16 +81,17 @@ cudaError_t launch_gather_pairs(const float* X, const float* Y, const float* Wt,
 cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStream_t s);
 // Surrogate cooling + dt reduction of the mixed step (tlq_surrogate.cu).
 // Stage 2 queues the cells that cool (cqueue) and folds its block maxima
-// into the clock's; the network pass cools the queued cells or queues them
-// for the exact integrator (queue); the fallback pass cools those and
-// finishes the dt reduction.  Queues: capacity nx ny nz; counts zero
-// between steps.
+// into the clock's; the sort pass cools the cells the exact integrator
+// takes in one step and queues the others for the network (nqueue) or the
+// exact integrator (queue); the network pass cools its cells or queues them
+// for the exact integrator; the fallback pass cools those and finishes the
+// dt reduction.  Queues: capacity nx ny nz; counts zero between steps.
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
                                Clock* clk, const void* img, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,
                                const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
-                               cudaStream_t s);
-// The same two passes for several meshes in two launches: fill_cool_job
+                               unsigned* nqueue, unsigned* nqcount, cudaStream_t s);
+// The same three passes for several meshes in three launches: fill_cool_job
 // writes one mesh's arguments (cool_job_bytes() of them) into a host array
 // that is copied to the device; mesh m runs on blocks [blk0, blk0 + nblk) of
 // each pass (ranges ascending and back to back from 0, nblk between 1 and
@@ -100,7 +101,8 @@ int cool_pass_blocks(const Params& p);
 void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, double* U1, long long it_base, Clock* clk,
                    const void* img, const float norm[6], const double box[6],
                    const float* gcum, const float* gslope, unsigned long long* counts, const unsigned* cqueue,
-                   unsigned* cqcount, unsigned* queue, unsigned* qcount, int blk0, int nblk);
+                   unsigned* cqcount, unsigned* queue, unsigned* qcount, unsigned* nqueue, unsigned* nqcount,
+                   int blk0, int nblk);
 cudaError_t launch_cool_mlp_dt_batch(const void* jobs, int njobs, int nblocks, cudaStream_t s);
 
 // log10 of a small device array in place (cooling-table temperatures).

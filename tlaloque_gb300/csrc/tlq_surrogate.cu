@@ -97,16 +97,20 @@ __device__ __forceinline__ long long interior_offset(const Params& p, const Layo
   return L.at(i, j, k);
 }
 
-// Pass 1 (network): stage 2 queued the interior cells that cool (temp >=
-// the table's first temperature, cooling.f90:71).  For each, densely, 32 to
-// a warp: the network's prediction where the cell lies in the training box,
-// accepted when the residual check passes; the others go to the fallback
-// queue for the exact integrator, and so do the cells whose cooling reaches
-// the table's first temperature within the step (closed form: G_t <= 0):
-// there the reference integrator's last sub-step decides how far below that
-// temperature the cell ends.  The block maxima of the signal speeds of the
-// cells cooled here are folded into the clock's (stage 2 left out the cells
-// it queued).
+// Pass 1 (sort): stage 2 queued the interior cells that cool (temp >= the
+// table's first temperature, cooling.f90:71).  A cell whose tau is at most
+// the integrator's sub-step is cooled here by the exact integrator's single
+// exponential step; a cell inside the training box goes to the network
+// queue; the others go to the fallback queue.
+// Pass 2 (network): the network queue densely, 32 cells to a warp (a warp
+// of the sort pass holds a few network cells at most, and its matrix tiles
+// would run for all 32 rows): the prediction, accepted when the residual
+// check passes; the others go to the fallback queue, and so do the cells
+// whose cooling reaches the table's first temperature within the step
+// (closed form: G_t <= 0): there the reference integrator's last sub-step
+// decides how far below that temperature the cell ends.
+// Both passes fold the block maxima of the signal speeds of the cells they
+// cooled into the clock's (stage 2 left out the cells it queued).
 // The state the step just wrote: U1 or U0 by the clock's buffer parity (the
 // clock has not advanced yet), so that one captured launch serves both
 // parities.
@@ -128,6 +132,8 @@ struct CoolJob {
   unsigned* cqcount;
   unsigned* queue;  // cells handed to the exact integrator
   unsigned* qcount;
+  unsigned* nqueue;  // cells for the network
+  unsigned* nqcount;
   unsigned blk0, nblk;  // this mesh's blocks of each pass: [blk0, blk0 + nblk)
 };
 
@@ -157,71 +163,150 @@ __device__ __forceinline__ const CoolJob& stage_job(SmemJob& s, const CoolJob* s
   return *reinterpret_cast<const CoolJob*>(s.w);
 }
 
+// The cooling quantities of a queued cell from its state u: primitives w,
+// temperature T, whether it cools (need), and for one that does its
+// tau = Lambda n^2 dt / E_th, the network's normalised features and whether
+// they lie in the training box.  One definition for both passes.
+struct CellCool {
+  float w[5], T, tau, lam, feat[3];
+  bool need, inbox;
+};
+__device__ __forceinline__ void cell_cool(const Params& p, const SurrogateArgs& sa, const double* u, float dtf,
+                                          CellCool& c) {
+  const float gm1 = p.f_gamma - 1.0f;
+  float cf[5];
+  mixed_cell(gm1, u, 1, cf, c.w);
+  c.T = (c.w[4] / c.w[0]) * p.f_cT;
+  c.need = cools_at(p, c.T, u);
+  c.tau = 0.f;
+  c.lam = 0.f;
+  c.feat[0] = c.feat[1] = c.feat[2] = 0.f;
+  c.inbox = false;
+  if (c.need) {
+    const float nd = c.w[0] * p.f_inv_muamu;
+    const float eth = c.w[4] / gm1;
+    c.lam = cool_coef_f(p.cool, c.T);
+    c.tau = (c.lam * nd) * (nd / eth) * dtf;
+    const float f0 = log10f(nd), f1 = log10f(c.T), f2 = log10f(c.tau);
+    // inclusive, with 1e-4 dex of slack for the FP32 logarithms of cells on
+    // a face of the box (e.g. a medium at the table's first temperature)
+    constexpr float SL = 1e-4f;
+    c.inbox = f0 >= sa.box[0] - SL && f0 <= sa.box[1] + SL && f1 >= sa.box[2] - SL && f1 <= sa.box[3] + SL &&
+              f2 >= sa.box[4] - SL && f2 <= sa.box[5] + SL;
+    c.feat[0] = (f0 - sa.norm[0]) / sa.norm[1];
+    c.feat[1] = (f1 - sa.norm[2]) / sa.norm[3];
+    c.feat[2] = (f2 - sa.norm[4]) / sa.norm[5];
+  }
+}
+
+// Warp-aggregated append of cell index v to a queue.
+__device__ __forceinline__ void warp_append(bool take, unsigned v, unsigned* queue, unsigned* count) {
+  const unsigned qm = __ballot_sync(0xffffffffu, take);
+  if (!qm) return;
+  const int lane = threadIdx.x & 31;
+  unsigned basei = 0;
+  if (lane == 0) basei = atomicAdd(count, (unsigned)__popc(qm));
+  basei = __shfl_sync(0xffffffffu, basei, 0);
+  if (take) queue[basei + __popc(qm & ((1u << lane) - 1u))] = v;
+}
+
+// The counters of the three outcomes (network, fallback, single step).
+__device__ __forceinline__ void add_counts(const SurrogateArgs& sa, unsigned long long used, unsigned long long fell,
+                                           unsigned long long one) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    used += __shfl_xor_sync(0xffffffffu, used, off);
+    fell += __shfl_xor_sync(0xffffffffu, fell, off);
+    one += __shfl_xor_sync(0xffffffffu, one, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (used) atomicAdd(&sa.counts[0], used);
+    if (fell) atomicAdd(&sa.counts[1], fell);
+    if (one) atomicAdd(&sa.counts[2], one);
+  }
+}
+
+__device__ void cool_sort_mesh(const CoolJob& j, double* red, unsigned nblocks, unsigned bid) {
+  const Params& p = j.p;
+  const Layout& L = j.L;
+  const Clock* clk = j.clk;
+  if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
+  const long long n = (long long)*j.cqcount;
+  if ((long long)bid * CT >= n) return;  // no queued cell for this block: nothing to fold
+  double* __restrict__ U = step_output(j.U0, j.U1, clk, j.it_base);
+  const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
+  const float dtf = d2f(clk->dt);
+  float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+  unsigned long long fell = 0, one = 0;
+  // warp-uniform trip count (the appends are warp-wide)
+  for (long long base = (long long)bid * CT; base < n; base += (long long)nblocks * CT) {
+    const long long q = base + threadIdx.x;
+    const bool valid = q < n;
+    long long o = 0;
+    unsigned cidx = 0;
+    double u[5] = {1.0, 0.0, 0.0, 0.0, 1.0};
+    if (valid) {
+      cidx = j.cqueue[q];
+      o = interior_offset(p, L, cidx);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
+    }
+    CellCool c;
+    cell_cool(p, j.sa, u, dtf, c);
+    const bool need = valid && c.need;
+    // tau at most the integrator's sub-step: the exact integrator is a single
+    // exponential step, cheaper and exact, and the network has nothing to gain
+    const bool single = need && !(c.tau > p.f_cool_sub_frac);
+    if (single) {
+      cool_cell_f(p, p.f_cT, p.f_inv_muamu, gm1, c.w, u[4], dtf, u);
+      U[4 * L.plane + o] = u[4];
+      speeds_max(c.w, gf, m0, m1, m2);
+    }
+    const bool net = need && !single && c.inbox;
+    const bool fb = need && !single && !c.inbox;
+    warp_append(net, cidx, j.nqueue, j.nqcount);
+    warp_append(fb, cidx, j.queue, j.qcount);
+    fell += fb ? 1 : 0;
+    one += single ? 1 : 0;
+  }
+  add_counts(j.sa, 0, fell, one);
+  cfl_contribute<CT>(f2d(m0), f2d(m1), f2d(m2), j.clk, red);
+}
+
 __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red, unsigned nblocks, unsigned bid) {
   const Params& p = j.p;
   const Layout& L = j.L;
   const Clock* clk = j.clk;
   const SurrogateArgs& sa = j.sa;
-  const unsigned* __restrict__ cqueue = j.cqueue;
-  unsigned* __restrict__ queue = j.queue;
-  unsigned* qcount = j.qcount;
-  if (!(clk->t < clk->tfin)) return;  // the step did not run (mainHD.f90:61)
-  const long long n = (long long)*j.cqcount;
-  if ((long long)bid * CT >= n) return;  // no queued cell for this block: no weights, nothing to fold
+  if (!(clk->t < clk->tfin)) return;
+  const long long n = (long long)*j.nqcount;
+  if ((long long)bid * CT >= n) return;  // no network cell for this block: no weights, nothing to fold
   double* __restrict__ U = step_output(j.U0, j.U1, clk, j.it_base);
   mlp::copy_weights<CT>(sa.img, W);
   __syncthreads();
   const CoolTable& tab = p.cool;
   const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
-  const float cT = p.f_cT;
-  const float inv_muamu = p.f_inv_muamu;
   const float dtf = d2f(clk->dt);
   const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-  unsigned long long used = 0, fell = 0, one = 0;
+  unsigned long long used = 0, fell = 0;
   // warp-uniform trip count: the network's tiles need all 32 lanes
   for (long long base = (long long)bid * CT; base < n; base += (long long)nblocks * CT) {
     const long long q = base + threadIdx.x;
     const bool valid = q < n;
-    long long o = 0, cidx = 0;
+    long long o = 0;
+    unsigned cidx = 0;
     double u[5] = {1.0, 0.0, 0.0, 0.0, 1.0};
     if (valid) {
-      cidx = cqueue[q];
+      cidx = j.nqueue[q];
       o = interior_offset(p, L, cidx);
 #pragma unroll
       for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
     }
-    float cf[5], w[5];
-    mixed_cell(gm1, u, 1, cf, w);
-    const float T = (w[4] / w[0]) * cT;
-    const bool need = valid && cools_at(p, T, u);
-    float feat[3] = {0.f, 0.f, 0.f}, tau = 0.f;
-    bool inbox = false;
-    if (need) {
-      const float nd = w[0] * inv_muamu;
-      const float eth = w[4] / gm1;
-      const float lam = cool_coef_f(tab, T);
-      tau = (lam * nd) * (nd / eth) * dtf;
-      const float f0 = log10f(nd), f1 = log10f(T), f2 = log10f(tau);
-      // inclusive, with 1e-4 dex of slack for the FP32 logarithms of cells on
-      // a face of the box (e.g. a medium at the table's first temperature)
-      constexpr float SL = 1e-4f;
-      inbox = f0 >= sa.box[0] - SL && f0 <= sa.box[1] + SL && f1 >= sa.box[2] - SL && f1 <= sa.box[3] + SL &&
-              f2 >= sa.box[4] - SL && f2 <= sa.box[5] + SL;
-      feat[0] = (f0 - sa.norm[0]) / sa.norm[1];
-      feat[1] = (f1 - sa.norm[2]) / sa.norm[3];
-      feat[2] = (f2 - sa.norm[4]) / sa.norm[5];
-    }
-    // tau at most the integrator's sub-step: the exact integrator is a single
-    // exponential step, cheaper and exact, and the network has nothing to gain
-    const bool single = need && !(tau > p.f_cool_sub_frac);
-    if (single) {
-      cool_cell_f(p, cT, inv_muamu, gm1, w, u[4], dtf, u);
-      U[4 * L.plane + o] = u[4];
-    }
-    const bool run = need && inbox && !single;
+    CellCool c;
+    cell_cool(p, sa, u, dtf, c);
     float y = 0.f;
-    if (__ballot_sync(0xffffffffu, run)) {
+    if (__ballot_sync(0xffffffffu, valid)) {
       // the warp's 32 cells as two m16 tiles (rows = lanes 0-15, 16-31)
       float yt[2][2];
 #pragma unroll 1
@@ -229,8 +314,8 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
         float xg[3], xg8[3];
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-          xg[f] = __shfl_sync(0xffffffffu, feat[f], 16 * tsel + g);
-          xg8[f] = __shfl_sync(0xffffffffu, feat[f], 16 * tsel + g + 8);
+          xg[f] = __shfl_sync(0xffffffffu, c.feat[f], 16 * tsel + g);
+          xg8[f] = __shfl_sync(0xffffffffu, c.feat[f], 16 * tsel + g + 8);
         }
         mlp::forward_tile(W, xg, xg8, g, tig, yt[tsel]);
       }
@@ -240,54 +325,44 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
       y = (lane < 16) ? (row < 8 ? a0 : a1) : (row < 8 ? b0 : b1);
     }
     bool ok = false;
-    if (run) {
-      const float lam = cool_coef_f(tab, T);
+    if (valid) {
+      const float T = c.T, tau = c.tau, lam = c.lam;
       const float Gt = g_of(tab, sa, T) - tau * T / lam;  // budget (gamma-1) n dt / k_B = tau T / Lambda(T)
       if (Gt > 0.0f) {
         const float Tint = g_inv(tab, sa, Gt);
         // the network's r: ln(T_new/T) = -(tau + tau^2 r); q = T_new/T - 1
         // without cancellation, clamped at the table's first temperature
-        const float q = fmaxf(expm1f(-(1.0f + tau * y) * tau), tab.Tf[0] / T - 1.0f);
-        ok = fabsf(T * q - (Tint - T)) <= p.f_mlp_tol * T;
+        const float qf = fmaxf(expm1f(-(1.0f + tau * y) * tau), tab.Tf[0] / T - 1.0f);
+        ok = fabsf(T * qf - (Tint - T)) <= p.f_mlp_tol * T;
         if (ok) {
-          const float dp = w[4] * q;
-          w[4] = w[4] + dp;
+          const float dp = c.w[4] * qf;
+          c.w[4] = c.w[4] + dp;
           U[4 * L.plane + o] = u[4] + f2d(dp / gm1);
         }
       }
     }
-    const bool queued = need && !ok && !single;
-    // warp-aggregated append to the fallback queue
-    const unsigned qm = __ballot_sync(0xffffffffu, queued);
-    if (qm) {
-      unsigned basei = 0;
-      if (lane == 0) basei = atomicAdd(qcount, (unsigned)__popc(qm));
-      basei = __shfl_sync(0xffffffffu, basei, 0);
-      if (queued) queue[basei + __popc(qm & ((1u << lane) - 1u))] = (unsigned)cidx;
-    }
+    const bool fb = valid && !ok;
+    warp_append(fb, cidx, j.queue, j.qcount);
     used += ok ? 1 : 0;
-    fell += queued ? 1 : 0;
-    one += single ? 1 : 0;
-    if (ok || single) speeds_max(w, gf, m0, m1, m2);
+    fell += fb ? 1 : 0;
+    if (ok) speeds_max(c.w, gf, m0, m1, m2);
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    used += __shfl_xor_sync(0xffffffffu, used, off);
-    fell += __shfl_xor_sync(0xffffffffu, fell, off);
-    one += __shfl_xor_sync(0xffffffffu, one, off);
-  }
-  if (lane == 0) {
-    atomicAdd(&sa.counts[0], used);
-    atomicAdd(&sa.counts[1], fell);
-    atomicAdd(&sa.counts[2], one);
-  }
+  add_counts(sa, used, fell, 0);
   cfl_contribute<CT>(f2d(m0), f2d(m1), f2d(m2), j.clk, red);
 }
 
-// The network pass of one mesh (jobs null: `one`) or of njobs meshes, each
-// on its own range of the grid's blocks.  One kernel, one call site: the
-// single-mesh and batched steps run the same instructions, so their FP32
-// results agree bit for bit.
+// The sort and network passes of one mesh (jobs null: `one`) or of njobs
+// meshes, each on its own range of the grid's blocks.  One kernel, one call
+// site each: the single-mesh and batched steps run the same instructions,
+// so their FP32 results agree bit for bit.
+__global__ void __launch_bounds__(CT) k_cool_sort(const __grid_constant__ CoolJob one,
+                                                  const CoolJob* __restrict__ jobs, int njobs) {
+  __shared__ double red[96];
+  __shared__ SmemJob sj;
+  const CoolJob& j = stage_job(sj, job_of_block(one, jobs, njobs, blockIdx.x));
+  cool_sort_mesh(j, red, j.nblk, blockIdx.x - j.blk0);
+}
+
 __global__ void __launch_bounds__(CT, 3) k_cool_net(const __grid_constant__ CoolJob one,
                                                  const CoolJob* __restrict__ jobs, int njobs) {
   __shared__ mlp::SmemWeights W;
@@ -325,14 +400,15 @@ __device__ void cool_fallback_mesh(const CoolJob& j, double* red, int* flag, uns
   if (*flag && threadIdx.x == 0) {
     *j.qcount = 0u;
     *j.cqcount = 0u;
+    *j.nqcount = 0u;
   }
 }
 
-// Pass 2 (fallback): the queued cells through the exact integrator (the
+// Pass 3 (fallback): the queued cells through the exact integrator (the
 // sub-cycled cooling with the run's sub-step settings), then the dt
-// reduction over the block maxima of stage 2 and both passes (the same
-// number of blocks each); the last block of a mesh empties its queues.  One
-// mesh (jobs null: `one`) or njobs meshes, as the network pass.
+// reduction over the block maxima of stage 2 and the three passes; the last
+// block of a mesh empties its queues.  One mesh (jobs null: `one`) or njobs
+// meshes, as the other passes.
 __global__ void __launch_bounds__(FT) k_cool_fallback_dt(const __grid_constant__ CoolJob one,
                                                          const CoolJob* __restrict__ jobs, int njobs) {
   __shared__ double red[96];
@@ -349,7 +425,8 @@ size_t cool_job_bytes() { return sizeof(CoolJob); }
 void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, double* U1, long long it_base, Clock* clk,
                    const void* img, const float norm[6], const double box[6],
                    const float* gcum, const float* gslope, unsigned long long* counts, const unsigned* cqueue,
-                   unsigned* cqcount, unsigned* queue, unsigned* qcount, int blk0, int nblk) {
+                   unsigned* cqcount, unsigned* queue, unsigned* qcount, unsigned* nqueue, unsigned* nqcount,
+                   int blk0, int nblk) {
   CoolJob j{};
   j.p = p;
   j.p.cooling = COOL_SUBCYCLE;  // the fallback: the sub-cycled integrator with the run's sub-step settings
@@ -370,6 +447,8 @@ void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, doub
   j.cqcount = cqcount;
   j.queue = queue;
   j.qcount = qcount;
+  j.nqueue = nqueue;
+  j.nqcount = nqcount;
   j.blk0 = (unsigned)blk0;
   j.nblk = (unsigned)nblk;
   std::memcpy(dst, &j, sizeof j);
@@ -379,13 +458,16 @@ cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, dou
                                Clock* clk, const void* img, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,
                                const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
-                               cudaStream_t s) {
+                               unsigned* nqueue, unsigned* nqcount, cudaStream_t s) {
   const int nb = pass_blocks(p);
   CoolJob j;
-  fill_cool_job(&j, p, L, U0, U1, it_base, clk, img, norm, box, gcum, gslope, counts, cqueue, cqcount, queue, qcount, 0,
-                nb);
-  k_cool_net<<<nb, CT, 0, s>>>(j, nullptr, 1);
+  fill_cool_job(&j, p, L, U0, U1, it_base, clk, img, norm, box, gcum, gslope, counts, cqueue, cqcount, queue, qcount,
+                nqueue, nqcount, 0, nb);
+  k_cool_sort<<<nb, CT, 0, s>>>(j, nullptr, 1);
   cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cool_net<<<nb, CT, 0, s>>>(j, nullptr, 1);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_cool_fallback_dt<<<nb, FT, 0, s>>>(j, nullptr, 1);
   return cudaGetLastError();
@@ -396,8 +478,11 @@ int cool_pass_blocks(const Params& p) { return pass_blocks(p); }
 cudaError_t launch_cool_mlp_dt_batch(const void* jobs, int njobs, int nblocks, cudaStream_t s) {
   const CoolJob* d = static_cast<const CoolJob*>(jobs);
   const CoolJob none{};
-  k_cool_net<<<nblocks, CT, 0, s>>>(none, d, njobs);
+  k_cool_sort<<<nblocks, CT, 0, s>>>(none, d, njobs);
   cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cool_net<<<nblocks, CT, 0, s>>>(none, d, njobs);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_cool_fallback_dt<<<nblocks, FT, 0, s>>>(none, d, njobs);
   return cudaGetLastError();
