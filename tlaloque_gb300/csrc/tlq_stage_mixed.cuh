@@ -76,16 +76,30 @@ __device__ __forceinline__ void mixed_cell(float gm1, const double* u, long long
 // cool_cell: the reference's exponential factor, its limiter and floor,
 // sub-cycled when asked).  The total energy changes by the thermal energy
 // removed, accumulated in FP64.
-__device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
-  int lo = 1, hi = t.n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (t.Tf[mid] > temp) hi = mid; else lo = mid + 1;
+// lo: the table entry the search returns (the first with T > temp, n above
+// the table), kept from the previous call as the first guess: a sub-cycled
+// cell's temperature moves little between sub-steps, and when the guess is
+// still the first entry above temp (the entry below it is not) the search is
+// skipped and the result is the same.
+__device__ __forceinline__ float cool_coef_seg(const CoolTable& t, float temp, int& lo) {
+  const bool same = lo >= 1 && lo <= t.n && !(t.Tf[lo - 1] > temp) && (lo == t.n || t.Tf[lo] > temp);
+  if (!same) {
+    lo = 1;
+    int hi = t.n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (t.Tf[mid] > temp) hi = mid; else lo = mid + 1;
+    }
   }
   if (lo >= t.n) return exp10f(t.Cf[t.n - 1]);
   const float T0 = t.logTf[lo - 1], C0 = t.Cf[lo - 1];
   const float T1 = t.logTf[lo], C1 = t.Cf[lo];
   return exp10f(__fmaf_rn((C1 - C0) / (T1 - T0), __fsub_rn(log10f(temp), T0), C0));
+}
+
+__device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
+  int lo = 0;
+  return cool_coef_seg(t, temp, lo);
 }
 
 // Whether cooling applies (temp >= the table's first temperature,
@@ -111,7 +125,8 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   if (!cools_at(p, temp, u)) return;
   const float p0 = w[4];
   float ETH = w[4] / gm1;
-  float aloss = cool_coef_f(t, temp);
+  int seg = 0;  // the table entry of the last coefficient
+  float aloss = cool_coef_seg(t, temp, seg);
   const float n = w[0] * inv_muamu;
   float ce = (aloss * n) * (n / ETH);
   int nsub = 1;
@@ -128,7 +143,7 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
       temp = (w[4] / w[0]) * cT;
       if (!(temp >= t.Tf[0])) break;  // (after a sub-step the state is no longer the stored one)
       ETH = w[4] / gm1;
-      aloss = cool_coef_f(t, temp);
+      aloss = cool_coef_seg(t, temp, seg);
       ce = (aloss * n) * (n / ETH);
     }
     float f = __expf(-ce * h);
