@@ -226,6 +226,7 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.use_p = 0;
   a.cqueue = ctx->mlp_cqueue;
   a.cqcount = ctx->mlp_qcount ? ctx->mlp_qcount + 1 : nullptr;
+  a.cool_counts = ctx->cool_counts;
   if (mixed)
     CK(launch_stage_mixed(2, ctx->tm_UPP, a, ctx->grid, ctx->stream));
   else

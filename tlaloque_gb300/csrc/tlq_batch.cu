@@ -172,6 +172,7 @@ void fill_desc(tlq_batch* b, int i) {
       a.use_p = 0;
       a.cqueue = (st == 2) ? c->mlp_cqueue : nullptr;
       a.cqcount = (st == 2 && c->mlp_qcount) ? c->mlp_qcount + 1 : nullptr;
+      a.cool_counts = (st == 2) ? c->cool_counts : nullptr;
     }
   d.it_base = c->it_base;
   d.gx = (c->cfg.nx + tlq::MTX - 1) / tlq::MTX;

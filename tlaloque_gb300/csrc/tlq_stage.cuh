@@ -47,7 +47,8 @@ struct StageArgs {
   int use_p;           // STAGE 1 with cooling: interior pressure from the P plane
   float* lapf;         // mixed form: eta * Laplacian of U (FP32, written by stage 1, read by stage 2)
   unsigned* cqueue;    // mixed form with the cooling surrogate: stage 2 queues the cells that cool
-  unsigned* cqcount;
+  unsigned* cqcount;   // (beyond a single step of the exact integrator, which it takes itself)
+  unsigned long long* cool_counts;  // [2]: the cells stage 2 cooled in a single step
 };
 
 template <class R>

@@ -335,6 +335,7 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   const int i = i0 + tx, j = j0 + ty;
   const bool cell_ok = (ty < MTY) && (i <= p.nx) && (j <= p.ny);
   float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
+  unsigned nsingle = 0;  // stage 2 with the surrogate: cells cooled in a single step
   const float cT = p.f_cT;
   const float inv_muamu = p.f_inv_muamu;
   const float etaf = p.f_eta;
@@ -441,8 +442,24 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
         float cf[5], w[5];
         mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
         if (p.cooling == COOL_MLP) {
-          // the surrogate's passes cool this cell and take its signal speeds
-          queued = cools_at(p, (w[4] / w[0]) * cT, un);
+          // A cell whose tau (Lambda n^2 dt / E_th, formed as the cooling
+          // passes form it) is at most the integrator's sub-step takes the
+          // exact integrator's single exponential step here (the passes would
+          // do the same); the passes cool the others and take their signal
+          // speeds.
+          const float T = (w[4] / w[0]) * cT;
+          if (cools_at(p, T, un)) {
+            const float nd = w[0] * inv_muamu;
+            const float eth = w[4] / gm1;
+            const float lam = cool_coef_f(p.cool, T);
+            const float tau = (lam * nd) * (nd / eth) * dtstep_f;
+            if (tau > p.f_cool_sub_frac) {
+              queued = true;
+            } else {
+              cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
+              ++nsingle;
+            }
+          }
         } else if (p.cooling != COOL_NONE) {
           cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
         }
@@ -489,6 +506,12 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       }
     }
     d0 = d1 = d2 = NAN;
+  }
+  if (STAGE == 2 && p.cooling == COOL_MLP && a.cool_counts) {
+    unsigned v = nsingle;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((tid & 31) == 0 && v) atomicAdd(&a.cool_counts[2], (unsigned long long)v);
   }
   if (STAGE == 2) {
     if (p.cooling != COOL_MLP) {
