@@ -80,12 +80,12 @@ cudaError_t launch_gather_pairs(const float* X, const float* Y, const float* Wt,
                                 float* X2, float* Y2, float* Wt2, cudaStream_t s);
 cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStream_t s);
 // Surrogate cooling + dt reduction of the mixed step (tlq_surrogate.cu).
-// Stage 2 queues the cells that cool (cqueue) and folds its block maxima
-// into the clock's; the sort pass cools the cells the exact integrator
-// takes in one step and queues the others for the network (nqueue) or the
-// exact integrator (queue); the network pass cools its cells or queues them
-// for the exact integrator; the fallback pass cools those and finishes the
-// dt reduction.  Queues: capacity nx ny nz; counts zero between steps.
+// Stage 2 cools the cells the exact integrator takes in one step, queues
+// the other cells that cool (cqueue) and folds its block maxima into the
+// clock's; the sort pass queues those for the network (nqueue) or the exact
+// integrator (queue); the network pass cools its cells or queues them for
+// the exact integrator; the fallback pass cools those and finishes the dt
+// reduction.  Queues: capacity nx ny nz; counts zero between steps.
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
                                Clock* clk, const void* img, const float norm[6], const double box[6],
                                const float* gcum, const float* gslope, unsigned long long* counts,

@@ -98,10 +98,12 @@ __device__ __forceinline__ long long interior_offset(const Params& p, const Layo
 }
 
 // Pass 1 (sort): stage 2 queued the interior cells that cool (temp >= the
-// table's first temperature, cooling.f90:71).  A cell whose tau is at most
-// the integrator's sub-step is cooled here by the exact integrator's single
-// exponential step; a cell inside the training box goes to the network
-// queue; the others go to the fallback queue.
+// table's first temperature, cooling.f90:71) beyond a single step of the
+// exact integrator (it cooled the cells whose tau is at most the
+// integrator's sub-step itself, with this pass's arithmetic).  A cell inside
+// the training box goes to the network queue, the others to the fallback
+// queue; a queued cell whose tau is at most the sub-step after all takes the
+// single exponential step here.
 // Pass 2 (network): the network queue densely, 32 cells to a warp (a warp
 // of the sort pass holds a few network cells at most, and its matrix tiles
 // would run for all 32 rows): the prediction, accepted when the residual
