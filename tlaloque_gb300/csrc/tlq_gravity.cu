@@ -15,20 +15,24 @@
 // parity test states that one condition twice), so within a half-sweep a
 // cell with s = 0 reads the new value of its x neighbour in rows of even j
 // and of its y neighbour in columns of odd i: a Gauss-Seidel order along i
-// and j.  A block walks a plane's anti-diagonals i + j = d in order, one
-// thread per i, and every other neighbour (east, north, the k planes, the
-// source) still holds its value from before the half-sweep, so those loads
-// run ahead of the sweep.  Planes are independent within a half-sweep, one
-// block each.  With the order kept and FP64 without contraction, every
+// and j.  A block walks a plane's anti-diagonals i + j = d in order, and
+// every other neighbour (east, north, the k planes, the source) still holds
+// its value from before the half-sweep.  A relax's ten half-sweeps run in one
+// cooperative launch, skewed by a few diagonals per half-sweep, each plane's
+// block checking its neighbour planes' progress (k_mg_relax_plane with the
+// plane in shared memory up to 128 cells, k_mg_relax_pipe from the level
+// arrays above; k_mg_half, one launch per half-sweep, where the planes cannot
+// all be resident).  With the order kept and FP64 without contraction, every
 // level is bit-identical to a sequential restatement; only the stopping
 // test's sum |dphi| is summed in another order (it decides only whether the
 // next V-cycle runs).
 //
-// The V-cycles are a fixed sequence of launches (31, the reference's cap),
-// each launch reading a device flag that the cycle's first kernel sets from
-// the reference's test (Dif > 10 and fewer than 31 cycles): the whole solve
-// is stream-ordered with no host round trip, so a CUDA graph captures it.
-// Levels of at most 32 cells run inside one block (one launch per cycle).
+// The reference's loop test (Dif > 10 and fewer than 31 cycles) runs on the
+// device, so the solve needs no host round trip: in a CUDA graph the
+// V-cycles are the body of a while node whose condition that test sets; run
+// directly, a fixed sequence of 31 cycle slots whose launches return once
+// the test failed.  Levels of at most 4 cells run inside one block (one
+// launch per cycle).
 //
 // Built with -fmad=false (FP64 as the restatement evaluates it).
 #include <algorithm>
