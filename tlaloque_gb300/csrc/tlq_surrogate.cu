@@ -1,11 +1,12 @@
 // tlq_surrogate.cu -- the learned cooling surrogate in the step (mixed form,
 // TLQ_COOL_MLP) and its training driver.
 //
-// In the step, stage 2 leaves cooling and the CFL reduction to
-// k_cool_mlp_dt: for each interior cell that cools (temp >= the table's
-// first temperature, cooling.f90:71), the network predicts
-// y = -ln(T_new/T)/tau from (log10 n, log10 T, log10 tau); the prediction is
-// accepted when the cell lies inside the training box and
+// In the step, stage 2 cools the cells the exact integrator takes in one
+// step and leaves the other cells that cool (temp >= the table's first
+// temperature, cooling.f90:71) and the CFL reduction to three passes
+// (k_cool_sort, k_cool_net, k_cool_fallback_dt): for a cell inside the
+// training box the network predicts y = -ln(T_new/T)/tau from
+// (log10 n, log10 T, log10 tau); the prediction is accepted when
 // |T_pred - T_int| <= 1e-3 T, T_int the closed-form solution of
 // dT/dt = -(gamma-1) n Lambda(T)/k_B for the piecewise power-law table
 // (Townsend 2009, ApJS 181, 391: exact integration of a power-law cooling
