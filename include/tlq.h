@@ -162,7 +162,8 @@ typedef struct tlq_stats {
   long long cool_fallback; /* TLQ_COOL_MLP: cell-steps handed to the exact integrator */
   double ms_cool;          /* TLQ_COOL_MLP: average device time of the timed cooling passes */
   long long cool_single;   /* TLQ_COOL_MLP: cell-steps with tau <= cool_sub_frac, cooled by the exact
-                              integrator's single exponential step (the network has nothing to gain) */
+                              integrator's single exponential step (the network has nothing to gain;
+                              stage 2 does these, so their time is in ms_stage2, not ms_cool) */
   double ms_grav;          /* self-gravity: average device time of the timed steps' two MultiGrid solves
                               (ms_stage1/ms_stage2 then time the stage kernels alone) */
 } tlq_stats;
