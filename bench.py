@@ -51,12 +51,28 @@ if ROOT not in sys.path:
 METRIC = "zone-updates/s on 1 GB300 at 256³ (mixed+surrogate vs plain FP64 at ≤1% L1 err); HBM GB/s"
 UNIT = "zone-updates/s"
 
-# FP64 operations per zone-update of the reference algorithm (add, mul, div,
-# sqrt, exp/log/pow; comparisons not counted), counted by the oracle's
-# counting build at each workload's size: python -m oracle.flops_report
-# --wind-n 256 --sedov-n 128 (one step after the first).
-FP64_FLOPS_PER_ZONE = {"wind256": 1022.8, "sedov128": 774.5, "sod": 1338.3}
-FP64_TFLOPS_NOMINAL = 1.25  # GB300 dense FP64, nominal (no measured figure on this machine)
+# FP64 operations per zone-update of the reference algorithm by kind,
+# counted by the oracle's counting build at each workload's size (one step
+# after the first): python -m oracle.flops_report --wind-n 256 --sedov-n 128.
+# cmp: comparisons (DSETP, issued on the FP64 pipe like an add).
+FP64_OPS_PER_ZONE = {
+    "wind256": {"add": 475.28, "mul": 442.29, "div": 89.98, "sqrt": 15.24, "cmp": 71.93},
+    "sedov128": {"add": 386.23, "mul": 322.22, "div": 52.77, "sqrt": 13.28, "cmp": 66.61},
+    "sod": {"add": 560.05, "mul": 648.96, "div": 109.46, "sqrt": 19.82, "cmp": 95.83},
+}
+
+
+def fp64_pipe_bound(ops: dict, rate: dict) -> dict:
+    """The plain FP64 step's compute roofline from the op counts and the FP64
+    pipe's measured rates (tlq_measure_fp64_rate): every add, multiply and
+    comparison takes one FMA slot (the FP64 kernels are built without
+    contraction), an IEEE division or square root the FMA-slot cost measured
+    for it; zone-updates/s at a fully busy pipe = FMA rate / slots."""
+    div_cost = rate["fma_per_s"] / rate["div_per_s"]
+    sqrt_cost = rate["fma_per_s"] / rate["sqrt_per_s"]
+    slots = ops["add"] + ops["mul"] + ops["cmp"] + ops["div"] * div_cost + ops["sqrt"] * sqrt_cost
+    return {"fma_slots_per_zone": slots, "div_fma_slots": div_cost, "sqrt_fma_slots": sqrt_cost,
+            "zone_updates_per_s_bound": rate["fma_per_s"] / slots}
 
 
 def load_peaks():
@@ -171,7 +187,7 @@ def cpu_oracle_rate(cfg, U0, budget_s: float, nthreads: int, min_steps: int = 2,
     """Time the oracle restatement on the host: zone-updates/s over a bounded
     number of steps of the same workload (steps until budget_s elapses)."""
     from oracle.oracle import Run
-    from tests.helpers import oracle_params
+    from oracle.oracle import params_from_config as oracle_params
     run = Run(oracle_params(cfg, nthreads=nthreads), U0)
     run.run(warm)  # first touch of the arrays (and the workload's first, heavier step)
     steps = 0
@@ -330,7 +346,7 @@ def run_reference(args, world, rank, dist):
     cfg, U0, desc = make_workload(args.workload)
     ncores = os.cpu_count() or 1
     from oracle.oracle import Run
-    from tests.helpers import oracle_params
+    from oracle.oracle import params_from_config as oracle_params
     run = Run(oracle_params(cfg, nthreads=ncores), U0)
     run.run(args.warmup)
     t0 = time.perf_counter()
@@ -454,23 +470,21 @@ def main():
     mix = measure(tlq.PREC_MIXED, args.steps, not cooling)
     forms = {"fp64": form(f64), "mixed": form(mix), "speedup_mixed_vs_fp64": mix["value"] / f64["value"],
              "mixed_vs_fp64": accuracy(mix, f64)}
-    # the plain form's bound: its HBM fraction next to its FP64-pipe occupancy
-    # (ncu --set full of the plain stage kernels on the 128^3 wind bubble: the
-    # FP64 pipe 79 % busy in both): FP64-pipe bound
+    # the plain form's bound: the FP64 pipe (measured here, with the oracle's
+    # op counts) next to its HBM fraction
     bpz64 = bytes_per_zone(cfg)
     forms["fp64"]["roofline"] = {
-        "bound": "fp64 pipe", "fp64_pipe_busy_ncu": 0.79,
         "hbm_achieved_gbs": bpz64["step"] * f64["value"] / 1e9,
         "hbm_frac": bpz64["step"] * f64["value"] / 1e9 / peak}
-    flops = FP64_FLOPS_PER_ZONE.get(args.workload)
-    if flops:
-        # oracle-counted arithmetic at the nominal FP64 rate; divisions and
-        # square roots take several FP64 instructions each, so the pipe
-        # occupancy above is the tighter measure
+    ops = FP64_OPS_PER_ZONE.get(args.workload)
+    if ops:
+        rate = tlq.measure_fp64_rate(local)
+        b = fp64_pipe_bound(ops, rate)
         forms["fp64"]["roofline"].update({
-            "fp64_flops_per_zone": flops, "fp64_tflops_achieved": flops * f64["value"] / 1e12,
-            "fp64_tflops_peak_nominal": FP64_TFLOPS_NOMINAL,
-            "fp64_flop_frac_nominal": flops * f64["value"] / 1e12 / FP64_TFLOPS_NOMINAL})
+            "bound": "fp64 pipe", "fp64_ops_per_zone": ops,
+            "fp64_rate_measured": {**rate, "how": "tlq_measure_fp64_rate: independent FMA / IEEE divide / IEEE "
+                                                 "square-root chains, 8 blocks of 256 threads per SM, CUDA events"},
+            **b, "fp64_pipe_frac": f64["value"] / b["zone_updates_per_s_bound"]})
     head = mix
     surrogate = None
     if cooling:

@@ -185,11 +185,11 @@ int tlq_set_stream(tlq_ctx* ctx, void* cuda_stream);
 int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* log10_lambda, int n);
 /* Spherical winds applied in borders (user/user.f90:57-70).  Copied. */
 int tlq_set_winds(tlq_ctx* ctx, const tlq_wind* winds, int n);
-/* Point masses (x, y, z, M per mass) of pgravity (source/pointsource_gravity.f90:12-39);
- * the reference hard-codes M = 8 Msun (:23).  Copied; enables the source term. */
 /* Plane winds imposed with the spherical ones in every ghost fill of the
  * step (user_boundaries), at most 6; n = 0 clears them. */
 int tlq_set_plane_winds(tlq_ctx* ctx, const tlq_plane_wind* w, int n);
+/* Point masses (x, y, z, M per mass) of pgravity (source/pointsource_gravity.f90:12-39);
+ * the reference hard-codes M = 8 Msun (:23).  Copied; enables the source term. */
 int tlq_set_point_masses(tlq_ctx* ctx, const double* xyzm, int n);
 
 /* State transfer.  tlq_upload takes U after borders(U,1) (mainHD.f90:38) and
@@ -345,6 +345,13 @@ int tlq_gravity_source(tlq_ctx* ctx, const double* UPrim, const double* phi, dou
  * the V-cycles run (may be NULL).  Needs self_gravity in the configuration. */
 int tlq_multigrid(tlq_ctx* ctx, const double* U, double* phi, int it, int* cycles);
 
+/* ---- Measurement (no counterpart in the reference) ----------------------
+ * Throughput of the FP64 pipe of `device`, for the plain FP64 step's
+ * roofline: independent dependency chains of FMA, IEEE division and IEEE
+ * square root, timed with CUDA events (~10 ms of GPU time).  Writes the
+ * operations per second of each. */
+int tlq_measure_fp64_rate(int device, double* fma_per_s, double* div_per_s, double* sqrt_per_s);
+
 /* ---- Allocation-free entry point (no counterpart in the reference) ------
  * time_step for callers that cannot allocate device memory: hosts whose GPU
  * memory belongs to an arena or pool allocator (an extra cudaMalloc can fail
@@ -358,12 +365,20 @@ int tlq_multigrid(tlq_ctx* ctx, const double* U, double* phi, int it, int* cycle
  * library (72 bytes, held by every GPU that loads the library until exit),
  * so:
  *   - NULL pointers and sizes < 1 are rejected with TLQ_ERR_ARG;
- *   - the first call on a device looks the variable's device address up on
- *     that device (cudaGetSymbolAddress); make that first call outside any
+ *   - every call asks the runtime for the variable's device address in the
+ *     current context (cudaGetSymbolAddress, which allocates nothing); the
+ *     first call in a context (on a device, or after cudaDeviceReset) loads
+ *     the library's module there, so make that first call outside any
  *     stream capture;
  *   - all calls share the variable: calls that overlap on the GPU
  *     (concurrent streams, several host threads) race and must be serialised
- *     by the caller. */
+ *     by the caller.
+ * The return code covers the arguments and the launch only: it is known
+ * before the kernel runs.  A state whose signal speeds give no finite,
+ * positive dt (a NaN or infinite speed, or all speeds zero) is not reported
+ * by the return code, as tlq_time_step reports it with TLQ_ERR_NONFINITE_DT:
+ * the dt written to *d_dt is then NaN, infinite or not positive, so check
+ * that it is finite and > 0 before using it. */
 int tlq_time_step_noalloc(const double* d_uprim, int nx, int ny, int nz, double dx, double dy, double dz,
                           double gamma, double cfl, double* d_dt, void* cuda_stream);
 

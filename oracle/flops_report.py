@@ -18,7 +18,7 @@ import sys
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 from oracle.oracle import count_flops  # noqa: E402
-from tests.helpers import oracle_params  # noqa: E402
+from oracle.oracle import params_from_config as oracle_params  # noqa: E402
 from tlaloque_gb300 import problems  # noqa: E402
 
 

@@ -18,7 +18,9 @@ import sys
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py /path/to/tlaloque  (the reference source tree)")
+ref = sys.argv[1]
 out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_solutions.npz")
 
 sod = np.loadtxt(os.path.join(ref, "solutions", "sod_e1rpex.out"))

@@ -27,7 +27,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle.oracle import Run  # noqa: E402
-from tests.helpers import oracle_params  # noqa: E402
+from oracle.oracle import params_from_config as oracle_params  # noqa: E402
 from tlaloque_gb300 import analysis, problems  # noqa: E402
 
 

@@ -188,3 +188,39 @@ def test_self_gravity_config_checks(gpu_lib):
     # periodic boundaries are fine with the serial build's (zero) faces
     with tlq.Context(tlq.Config(**{**cfg.__dict__, "bc": (tlq.BC_PERIODIC,) * 6, "grav_bc": tlq.GBC_ZERO})):
         pass
+
+
+def test_multigrid_wait_runs_out(gpu_lib, monkeypatch):
+    """Failure detection of the pipelined relax, without a fault: with the
+    limit of its neighbour-progress polls set to 0 (TLQ_MG_WAIT_LIMIT when
+    the context is created) a plane gives up at its first wait that is not
+    already satisfied, sets the abort flag, and every block leaves the
+    launch.  The calls return (nothing hangs) with TLQ_ERR_TIMEOUT -- the
+    per-routine MultiGrid and a step, whose solves run inside its graph --
+    and a context created afterwards with the default limit steps normally,
+    bit-identical to the oracle."""
+    cfg, U0 = problems.gravitating_cloud(32, grav_bc=tlq.GBC_ZERO)
+    monkeypatch.setenv("TLQ_MG_WAIT_LIMIT", "0")
+    U = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U, 1)
+        with pytest.raises(tlq.TlqError) as err:
+            ctx.multigrid(U, np.zeros(cfg.phi_shape, order="F"), 0)
+        assert err.value.code == tlq.ERR_TIMEOUT
+        ctx.upload(U)
+        with pytest.raises(tlq.TlqError) as err:
+            ctx.step()
+        assert err.value.code == tlq.ERR_TIMEOUT
+    monkeypatch.delenv("TLQ_MG_WAIT_LIMIT")
+    run = Run(oracle_params(cfg), U0)
+    run.run(2)
+    U = U0.copy(order="F")
+    with tlq.Context(cfg) as ctx:
+        ctx.borders(U, 1)
+        ctx.upload(U)
+        ctx.step()
+        t, it, dt = ctx.step()
+        Ug, _ = ctx.state()
+    m = face_ghost_mask(cfg)
+    assert (t, it, dt) == (run.t, run.it, run.dt)
+    np.testing.assert_array_equal(Ug[:, m], run.U[:, m])

@@ -35,6 +35,7 @@ UNITS = [
     ("tlq_batch.cu", ["--use_fast_math"]),
     ("tlq_output.cu", []),
     ("tlq_gravity.cu", ["-fmad=false"]),
+    ("tlq_probe.cu", []),
 ]
 
 

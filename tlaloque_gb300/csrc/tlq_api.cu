@@ -906,6 +906,7 @@ int tlq_multigrid(tlq_ctx* ctx, const double* U, double* phi, int it, int* cycle
   int st = 0;
   rc = mg_cycles_and_status(ctx, cycles, &st);
   if (rc) return rc;
+  if (st & MG_ST_TIMEOUT) return fail(ctx, TLQ_ERR_TIMEOUT, "a pipelined relax gave up waiting for a neighbouring plane");
   if (st) return fail(ctx, TLQ_ERR_TIMEOUT, "coarsest-level solve did not converge");
   return TLQ_OK;
 }

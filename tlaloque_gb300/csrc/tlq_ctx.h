@@ -117,5 +117,9 @@ cudaError_t mg_alloc(tlq_ctx* ctx);
 void mg_free(tlq_ctx* ctx);
 cudaError_t enqueue_multigrid_soa(tlq_ctx* ctx, const double* U, cudaStream_t s);
 cudaError_t enqueue_multigrid_aos(tlq_ctx* ctx, const double* U, const Clock* clk, cudaStream_t s);
+// status bits: the coarsest-level solve did not converge; a pipelined relax
+// gave up waiting for a neighbouring plane (its bounded wait ran out)
+constexpr int MG_ST_SOLVE = 1;
+constexpr int MG_ST_TIMEOUT = 2;
 int mg_cycles_and_status(tlq_ctx* ctx, int* cycles, int* status);
 }  // namespace tlq

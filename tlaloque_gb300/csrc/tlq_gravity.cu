@@ -54,9 +54,10 @@ constexpr int MG_PF = 4;            // diagonal steps the smoother's loads run a
 constexpr int MG_MOM_THREADS = 256;
 constexpr int MG_MOM_BLOCKS = 152 * 2;
 constexpr int MG_SOLVE_LIMIT = 100000;  // coarsest-level Gauss-Seidel passes before giving up
-constexpr long long MG_WAIT_LIMIT = 1LL << 24;  // polls of a neighbour's progress before giving up (~1 s)
-constexpr int MG_ST_SOLVE = 1;
-constexpr int MG_ST_TIMEOUT = 2;
+// Polls of a neighbour's progress before a pipelined relax gives up (~1 s);
+// TLQ_MG_WAIT_LIMIT in the environment of tlq_create overrides it (a short
+// limit lets a test make the wait run out and check the error status).
+constexpr long long MG_WAIT_LIMIT = 1LL << 24;
 
 struct MgLevel {
   int n;
@@ -76,6 +77,7 @@ struct MgCtl {
   double part[2 * 1024];             // per-plane partial sums of the last pass's |change|
   int abort;                         // a pipelined relax gave up waiting (sticky for the call)
   int prog[1026];                    // pipelined relax: plane k's last finished diagonal, hs*(2n+2) + d
+  long long wait_limit;              // polls of a neighbour's progress before giving up (set at allocation)
 };
 
 __host__ __device__ __forceinline__ long long mgi(int n, int i, int j, int k) {
@@ -519,7 +521,7 @@ __device__ bool mg_wait(MgCtl* c, int k, int n, int need, int* s_ok) {
       if (nb < 1 || nb > n) continue;
       long long tries = 0;
       while (prog[nb] < need) {
-        if (*abort || ++tries > MG_WAIT_LIMIT) {
+        if (*abort || ++tries > c->wait_limit) {
           ok = 0;
           break;
         }
@@ -1139,6 +1141,15 @@ cudaError_t mg_alloc(tlq_ctx* ctx) {
   e = cudaMalloc(&ctx->mg_ctl, sizeof(MgCtl));
   if (e != cudaSuccess) return e;
   e = cudaMemset(ctx->mg_ctl, 0, sizeof(MgCtl));
+  if (e != cudaSuccess) return e;
+  long long limit = MG_WAIT_LIMIT;
+  if (const char* env = std::getenv("TLQ_MG_WAIT_LIMIT")) {
+    char* end = nullptr;
+    const long long v = std::strtoll(env, &end, 10);
+    if (end != env && *end == '\0' && v >= 0) limit = v;
+  }
+  e = cudaMemcpy(reinterpret_cast<char*>(ctx->mg_ctl) + offsetof(MgCtl, wait_limit), &limit, sizeof limit,
+                 cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return e;
   e = cudaMalloc(&ctx->mg_mom, (size_t)MG_MOM_BLOCKS * 25 * sizeof(double));
   if (e != cudaSuccess) return e;

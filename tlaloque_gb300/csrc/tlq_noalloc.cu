@@ -12,8 +12,6 @@
 // The ticket and the running maxima of the single-pass CFL reduction live in
 // one file-scope device variable (below, 72 bytes), which every GPU that
 // loads the library holds until the process exits.
-#include <mutex>
-
 #include "../../include/tlq.h"
 #include "tlq_internal.h"
 
@@ -23,14 +21,13 @@ namespace {
 constexpr int NA_THREADS = 256;
 constexpr int NA_CELLS_PER_THREAD = 16;
 constexpr long long NA_CELLS_PER_BLOCK = (long long)NA_THREADS * NA_CELLS_PER_THREAD;  // 4096
-constexpr int NA_MAX_DEVICES = 64;
 
 struct NoAllocScratch {
   Clock clk;  // the reduction's ticket and maxima (zero before a call) and its dt
 };
 
 // The scratch, per device.  Host code must not use this name as an address;
-// it looks the device address up once per device (below).
+// it asks the runtime for the device address (below).
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 // Same reduction as the per-routine time_step kernel, with a fixed chunk of
@@ -61,24 +58,17 @@ __global__ void __launch_bounds__(NA_THREADS) k_time_step_noalloc(Params p, Aos 
   if (flag && threadIdx.x == 0) *d_dt = sc->clk.dt;
 }
 
-std::mutex g_mutex;
-void* g_scratch_addr[NA_MAX_DEVICES] = {};
-
-// Set-up, once per device with that device current: the device address of
-// the scratch array.
+// The device address of the scratch variable in the current context, looked
+// up on every call (the lookup allocates nothing).  A cached address could
+// outlive its module: after cudaDeviceReset the library's module is loaded
+// again, and a caller that makes another driver context current sees another
+// copy of the variable.  The first lookup in a context loads the module
+// there; make that first call outside any stream capture.
 cudaError_t scratch_address(NoAllocScratch** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* ptr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = ptr;
-  }
-  *out = static_cast<NoAllocScratch*>(g_scratch_addr[dev]);
+  *out = static_cast<NoAllocScratch*>(ptr);
   return cudaSuccess;
 }
 
@@ -104,6 +94,10 @@ extern "C" int tlq_time_step_noalloc(const double* d_uprim, int nx, int ny, int 
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   // The scratch keeps the previous call's contents: ticket and maxima must start at 0.
   if (cudaMemsetAsync(&sc->clk, 0, sizeof(Clock), s) != cudaSuccess) return TLQ_ERR_CUDA;
-  k_time_step_noalloc<<<nblocks, NA_THREADS, 0, s>>>(p, A, d_uprim, sc, d_dt);
-  return cudaGetLastError() == cudaSuccess ? TLQ_OK : TLQ_ERR_CUDA;
+  // The launch's own status (cudaGetLastError would also consume an error
+  // left by the caller's earlier launches and report it as this call's).
+  void* args[] = {&p, (void*)&A, (void*)&d_uprim, &sc, &d_dt};
+  const cudaError_t e = cudaLaunchKernel((const void*)k_time_step_noalloc, dim3((unsigned)nblocks), dim3(NA_THREADS),
+                                         args, 0, s);
+  return e == cudaSuccess ? TLQ_OK : TLQ_ERR_CUDA;
 }

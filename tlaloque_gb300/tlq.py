@@ -33,7 +33,7 @@ EXPORTS = (
     "tlq_run_until", "tlq_synchronize", "tlq_stats_get", "tlq_enable_timing", "tlq_last_error", "tlq_status_string",
     "tlq_conserved_sums", "tlq_calc_prims", "tlq_time_step", "tlq_fluxes", "tlq_godunov", "tlq_borders",
     "tlq_viscous_step", "tlq_cooling", "tlq_point_potential", "tlq_gravity_source", "tlq_multigrid",
-    "tlq_time_step_noalloc",
+    "tlq_time_step_noalloc", "tlq_measure_fp64_rate",
     "tlq_surrogate_opts_default", "tlq_train_cooling_surrogate", "tlq_get_cooling_surrogate",
     "tlq_set_cooling_surrogate", "tlq_cooling_pairs", "tlq_mlp_loss_grad", "tlq_mlp_infer",
     "tlq_set_tfin", "tlq_set_plane_winds", "tlq_output", "tlq_output_wait", "tlq_set_tiling", "tlq_get_tiling", "tlq_autotune", "tlq_batch_create", "tlq_batch_destroy", "tlq_batch_size", "tlq_batch_member",
@@ -101,6 +101,17 @@ class CSurrogateReport(C.Structure):
 _lib = None
 
 
+def measure_fp64_rate(device: int = 0) -> dict:
+    """FP64 pipe throughput of `device` (tlq_measure_fp64_rate): FMA,
+    IEEE division and square root operations per second."""
+    L = load_library()
+    f, d, q = C.c_double(), C.c_double(), C.c_double()
+    rc = L.tlq_measure_fp64_rate(device, C.byref(f), C.byref(d), C.byref(q))
+    if rc != OK:
+        raise TlqError(rc, "measure_fp64_rate")
+    return {"fma_per_s": f.value, "div_per_s": d.value, "sqrt_per_s": q.value}
+
+
 def load_library(path: str = LIB_PATH):
     """Load libtlq.so; raises if it has not been built (no fallback)."""
     global _lib
@@ -114,6 +125,7 @@ def load_library(path: str = LIB_PATH):
     I = C.c_int
     sig = {
         "tlq_config_default": (None, [C.POINTER(CConfig)]),
+        "tlq_measure_fp64_rate": (I, [I, D, D, D]),
         "tlq_create": (I, [C.POINTER(CConfig), C.POINTER(V)]),
         "tlq_destroy": (I, [V]),
         "tlq_set_tfin": (I, [V, C.c_double]),
