@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libtlq_oracle.so")
 BC_OUTFLOW, BC_REFLECTIVE, BC_PERIODIC, BC_INFLOW = 1, 2, 3, 4
 LIM_NONE, LIM_VANLEER, LIM_MINMOD, LIM_UMIST, LIM_WOODWARD, LIM_SUPERBEE = 1, 2, 3, 4, 5, 6
 SOLVER_HLLC, SOLVER_HLL = 0, 1
-COOL_NONE, COOL_REF, COOL_SUBCYCLE = 0, 1, 2
+COOL_NONE, COOL_REF, COOL_SUBCYCLE, COOL_EXACT = 0, 1, 2, 4
 GBC_ZERO, GBC_MULTIPOLE = 0, 1
 
 
@@ -96,6 +96,9 @@ def lib():
         L.tlqo_gravity_source.argtypes = [P, D, D, D]
         L.tlqo_cool_coef.restype = C.c_double
         L.tlqo_cool_coef.argtypes = [P, C.c_double]
+        L.tlqo_cool_gcum.argtypes = [P, D]
+        L.tlqo_cool_exact_T.restype = C.c_double
+        L.tlqo_cool_exact_T.argtypes = [P, D, C.c_double, C.c_double, C.c_double]
         L.tlqo_mg_levels.restype = C.c_int
         L.tlqo_mg_levels.argtypes = [P]
         L.tlqo_mg_work_len.restype = C.c_long
@@ -296,6 +299,13 @@ class Oracle:
 
     def cooling(self, W, U, dt):
         self.L.tlqo_cooling(self._pp, _ptr(W), _ptr(U), float(dt))
+
+    def cool_exact_T(self, T: float, tau: float) -> float:
+        """The exact integrator's temperature after a step of cooling number
+        tau from T (>= the table's first temperature)."""
+        g = np.zeros(self.p.cool_T.size)
+        self.L.tlqo_cool_gcum(self._pp, _ptr(g))
+        return self.L.tlqo_cool_exact_T(self._pp, _ptr(g), float(T), self.cool_coef(T), float(tau))
 
     def cool_coef(self, T: float) -> float:
         return self.L.tlqo_cool_coef(self._pp, float(T))

@@ -497,13 +497,74 @@ double tlqo_cool_coef(const tlqo_params* p, double temp) {
 /* calcTemp, source/cooling.f90:146-159. */
 static inline double calc_temp(const tlqo_params* p, const double* w) { return w[4] * p->mu0 * AMU / (w[0] * KB); }
 
+/* The exact integrator (TLQO_COOL_EXACT): the temperature after a step of a
+ * cell at temp >= T_0 with cooling number tau = ce*dt (ce = Lambda n^2 / E_th
+ * at temp).  At fixed density, d ln T/dt = -ce(T) is the sub-cycled
+ * integrator's equation in the limit of infinitely many sub-steps; with
+ * E_th proportional to T it is dT/dt = -kappa Lambda(T), and find_coef's
+ * interpolation, log-linear between nodes (cooling.f90:133-140), makes
+ * Lambda(T) = Lambda_i (T/T_i)^s_i on [T_i, T_{i+1}) a power law, held at
+ * the last node's value above the table.  So the step integrates in closed
+ * form (exact integration of a piecewise power-law cooling function:
+ * Townsend 2009, ApJS 181, 391): with a = 1 - s_i, the cell stays in its
+ * segment while tau <= (1 - (T_i/T)^a)/a and then ends at
+ * T (1 - a tau)^(1/a); otherwise it crosses T_i with budget
+ * B = (tau - tau_i) T/Lambda(T) left of G(T) = int_{T_0}^{T} dT'/Lambda,
+ * and ends in the segment j whose nodes bracket G(T_i) - B (G at the nodes
+ * is a running sum of the segments' integrals).  Below T_0 nothing cools, so
+ * a cell that reaches T_0 within the step ends there. */
+static double seg_slope(const tlqo_params* p, int i) {
+  if (i >= p->ncool - 1) return 0.0; /* held above the last node */
+  return (p->coolC[i + 1] - p->coolC[i]) / (log10(p->coolT[i + 1]) - log10(p->coolT[i]));
+}
+
+/* x^(1/a) of the power-law solution, its a -> 0 limit exp(lim_arg). */
+static double pow_inv(double base, double a, double lim_arg) {
+  return fabs(a) < 1e-9 ? exp(lim_arg) : pow(base, 1.0 / a);
+}
+
+/* G at the nodes: gcum[0] = 0, gcum[i+1] = gcum[i] + int_{T_i}^{T_{i+1}} dT/Lambda. */
+void tlqo_cool_gcum(const tlqo_params* p, double* gcum) {
+  gcum[0] = 0.0;
+  for (int i = 0; i + 1 < p->ncool; ++i) {
+    const double a = 1.0 - seg_slope(p, i), Li = pow(10.0, p->coolC[i]), r = p->coolT[i + 1] / p->coolT[i];
+    const double g = fabs(a) < 1e-9 ? (p->coolT[i] / Li) * log(r) : (p->coolT[i] / Li) * (pow(r, a) - 1.0) / a;
+    gcum[i + 1] = gcum[i] + g;
+  }
+}
+
+double tlqo_cool_exact_T(const tlqo_params* p, const double* gcum, double temp, double lam, double tau) {
+  const int n = p->ncool;
+  int lo = 1, hi = n; /* first node above temp (n: none), as find_coef */
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (p->coolT[mid] > temp) hi = mid; else lo = mid + 1;
+  }
+  const int i = lo - 1; /* segment: T_i <= temp < T_{i+1}, n-1 at or above the last node */
+  const double a = 1.0 - seg_slope(p, i), xlo = p->coolT[i] / temp;
+  const double tau_i = fabs(a) < 1e-9 ? -log(xlo) : (1.0 - pow(xlo, a)) / a;
+  if (tau <= tau_i) return temp * pow_inv(1.0 - a * tau, a, -tau);
+  const double G = gcum[i] - (tau - tau_i) * temp / lam; /* G(T_new) */
+  if (!(G > 0.0)) return p->coolT[0];
+  lo = 0;
+  hi = i - 1; /* last node j < i with gcum[j] <= G */
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (gcum[mid] <= G) lo = mid; else hi = mid - 1;
+  }
+  const int j = lo;
+  const double aj = 1.0 - seg_slope(p, j), q = (G - gcum[j]) * pow(10.0, p->coolC[j]) / p->coolT[j];
+  return p->coolT[j] * pow_inv(1.0 + aj * q, aj, q);
+}
+
 /* One cell of apply_cooling (source/cooling.f90:64-117) and, for
  * TLQO_COOL_SUBCYCLE, the sub-cycled integrator built on it: the step is cut
  * into nsub equal sub-steps, nsub = ceil(ce*dt / cool_sub_frac) clamped to
  * [1, cool_max_sub], each applying the reference's exponential factor with
  * its limiter and floor at the current temperature.  nsub = 1 is exactly the
- * reference formula. */
-static void cool_cell(const tlqo_params* p, double* w, double* u, double dt) {
+ * reference formula.  TLQO_COOL_EXACT takes the same single step when
+ * ce*dt <= cool_sub_frac and the closed form above otherwise. */
+static void cool_cell(const tlqo_params* p, const double* gcum, double* w, double* u, double dt) {
   const double g = p->gamma;
   const double Tmin = p->coolT[0];
   double temp = calc_temp(p, w);
@@ -514,6 +575,13 @@ static void cool_cell(const tlqo_params* p, double* w, double* u, double dt) {
   double aloss = tlqo_cool_coef(p, temp);
   double numdens = w[0] / (p->mu0 * AMU);
   double ce = aloss * (numdens * numdens) / ETH;
+  if (p->cooling == TLQO_COOL_EXACT && ce * dt > p->cool_sub_frac) {
+    const double Tn = tlqo_cool_exact_T(p, gcum, temp, aloss, ce * dt);
+    w[4] = w[4] * (Tn / temp);
+    ETH = w[4] / (g - 1);
+    u[4] = EK + ETH;
+    return;
+  }
   int nsub = 1;
   if (p->cooling == TLQO_COOL_SUBCYCLE && ce * dt > p->cool_sub_frac) {
     double q = ceil(ce * dt / p->cool_sub_frac);
@@ -546,10 +614,16 @@ static void cool_cell(const tlqo_params* p, double* w, double* u, double dt) {
 
 void tlqo_cooling(const tlqo_params* p, double* W, double* U, double dt) {
   if (p->cooling == TLQO_COOL_NONE || p->ncool < 2) return;
+  double* gcum = NULL;
+  if (p->cooling == TLQO_COOL_EXACT) {
+    gcum = (double*)malloc((size_t)p->ncool * sizeof(double));
+    tlqo_cool_gcum(p, gcum);
+  }
 #pragma omp parallel for collapse(2) num_threads(NTHREADS(p))
   for (int k = 1; k <= p->nz; ++k)
     for (int j = 1; j <= p->ny; ++j)
-      for (int i = 1; i <= p->nx; ++i) cool_cell(p, W + IX(p, 0, i, j, k), U + IX(p, 0, i, j, k), dt);
+      for (int i = 1; i <= p->nx; ++i) cool_cell(p, gcum, W + IX(p, 0, i, j, k), U + IX(p, 0, i, j, k), dt);
+  free(gcum);
 }
 
 /* ---------------------------------------------------------------------------

@@ -32,7 +32,10 @@ enum { TLQO_LIM_NONE = 1, TLQO_LIM_VANLEER = 2, TLQO_LIM_MINMOD = 3, TLQO_LIM_UM
 enum { TLQO_SOLVER_HLLC = 0, TLQO_SOLVER_HLL = 1 };
 /* Cooling modes: none; the reference's single exponential step
  * (source/cooling.f90:47-119); the sub-cycled integrator built on it. */
-enum { TLQO_COOL_NONE = 0, TLQO_COOL_REF = 1, TLQO_COOL_SUBCYCLE = 2 };
+/* TLQO_COOL_EXACT: the sub-cycled integrator in the limit of infinitely many
+ * sub-steps (closed form), with the reference formula for a cell that needs
+ * one sub-step.  Value 4 (3 is the GPU's learned surrogate). */
+enum { TLQO_COOL_NONE = 0, TLQO_COOL_REF = 1, TLQO_COOL_SUBCYCLE = 2, TLQO_COOL_EXACT = 4 };
 
 /* Boundary values of the self-gravity potential on the mesh faces: the
  * reference's serial build never imposes any (they stay 0), its MPI build on
@@ -105,6 +108,11 @@ long tlqo_mg_work_len(const tlqo_params* p);
 int tlqo_multigrid(const tlqo_params* p, const double* U, double* phi, int it, double* work);
 void tlqo_gravity_source(const tlqo_params* p, const double* UPrim, const double* phi, double* S);
 double tlqo_cool_coef(const tlqo_params* p, double temp);
+/* The exact integrator's closed form (TLQO_COOL_EXACT): G at the table
+ * nodes (ncool values), and the temperature after a step of cooling number
+ * tau of a cell at temp >= T_0 whose find_coef value is lam. */
+void tlqo_cool_gcum(const tlqo_params* p, double* gcum);
+double tlqo_cool_exact_T(const tlqo_params* p, const double* gcum, double temp, double lam, double tau);
 
 /* Whole-run state of the main loop, source/mainHD.f90:22-100. */
 typedef struct tlqo_state {

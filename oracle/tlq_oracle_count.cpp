@@ -12,7 +12,7 @@
  *
  * Categories: add (+ and - of two values, including compound assignment),
  * mul, div, sqrt, cmp (<, >, <=, >=, ==, !=, which also carry the Fortran
- * MIN/MAX), trans (exp, log10, pow, and the self-gravity's acos, atan2, cos,
+ * MIN/MAX), trans (exp, log, log10, pow, and the self-gravity's acos, atan2, cos,
  * sin, Gamma); fabs, copysign, ceil, negation and conversions are not
  * counted.
  */
@@ -54,6 +54,7 @@ inline bool operator!=(fd a, fd b) { ++g_cmp; return a.v != b.v; }
 inline fd sqrt(fd a) { ++g_sqrt; return fd(std::sqrt(a.v)); }
 inline fd exp(fd a) { ++g_trans; return fd(std::exp(a.v)); }
 inline fd log10(fd a) { ++g_trans; return fd(std::log10(a.v)); }
+inline fd log(fd a) { ++g_trans; return fd(std::log(a.v)); }
 inline fd pow(fd a, fd b) { ++g_trans; return fd(std::pow(a.v, b.v)); }
 inline fd fabs(fd a) { return fd(std::fabs(a.v)); }
 inline fd copysign(fd a, fd b) { return fd(std::copysign(a.v, b.v)); }
