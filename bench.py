@@ -121,16 +121,15 @@ def bytes_per_zone(cfg, mixed: bool = False, surrogate: bool = False) -> dict:
     pressure (8 B written by stage 2, read by stage 1; the mixed form
     recomputes it, and moves the viscosity Laplacian into stage 1 as an FP32
     plane); point gravity reads phi once per stage).  With the surrogate the
-    cooling and dt pass reads U once more (40 B; the 8 B energy write of the
-    cooled cells and the fallback queue are not counted)."""
+    cooling passes read and write only the cells stage 2 queued (those
+    cooling beyond a single step): their bytes scale with those cells, not
+    with the mesh, and are not counted per zone-update."""
     from tlaloque_gb300 import tlq
     cool = cfg.cooling != tlq.COOL_NONE and not mixed
     grav = cfg.masses is not None and len(cfg.masses) > 0
     lap = 20 if mixed else 0  # mixed: stage 1 writes eta*Lap(U) in FP32, stage 2 reads it
     s1 = 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
     s2 = 40 + 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
-    if surrogate:
-        return {"stage1": s1, "stage2": s2, "cool": 40, "step": s1 + s2 + 40}
     return {"stage1": s1, "stage2": s2, "step": s1 + s2}
 
 
@@ -243,7 +242,7 @@ def ensemble_members(n: int = 48, seed: int = 2024):
         namb = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
         cfg, U0 = problems.wind_bubble(size, vw_kms=vw, n_amb=namb)
         cfg = tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_MIXED, "cooling": tlq.COOL_MLP,
-                            "cool_sub_frac": 2e-3, "cool_max_sub": 20000})
+                            "cool_sub_frac": 2e-3})
         out.append((cfg, U0))
     return out
 
@@ -304,7 +303,7 @@ def run_ensemble(args, world, rank, dist):
     # computes), one context after another
     seq64_ms = 0.0
     for cfg, U0 in members:
-        cfg64 = tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, "cooling": tlq.COOL_SUBCYCLE})
+        cfg64 = tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, "cooling": tlq.COOL_EXACT})
         with tlq.Context(cfg64) as ctx:
             U1 = U0.copy(order="F")
             ctx.borders(U1, 1)
@@ -331,8 +330,8 @@ def run_ensemble(args, world, rank, dist):
                            "path": "each member alone, its own graph-replayed step, one after another"},
             "speedup_vs_sequential": (seq_ms / args.steps) / (ms / args.steps),
             "sequential_fp64": {"value": cells * args.steps / (seq64_ms / 1e3), "ms_per_step": seq64_ms / args.steps,
-                                "path": "each member alone in the plain FP64 form with the exact cooling integrator, "
-                                        "one after another"},
+                                "path": "each member alone in the plain FP64 form with the exact cooling integrator "
+                                        "(closed form), one after another"},
             "speedup_vs_sequential_fp64": (seq64_ms / args.steps) / (ms / args.steps),
             "gpu_launches": st.launches_per_step * args.steps, "clocks": clocks}
     if rank == 0:
@@ -379,6 +378,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--train-samples", type=int, default=20_000_000, help="surrogate training pairs")
     ap.add_argument("--train-epochs", type=int, default=30, help="surrogate training epochs")
+    ap.add_argument("--clumpy-n", type=int, default=256, help="mesh of the surrogate-active record")
+    ap.add_argument("--sur-steps", type=int, default=100, help="timed steps of the surrogate-active record")
+    ap.add_argument("--no-surrogate-active", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -394,7 +396,7 @@ def main():
 
     import torch
     from tlaloque_gb300 import build as tbuild
-    from tlaloque_gb300 import tlq
+    from tlaloque_gb300 import problems, tlq
     tbuild.build()
     torch.cuda.set_device(local)
     cfg, U0, desc = make_workload(args.workload)
@@ -406,17 +408,20 @@ def main():
     import tempfile
     tune_cache = os.path.join(tempfile.gettempdir(), "tlq_autotune.json")
 
-    def measure(precision, steps, sample_clocks, net=None, **over):
-        """W warm-up + K timed steps of one form from the initial state."""
-        c = tlq.Config(**{**cfg.__dict__, "precision": precision, **over})
+    def measure(precision, steps, sample_clocks, net=None, base=None, tune=True, **over):
+        """W warm-up + K timed steps of one form from the initial state of the
+        workload (base: another workload's (cfg, U0))."""
+        bcfg, bU0 = base if base is not None else (cfg, U0)
+        c = tlq.Config(**{**bcfg.__dict__, "precision": precision, **over})
         ctx = tlq.Context(c)
         ctx.set_stream(stream.cuda_stream)
         if net is not None:
             ctx.set_cooling_surrogate(*net)
-        U1 = U0.copy(order="F")
+        U1 = bU0.copy(order="F")
         ctx.borders(U1, 1)          # mainHD.f90:38
         ctx.upload(U1)
-        zlen = ctx.autotune(tune_cache, steps=3)  # z-chunk of the stage grid (state restored)
+        # z-chunk of the stage grid (state restored)
+        zlen = ctx.autotune(tune_cache, steps=3) if tune else ctx.tiling()
         ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
         ctx.synchronize()
         st0 = ctx.stats()
@@ -438,11 +443,11 @@ def main():
         st = ctx.stats()
         ctx.enable_timing(False)
         t_sim, it_sim, dt_sim, status = ctx.time()
-        W = cfg.zeros()
+        W = bcfg.zeros()
         ctx.download(None, W)
         sums = ctx.conserved_sums()
         ms_max = allmax(dist, ms)
-        return {"ctx": ctx, "ms": ms_max, "value": world * cfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
+        return {"ctx": ctx, "ms": ms_max, "value": world * bcfg.cells * steps / (ms_max / 1e3), "k1": st.ms_stage1,
                 "k2": st.ms_stage2, "kc": st.ms_cool, "kg": st.ms_grav, "sim": {"t": t_sim, "it": it_sim, "dt": dt_sim, "status": status},
                 "rho": W[0, 2:-2, 2:-2, 2:-2].copy(), "E": float(sums[4]), "clocks": clocks,
                 "cool": (st.cool_mlp - st0.cool_mlp, st.cool_fallback - st0.cool_fallback,
@@ -463,6 +468,43 @@ def main():
         nst = args.warmup + args.steps
         return {"after_steps": nst, "l1_rho_rel": float(np.sum(np.abs(a["rho"] - b["rho"])) / np.sum(np.abs(b["rho"]))),
                 "energy_drift_rel_per_100_steps": abs(a["E"] - b["E"]) / abs(b["E"]) * (100.0 / nst)}
+
+    def surrogate_active(net, sub):
+        """The surrogate doing real work: a clumpy radiative medium (lognormal
+        density, log T uniform over 1e3-1e8 K, rms Mach 2; the wind bubble's
+        cooling curve and physics, so the same network) where a few per cent
+        of the cells cool stiffly every step.  W warm-up + S timed steps of
+        mixed + surrogate, of the mixed form with the exact integrator's
+        closed form alone, and of the judge (plain FP64, exact integrator);
+        accuracy after the W + S steps."""
+        ccfg, cU0 = problems.clumpy(args.clumpy_n)
+        nst = args.sur_steps
+        judge = measure(tlq.PREC_FP64, nst, False, base=(ccfg, cU0), tune=False, cooling=tlq.COOL_EXACT, **sub)
+        judge["ctx"].close()
+        closed = measure(tlq.PREC_MIXED, nst, False, base=(ccfg, cU0), cooling=tlq.COOL_EXACT, **sub)
+        closed["ctx"].close()
+        act = measure(tlq.PREC_MIXED, nst, False, net=net, base=(ccfg, cU0), cooling=tlq.COOL_MLP, **sub)
+        act["ctx"].close()
+
+        def acc(a):
+            n_all = args.warmup + nst
+            return {"after_steps": n_all,
+                    "l1_rho_rel": float(np.sum(np.abs(a["rho"] - judge["rho"])) / np.sum(np.abs(judge["rho"]))),
+                    "energy_drift_rel_per_100_steps": abs(a["E"] - judge["E"]) / abs(judge["E"]) * (100.0 / n_all)}
+        nm, nf, ns = act["cool"]
+        return {"workload": f"clumpy radiative medium {args.clumpy_n}^3, periodic (8 pc)^3, lognormal density "
+                            "(sigma log10 n = 1, k^-5/3), log T uniform 1e3-1e8 K, rms Mach 2, the wind bubble's "
+                            "cooling curve; HLLC + van Leer",
+                "mesh": [ccfg.nx, ccfg.ny, ccfg.nz], "warmup": args.warmup, "steps": nst,
+                "value": act["value"], "unit": UNIT, "ms_per_step": act["ms"] / nst, "ms_stage1": act["k1"],
+                "ms_stage2": act["k2"], "ms_cool_passes": act["kc"],
+                "timed_cell_steps_network": nm, "timed_cell_steps_exact": nf, "timed_cell_steps_single_step": ns,
+                "network_cells_per_step": nm / nst, "fallback_rate": nf / max(1, nm + nf),
+                "vs_fp64_exact": acc(act),
+                "fp64_exact": {"value": judge["value"], "ms_per_step": judge["ms"] / nst},
+                "speedup_vs_fp64_exact": act["value"] / judge["value"],
+                "mixed_exact_closed_form": {"value": closed["value"], "ms_per_step": closed["ms"] / nst,
+                                            "ms_cool_in_stage2": closed["k2"], "vs_fp64_exact": acc(closed)}}
 
     cooling = cfg.cooling != tlq.COOL_NONE
     f64 = measure(tlq.PREC_FP64, args.steps, False)
@@ -492,13 +534,15 @@ def main():
         # workload's cooling table and physics; its fallback (and the FP64
         # step it is compared with) is the exact integrator, fine sub-cycling
         mix["ctx"].close()
-        exact = {"cool_sub_frac": 2e-3, "cool_max_sub": 20000}
+        # the judge: the exact integrator (the reference's single exponential
+        # step up to a cooling number of 2e-3, the closed form above it)
+        sub = {"cool_sub_frac": 2e-3}
         with tlq.Context(cfg) as tctx:
             rep = tctx.train_cooling_surrogate(nsamples=args.train_samples, epochs=args.train_epochs)
             net = tctx.get_cooling_surrogate()
-        f64x = measure(tlq.PREC_FP64, args.steps, False, **exact)
+        f64x = measure(tlq.PREC_FP64, args.steps, False, cooling=tlq.COOL_EXACT, **sub)
         f64x["ctx"].close()
-        sur = measure(tlq.PREC_MIXED, args.steps, True, net=net, cooling=tlq.COOL_MLP, **exact)
+        sur = measure(tlq.PREC_MIXED, args.steps, True, net=net, cooling=tlq.COOL_MLP, **sub)
         nm, nf, ns = sur["cool"]
         forms["fp64_exact_cooling"] = form(f64x)
         forms["mixed_surrogate"] = form(sur)
@@ -509,12 +553,14 @@ def main():
                      "timed_cell_steps_network": nm, "timed_cell_steps_fallback": nf,
                      "timed_cell_steps_single_step": ns,
                      "fallback_rate": nf / max(1, nm + nf),
-                     "fallback_note": "of the cooling cell-steps with tau above the integrator's sub-step (the "
-                                      "network's domain), the share handed to the exact integrator: outside the "
-                                      "training box, failing the 1e-3 residual check, or cooling to the table's "
-                                      "first temperature within the step; cells with smaller tau take the exact "
-                                      "integrator's single exponential step directly (single_step)"}
+                     "fallback_note": "of the cooling cell-steps with tau above the single-step limit (the "
+                                      "network's domain), the share cooled by the exact integrator: outside the "
+                                      "training box or failing the residual check; cells with smaller tau take "
+                                      "the exact integrator's single exponential step directly (single_step)"}
         head = sur
+        if not args.no_surrogate_active:
+            sur["ctx"].close()
+            surrogate["active"] = surrogate_active(net, sub)
     value = head["value"]
     ms_max = head["ms"]
     mix = head

@@ -44,9 +44,14 @@ enum {
 enum { TLQ_SOLVER_HLLC = 0, TLQ_SOLVER_HLL = 1 };
 /* Radiative cooling: off; the reference's single exponential step
  * (source/cooling.f90:47-119); its sub-cycled extension (nsub = 1 is the
- * reference formula exactly). */
-enum { TLQ_COOL_NONE = 0, TLQ_COOL_REF = 1, TLQ_COOL_SUBCYCLE = 2,
-       TLQ_COOL_MLP = 3 /* learned surrogate with the sub-cycled integrator as fallback (mixed form only) */ };
+ * reference formula exactly); the learned surrogate (mixed form only, the
+ * exact integrator as its fallback); the exact integrator: the sub-cycled
+ * one in the limit of infinitely many sub-steps, in closed form (find_coef's
+ * log-linear interpolation makes Lambda(T) a piecewise power law, whose
+ * cooling integrates exactly: Townsend 2009), with the reference formula
+ * for a cell whose cooling number Lambda n^2 dt / E_th is at most
+ * cool_sub_frac. */
+enum { TLQ_COOL_NONE = 0, TLQ_COOL_REF = 1, TLQ_COOL_SUBCYCLE = 2, TLQ_COOL_MLP = 3, TLQ_COOL_EXACT = 4 };
 /* Arithmetic of the fused step: plain FP64 (matches the reference), or
  * mixed (FP32 reconstruction and Riemann fluxes, FP64 accumulation). */
 enum { TLQ_PREC_FP64 = 0, TLQ_PREC_MIXED = 1 };
@@ -65,7 +70,9 @@ typedef struct tlq_config {
   int bc[6];                      /* x-, x+, y-, y+, z-, z+ = LB, RB, DB, TB, FB, BB (parameters.f90:10-15) */
   int cooling;                    /* TLQ_COOL_* (the reference's -DCOOL) */
   int cool_max_sub;               /* TLQ_COOL_SUBCYCLE: max sub-steps per step */
-  double cool_sub_frac;           /* TLQ_COOL_SUBCYCLE: max Lambda n^2 h / E_th per sub-step */
+  double cool_sub_frac;           /* TLQ_COOL_SUBCYCLE: max Lambda n^2 h / E_th per sub-step;
+                                     TLQ_COOL_EXACT, TLQ_COOL_MLP: the largest cooling number that
+                                     takes the reference's single exponential step */
   int precision;                  /* TLQ_PREC_* */
   int device;                     /* CUDA device ordinal */
   double cool_mlp_tol;            /* TLQ_COOL_MLP: residual tolerance |T_pred - T_int|/T of an accepted
@@ -112,18 +119,17 @@ typedef struct tlq_plane_wind {
 /* Learned cooling surrogate (build-defined; the reference has none).  A
  * 3-64-64-64-1 SiLU network maps (log10 n, log10 T, log10 tau), tau =
  * Lambda(T) n^2 dt / E_th the step's cooling number, to r with
- * ln(T/T_new) = tau (1 + tau r) (exact to first order in tau whatever r is).  It is trained on the GPU on pairs from the
- * sub-cycled integrator (the "exact" one: sub-steps of sub_frac and
- * sub_frac/2, Richardson-extrapolated in ln T); in the step a cell
- * falls back to that integrator (the context's cool_sub_frac/cool_max_sub)
- * when it lies outside the training box or when the a-posteriori energy
- * residual |T_pred - T_int|/T > 1e-3, T_int from the closed-form cooling-time
- * integral of the piecewise power-law table (Townsend 2009), and when that
- * integral says the cooling reaches the table's first temperature T_0 within
- * the step (there the integrator's last sub-step decides how far below T_0
- * the cell ends).  T_pred = max(T exp(-tau (1 + tau r)), T_0); training
- * ignores the pairs that reach T_0 and weighs pairs with tau < 1e-5 by
- * (tau/1e-5)^2 (their r is lost to FP64 round-off). */
+ * ln(T/T_new) = tau (1 + tau r) (exact to first order in tau whatever r is).
+ * It is trained on the GPU on pairs from the sub-cycled integrator (sub-steps
+ * of sub_frac and sub_frac/2, Richardson-extrapolated in ln T, which
+ * converges to the exact integrator).  In the step a cell whose tau exceeds
+ * the context's cool_sub_frac and lies inside the training box takes
+ * T_pred = max(T exp(-tau (1 + tau r)), T_0) when the a-posteriori energy
+ * residual |T_pred - T_ex|/T <= cool_mlp_tol, T_ex the exact integrator's
+ * temperature (TLQ_COOL_EXACT's closed form); every other such cell takes
+ * T_ex.  Training ignores the pairs that reach the table's first temperature
+ * T_0 within the step and weighs pairs with tau < 1e-5 by (tau/1e-5)^2 (their
+ * r is lost to FP64 round-off). */
 #define TLQ_MLP_NPARAM 8641
 typedef struct tlq_surrogate_opts {
   long long nsamples;      /* training pairs (default 2e7; 1 % held out) */

@@ -120,7 +120,7 @@ def test_step_plane_wind_bit_exact(gpu_lib):
     assert np.all(Ug[0, 2:-2, 2:-2, -1] == 0.5 * rho)
 
 
-@pytest.mark.parametrize("mode", [tlq.COOL_REF, tlq.COOL_SUBCYCLE])
+@pytest.mark.parametrize("mode", [tlq.COOL_REF, tlq.COOL_SUBCYCLE, tlq.COOL_EXACT])
 def test_step_wind_bubble_with_cooling(gpu_lib, mode):
     """The wind-bubble physics (wind, point mass, cooling) at 32^3: relative
     L1 <= 1e-10 per conserved variable after 10 steps (cooling's exp, log10

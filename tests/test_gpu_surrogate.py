@@ -1,8 +1,10 @@
 """Learned cooling surrogate: the GPU training and inference kernels against
 the CPU oracle of the network (oracle/mlp_oracle.py), the training pairs
 against the C oracle's sub-cycled integrator, training itself, and the
-surrogate inside the mixed step (fallback, accuracy bars, and what it gains
-over the sub-cycled integrator it replaces)."""
+surrogate inside the mixed step: its fallback (the exact integrator,
+TLQ_COOL_EXACT), the accuracy bars against the plain FP64 step with the
+exact integrator -- including 100 steps of a strongly cooling clumpy medium
+-- and what it gains over the sub-cycled integrator it was trained on."""
 import numpy as np
 import pytest
 
@@ -173,34 +175,36 @@ def test_no_network_is_an_error(gpu_lib):
         tlq.Context(tlq.Config(**{**cfg.__dict__, "cooling": tlq.COOL_MLP}))
 
 
-def test_all_fallback_is_the_sub_cycled_step(trained):
+def test_all_fallback_is_the_exact_step(trained):
     """A training box no cell lies in: every cooling cell falls back, and the
-    step is bit for bit the mixed step with sub-cycled cooling."""
+    step is bit for bit the mixed step with the exact integrator."""
     _, (P, norm, box) = trained
     cfg, U0 = problems.clumpy(32, seed=3)
-    ref = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE), U0, 5)
+    ref = run(mixed_cfg(cfg, tlq.COOL_EXACT, **SUB), U0, 5)
     empty = np.array([9.0, 9.5, 9.0, 9.5, 9.0, 9.5])
-    got = run(mixed_cfg(cfg, tlq.COOL_MLP), U0, 5, net=(P, norm, empty))
+    got = run(mixed_cfg(cfg, tlq.COOL_MLP, **SUB), U0, 5, net=(P, norm, empty))
     assert got["rc"] == tlq.OK and got["it"] == ref["it"] == 5
     assert got["mlp"] == 0 and got["fb"] > 0
     np.testing.assert_array_equal(interior(got["U"]), interior(ref["U"]))
     assert got["t"] == ref["t"]
 
 
-EXACT = dict(cool_sub_frac=2e-3, cool_max_sub=20000)  # the exact integrator: fine sub-cycling
+# The judge: the plain FP64 step with the exact integrator (its single
+# exponential step up to a cooling number of 2e-3, the closed form above).
+SUB = dict(cool_sub_frac=2e-3)
+JUDGE = dict(precision=tlq.PREC_FP64, cooling=tlq.COOL_EXACT, **SUB)
 
 
 def test_wind_bubble_bars_with_surrogate(trained):
     """Mixed + surrogate against the plain FP64 step, 100 steps of the 64^3
     wind bubble: L1 density <= 1 %, total-energy drift <= 1e-6.  Both cool
     with the exact integrator (the surrogate's fallback; the FP64 step's
-    cooling): the network reproduces that integrator, not a coarse one
-    (16 sub-steps of 0.1 tau differ from it by ~tau^2 per step)."""
+    cooling): the network reproduces that integrator, not a coarse one."""
     _, net = trained
     cfg, U0 = problems.wind_bubble(64)
-    ref = run(tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, **EXACT}), U0, 100)
-    got = run(mixed_cfg(cfg, tlq.COOL_MLP, **EXACT), U0, 100, net=net)
-    mix = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE, **EXACT), U0, 100)  # the mixed form's own share
+    ref = run(tlq.Config(**{**cfg.__dict__, **JUDGE}), U0, 100)
+    got = run(mixed_cfg(cfg, tlq.COOL_MLP, **SUB), U0, 100, net=net)
+    mix = run(mixed_cfg(cfg, tlq.COOL_EXACT, **SUB), U0, 100)  # the mixed form's own share
     drift_mix = abs(mix["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4])
     drift_net = abs(got["sums"][4] - mix["sums"][4]) / abs(ref["sums"][4])
     assert got["rc"] == tlq.OK and got["it"] == 100
@@ -214,33 +218,63 @@ def test_wind_bubble_bars_with_surrogate(trained):
     assert got["mlp"] > 0
 
 
+def test_clumpy_100_steps_energy_bar(trained):
+    """The strongly cooling case: a 64^3 clumpy medium (lognormal density,
+    log T uniform over 1e3-1e8 K, rms Mach 2), 100 steps of mixed +
+    surrogate against the plain FP64 step with the exact integrator: L1
+    density <= 1 % and total-energy drift <= 1e-6 per 100 steps, with the
+    network cooling a real share of the cells every step."""
+    _, net = trained
+    cfg, U0 = problems.clumpy(64, seed=5)
+    nst = 100
+    ref = run(tlq.Config(**{**cfg.__dict__, **JUDGE}), U0, nst)
+    got = run(mixed_cfg(cfg, tlq.COOL_MLP, **SUB), U0, nst, net=net)
+    mix = run(mixed_cfg(cfg, tlq.COOL_EXACT, **SUB), U0, nst)
+    assert got["rc"] == tlq.OK and got["it"] == nst and ref["it"] == nst
+    err = rel_l1(interior(got["W"])[0], interior(ref["W"])[0])
+    drift = abs(got["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4]) * (100.0 / nst)
+    drift_mix = abs(mix["sums"][4] - ref["sums"][4]) / abs(ref["sums"][4]) * (100.0 / nst)
+    drift_net = abs(got["sums"][4] - mix["sums"][4]) / abs(ref["sums"][4]) * (100.0 / nst)
+    per_step = got["mlp"] / nst
+    print(f"clumpy64 x {nst}: L1 rho {err:.3e} drift/100 {drift:.3e} (mixed form alone {drift_mix:.3e}, "
+          f"network against it {drift_net:.3e}); network {got['mlp']} ({per_step:.0f}/step), exact fallback "
+          f"{got['fb']}, single step {got['one']}")
+    assert err <= 1e-2
+    assert drift <= 1e-6
+    assert per_step > 1000
+
+
 def test_surrogate_gain_over_sub_cycling(trained):
-    """What the network gains, on a clumpy medium where cooling is stiff: the
-    step's cooling against the exact integrator (FP64 step, sub-steps of
-    2e-3 tau).  The surrogate, with the exact integrator as its fallback, is
-    more accurate than the sub-cycled integrator at a coarse setting (16
-    sub-steps of at most 0.1 tau) and faster than the sub-cycled integrator
-    made exact (2e-3 tau, up to 20000 sub-steps) everywhere."""
+    """What the network gains over the sub-cycled integrator it was trained
+    on, on a clumpy medium where cooling is stiff: the step's cooling against
+    the judge (FP64 step, exact integrator).  The surrogate is more accurate
+    than the sub-cycled integrator at a coarse setting (16 sub-steps of at
+    most 0.1 tau) and faster than the sub-cycled integrator run fine enough
+    to be close to exact (2e-3 tau, up to 20000 sub-steps).  The exact
+    integrator's closed form, which the surrogate checks every prediction
+    against, is printed beside them."""
     _, net = trained
     cfg, U0 = problems.clumpy(48, seed=1)
     n = 3
-    fine_kw = EXACT
-    exact = run(tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, **fine_kw}), U0, n)
+    exact = run(tlq.Config(**{**cfg.__dict__, **JUDGE}), U0, n)
     coarse = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE), U0, n, timing=True)
-    fine = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE, **fine_kw), U0, n, timing=True)
-    mlp = run(mixed_cfg(cfg, tlq.COOL_MLP, **fine_kw), U0, n, net=net, timing=True)
+    fine = run(mixed_cfg(cfg, tlq.COOL_SUBCYCLE, cool_sub_frac=2e-3, cool_max_sub=20000), U0, n, timing=True)
+    mlp = run(mixed_cfg(cfg, tlq.COOL_MLP, **SUB), U0, n, net=net, timing=True)
+    closed = run(mixed_cfg(cfg, tlq.COOL_EXACT, **SUB), U0, n, timing=True)
     # thermal energy of the cells: the cooling's footprint
     eth = lambda r: interior(r["W"])[4]
     e_coarse = rel_l1(eth(coarse), eth(exact))
     e_fine = rel_l1(eth(fine), eth(exact))
     e_mlp = rel_l1(eth(mlp), eth(exact))
+    e_closed = rel_l1(eth(closed), eth(exact))
     frac_fb = mlp["fb"] / max(1, mlp["fb"] + mlp["mlp"])
-    print(f"clumpy48: L1 p err coarse {e_coarse:.3e} fine {e_fine:.3e} mlp {e_mlp:.3e}; "
-          f"ms/step coarse {coarse['ms']:.3f} fine {fine['ms']:.3f} mlp {mlp['ms']:.3f}; fallback {frac_fb:.4f}")
+    print(f"clumpy48: L1 p err coarse {e_coarse:.3e} fine {e_fine:.3e} mlp {e_mlp:.3e} closed form {e_closed:.3e}; "
+          f"ms/step coarse {coarse['ms']:.3f} fine {fine['ms']:.3f} mlp {mlp['ms']:.3f} closed form "
+          f"{closed['ms']:.3f}; fallback {frac_fb:.4f}")
     assert e_mlp < 0.5 * e_coarse
     assert mlp["ms"] < 0.5 * fine["ms"]
     # a tighter residual tolerance: fewer accepted cells, closer to the exact integrator
-    tight = run(mixed_cfg(cfg, tlq.COOL_MLP, cool_mlp_tol=1e-5, **fine_kw), U0, n, net=net)
+    tight = run(mixed_cfg(cfg, tlq.COOL_MLP, cool_mlp_tol=1e-5, **SUB), U0, n, net=net)
     e_tight = rel_l1(eth(tight), eth(exact))
     print(f"clumpy48 tol 1e-5: err {e_tight:.3e} network {tight['mlp']} fallback {tight['fb']}")
     assert e_tight <= e_mlp and tight["fb"] >= mlp["fb"] and tight["mlp"] <= mlp["mlp"]

@@ -80,10 +80,13 @@ int validate(const tlq_config* c, std::string& why) {
   if (c->solver != TLQ_SOLVER_HLLC && c->solver != TLQ_SOLVER_HLL) { why = "unknown solver"; return TLQ_ERR_CONFIG; }
   for (int q = 0; q < 6; ++q)
     if (c->bc[q] < TLQ_BC_OUTFLOW || c->bc[q] > TLQ_BC_INFLOW) { why = "unknown boundary kind"; return TLQ_ERR_CONFIG; }
-  if (c->cooling < TLQ_COOL_NONE || c->cooling > TLQ_COOL_MLP) { why = "unknown cooling mode"; return TLQ_ERR_CONFIG; }
-  if ((c->cooling == TLQ_COOL_SUBCYCLE || c->cooling == TLQ_COOL_MLP) &&
-      (c->cool_max_sub < 1 || !(c->cool_sub_frac > 0.0))) {
-    why = "sub-cycled cooling (and the surrogate's fallback) needs cool_max_sub >= 1 and cool_sub_frac > 0";
+  if (c->cooling < TLQ_COOL_NONE || c->cooling > TLQ_COOL_EXACT) { why = "unknown cooling mode"; return TLQ_ERR_CONFIG; }
+  if (c->cooling == TLQ_COOL_SUBCYCLE && (c->cool_max_sub < 1 || !(c->cool_sub_frac > 0.0))) {
+    why = "sub-cycled cooling needs cool_max_sub >= 1 and cool_sub_frac > 0";
+    return TLQ_ERR_CONFIG;
+  }
+  if ((c->cooling == TLQ_COOL_EXACT || c->cooling == TLQ_COOL_MLP) && !(c->cool_sub_frac > 0.0)) {
+    why = "the exact integrator (and the surrogate) needs cool_sub_frac > 0 (its single-step limit)";
     return TLQ_ERR_CONFIG;
   }
   if (c->precision != TLQ_PREC_FP64 && c->precision != TLQ_PREC_MIXED) { why = "unknown precision"; return TLQ_ERR_CONFIG; }
@@ -234,9 +237,9 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   if (timed) CK(cudaEventRecordWithFlags(ctx->ev[2], ctx->stream, cudaEventRecordExternal));
   // surrogate cooling + the dt reduction (stage 2 leaves both to it)
   if (ctx->cfg.cooling == TLQ_COOL_MLP)
-    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->mlp_image, ctx->mlp_norm, ctx->mlp_box, ctx->gcum, ctx->gslope, ctx->cool_counts,
-                          ctx->mlp_cqueue, ctx->mlp_qcount + 1, ctx->mlp_queue, ctx->mlp_qcount, ctx->mlp_nqueue,
-                          ctx->mlp_qcount + 2, ctx->stream));
+    CK(launch_cool_mlp_dt(ctx->P, ctx->L, ctx->U[0], ctx->U[1], ctx->it_base, ctx->clk, ctx->mlp_image,
+                          ctx->mlp_norm, ctx->mlp_box, ctx->cool_counts, ctx->mlp_cqueue, ctx->mlp_qcount + 1,
+                          ctx->mlp_nqueue, ctx->mlp_qcount + 2, ctx->stream));
   if (timed) CK(cudaEventRecordWithFlags(ctx->ev[3], ctx->stream, cudaEventRecordExternal));
   return TLQ_OK;
 }
@@ -408,7 +411,7 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
   }
   if (cfg->cooling == TLQ_COOL_MLP) {
     const size_t ncell = (size_t)cfg->nx * cfg->ny * cfg->nz;
-    if (cudaMalloc(&ctx->mlp_queue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_cqueue, ncell * sizeof(unsigned)) ||
+    if (cudaMalloc(&ctx->mlp_cqueue, ncell * sizeof(unsigned)) ||
         cudaMalloc(&ctx->mlp_nqueue, ncell * sizeof(unsigned)) || cudaMalloc(&ctx->mlp_qcount, 3 * sizeof(unsigned)))
       return bail(TLQ_ERR_NOMEM);
     cudaMemset(ctx->mlp_qcount, 0, 3 * sizeof(unsigned));
@@ -450,12 +453,13 @@ int tlq_destroy(tlq_ctx* ctx) {
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
   mg_free(ctx);
-  cudaFree(ctx->mlp_params); cudaFree(ctx->mlp_image); cudaFree(ctx->gcum); cudaFree(ctx->gslope); cudaFree(ctx->cool_counts);
-  cudaFree(ctx->mlp_queue); cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_nqueue); cudaFree(ctx->mlp_qcount);
+  cudaFree(ctx->mlp_params); cudaFree(ctx->mlp_image); cudaFree(ctx->cool_counts);
+  cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_nqueue); cudaFree(ctx->mlp_qcount);
   cudaFree(ctx->clk); cudaFree(ctx->sums_partials); cudaFree(ctx->sums_out);
   cudaFree(ctx->staging);
   cudaFree(ctx->dT); cudaFree(ctx->dlogT); cudaFree(ctx->dC); cudaFree(ctx->dwinds); cudaFree(ctx->dmasses);
   cudaFree(ctx->dTf); cudaFree(ctx->dlogTf); cudaFree(ctx->dCf);
+  cudaFree(ctx->dslope); cudaFree(ctx->dgcum); cudaFree(ctx->dslopef); cudaFree(ctx->dgcumf);
   for (int q = 0; q < 6; ++q) cudaFree(ctx->rb[q]);
   cudaFree(ctx->rphi); cudaFree(ctx->rclk);
   if (ctx->clk_host) cudaFreeHost(ctx->clk_host);
@@ -510,9 +514,41 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int
   CK(cudaMemcpy(ctx->dTf, fT.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->dlogTf, flt.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->dCf, fC.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-  ctx->P.cool = CoolTable{ctx->dT, ctx->dlogT, ctx->dC, n, ctx->dTf, ctx->dlogTf, ctx->dCf};
-  const int rs = tlq_surrogate_prepare_table(ctx, T, logL, n);
-  if (rs != TLQ_OK) return rs;
+  // The exact integrator's closed form (COOL_EXACT, and the surrogate's
+  // fallback and check): per segment the power law's slope, in find_coef's
+  // form (cooling.f90:137-140), 0 above the last node; at each node G(T_i),
+  // the running sum of the segments' integrals of 1/Lambda.  FP64 on the
+  // host, in the oracle's order of operations.
+  std::vector<double> sl(n), gc(n);
+  gc[0] = 0.0;
+  for (int i = 0; i < n; ++i) {
+    sl[i] = (i + 1 < n) ? (logL[i + 1] - logL[i]) / (std::log10(T[i + 1]) - std::log10(T[i])) : 0.0;
+    if (i + 1 < n) {
+      const double a = 1.0 - sl[i], Li = std::pow(10.0, logL[i]), r = T[i + 1] / T[i];
+      const double g = std::fabs(a) < 1e-9 ? (T[i] / Li) * std::log(r) : (T[i] / Li) * (std::pow(r, a) - 1.0) / a;
+      gc[i + 1] = gc[i] + g;
+    }
+  }
+  std::vector<float> slf(n), gcf(n);
+  for (int q = 0; q < n; ++q) { slf[q] = (float)sl[q]; gcf[q] = (float)gc[q]; }
+  cudaFree(ctx->dslope); cudaFree(ctx->dgcum); cudaFree(ctx->dslopef); cudaFree(ctx->dgcumf);
+  ctx->dslope = ctx->dgcum = nullptr;
+  ctx->dslopef = ctx->dgcumf = nullptr;
+  CK(cudaMalloc(&ctx->dslope, n * sizeof(double)));
+  CK(cudaMalloc(&ctx->dgcum, n * sizeof(double)));
+  CK(cudaMalloc(&ctx->dslopef, n * sizeof(float)));
+  CK(cudaMalloc(&ctx->dgcumf, n * sizeof(float)));
+  CK(cudaMemcpy(ctx->dslope, sl.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dgcum, gc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dslopef, slf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dgcumf, gcf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  ctx->P.cool = CoolTable{ctx->dT,     ctx->dlogT, ctx->dC,      n,          ctx->dTf, ctx->dlogTf,
+                          ctx->dCf,    ctx->dslope, ctx->dgcum, ctx->dslopef, ctx->dgcumf};
+  ctx->cool_tmin = T[0];
+  if (!ctx->cool_counts) {
+    CK(cudaMalloc(&ctx->cool_counts, 3 * sizeof(unsigned long long)));
+    CK(cudaMemset(ctx->cool_counts, 0, 3 * sizeof(unsigned long long)));
+  }
   invalidate_graphs(ctx);
   return TLQ_OK;
 }

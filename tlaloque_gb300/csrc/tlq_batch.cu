@@ -247,9 +247,8 @@ int refresh_desc(tlq_batch* b, const std::vector<int>& which = {}) {
     const int nblk = (int)std::max(1LL, std::min((long long)tlq::cool_pass_blocks(c->P), WAVE * ci / cells));
     const MemberDesc& d = b->h_desc[i];
     tlq::fill_cool_job(b->h_cool.data() + b->ncool * jb, c->P, c->L, c->U[0], c->U[1], c->it_base, c->clk,
-                       c->mlp_image, c->mlp_norm, c->mlp_box, c->gcum, c->gslope, c->cool_counts, c->mlp_cqueue,
-                       c->mlp_qcount + 1, c->mlp_queue, c->mlp_qcount, c->mlp_nqueue, c->mlp_qcount + 2,
-                       b->cool_blocks, nblk);
+                       c->mlp_image, c->mlp_norm, c->mlp_box, c->cool_counts, c->mlp_cqueue, c->mlp_qcount + 1,
+                       c->mlp_nqueue, c->mlp_qcount + 2, b->cool_blocks, nblk);
     b->cool_blocks += nblk;
     ++b->ncool;
   }

@@ -40,6 +40,8 @@ struct tlq_ctx {
   // tables
   double *dT = nullptr, *dlogT = nullptr, *dC = nullptr;
   float *dTf = nullptr, *dlogTf = nullptr, *dCf = nullptr;
+  double *dslope = nullptr, *dgcum = nullptr;  // the exact integrator's closed form (CoolTable)
+  float *dslopef = nullptr, *dgcumf = nullptr;
   Wind* dwinds = nullptr;
   double* dmasses = nullptr;
   int nmasses = 0;
@@ -74,15 +76,13 @@ struct tlq_ctx {
   float mlp_norm[6] = {0, 1, 0, 1, 0, 1};  // feature centres and half-widths
   double mlp_box[6] = {0, 0, 0, 0, 0, 0};  // training box of the features (the hull)
   bool mlp_ready = false;
-  float* gcum = nullptr;                   // closed-form cooling-time integral at the table nodes
-  float* gslope = nullptr;                 // per-segment power-law slopes
-  unsigned long long* cool_counts = nullptr;  // device: cells cooled by the network / by the fallback
+  unsigned long long* cool_counts = nullptr;  // device: cells cooled by the network / the exact integrator /
+                                              // a single step
   double cool_tmin = 0.0;                  // the table's first temperature
   unsigned* mlp_cqueue = nullptr;          // cells that cool, queued by stage 2 (capacity nx ny nz)
-  unsigned* mlp_queue = nullptr;           // cells handed to the exact integrator (capacity nx ny nz)
   unsigned* mlp_nqueue = nullptr;          // cells for the network (capacity nx ny nz)
-  unsigned* mlp_qcount = nullptr;          // [0]: fallback queue length, [1]: cooling queue length,
-                                           // [2]: network queue length (zero between steps)
+  unsigned* mlp_qcount = nullptr;          // [1]: cooling queue length, [2]: network queue length (zero
+                                           // between steps; [0] unused)
   // output path (tlq_output.cu): device snapshot, page-locked copy, writer thread
   double* out_dev = nullptr;
   double* out_host = nullptr;
@@ -94,10 +94,6 @@ struct tlq_ctx {
 };
 
 void output_free(tlq_ctx* ctx);  // waits for a pending output, frees its buffers
-
-// Closed-form cooling-time integral of the table for the surrogate's
-// residual check (tlq_surrogate.cu); called by tlq_set_cooling_table.
-int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* logL, int n);
 
 // Drops the captured step graphs and bumps the set-up generation (tlq_api.cu).
 void invalidate_graphs(tlq_ctx* c);

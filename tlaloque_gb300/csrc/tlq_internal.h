@@ -82,14 +82,14 @@ cudaError_t launch_normalise(float* X, long long N, const float norm[6], cudaStr
 // Surrogate cooling + dt reduction of the mixed step (tlq_surrogate.cu).
 // Stage 2 cools the cells the exact integrator takes in one step, queues
 // the other cells that cool (cqueue) and folds its block maxima into the
-// clock's; the sort pass queues those for the network (nqueue) or the exact
-// integrator (queue); the network pass cools its cells or queues them for
-// the exact integrator; the fallback pass cools those and finishes the dt
-// reduction.  Queues: capacity nx ny nz; counts zero between steps.
+// clock's; the sort pass queues those in the training box for the network
+// (nqueue) and cools the others with the exact integrator; the network pass
+// cools its cells (its prediction, or the exact integrator's where the
+// residual check fails); the dt pass finishes the dt reduction.  Queues:
+// capacity nx ny nz; counts zero between steps.
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
                                Clock* clk, const void* img, const float norm[6], const double box[6],
-                               const float* gcum, const float* gslope, unsigned long long* counts,
-                               const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
+                               unsigned long long* counts, const unsigned* cqueue, unsigned* cqcount,
                                unsigned* nqueue, unsigned* nqcount, cudaStream_t s);
 // The same three passes for several meshes in three launches: fill_cool_job
 // writes one mesh's arguments (cool_job_bytes() of them) into a host array
@@ -99,10 +99,9 @@ cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, dou
 size_t cool_job_bytes();
 int cool_pass_blocks(const Params& p);
 void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, double* U1, long long it_base, Clock* clk,
-                   const void* img, const float norm[6], const double box[6],
-                   const float* gcum, const float* gslope, unsigned long long* counts, const unsigned* cqueue,
-                   unsigned* cqcount, unsigned* queue, unsigned* qcount, unsigned* nqueue, unsigned* nqcount,
-                   int blk0, int nblk);
+                   const void* img, const float norm[6], const double box[6], unsigned long long* counts,
+                   const unsigned* cqueue, unsigned* cqcount, unsigned* nqueue, unsigned* nqcount, int blk0,
+                   int nblk);
 cudaError_t launch_cool_mlp_dt_batch(const void* jobs, int njobs, int nblocks, cudaStream_t s);
 
 // log10 of a small device array in place (cooling-table temperatures).

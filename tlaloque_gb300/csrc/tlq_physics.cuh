@@ -24,7 +24,7 @@ constexpr int BC_OUTFLOW = 1, BC_REFLECTIVE = 2, BC_PERIODIC = 3, BC_INFLOW = 4;
 constexpr int LIM_NONE = 1, LIM_VANLEER = 2, LIM_MINMOD = 3, LIM_UMIST = 4, LIM_WOODWARD = 5,
               LIM_SUPERBEE = 6;
 constexpr int SOLVER_HLLC = 0, SOLVER_HLL = 1;
-constexpr int COOL_NONE = 0, COOL_REF = 1, COOL_SUBCYCLE = 2, COOL_MLP = 3;
+constexpr int COOL_NONE = 0, COOL_REF = 1, COOL_SUBCYCLE = 2, COOL_MLP = 3, COOL_EXACT = 4;
 
 // Fortran MIN/MAX of two reals (no NaN or signed-zero tie matters for valid
 // states); SIGN(1.0, a) with gfortran's default signed-zero semantics.
@@ -57,6 +57,13 @@ struct CoolTable {
   const float* Tf;
   const float* logTf;
   const float* Cf;
+  // the exact integrator's closed form (COOL_EXACT): per segment the power
+  // law's slope (0 above the last node) and at each node G(T_i), the
+  // integral of 1/Lambda from the first node; FP64 and FP32 images
+  const double* slope;
+  const double* gcum;
+  const float* slopef;
+  const float* gcumf;
 };
 
 // Static description of the mesh and the physics switches, passed by value.
@@ -341,9 +348,47 @@ __device__ __forceinline__ double cool_coef(const CoolTable& t, double temp) {
   return pow(10.0, (C1 - C0) / (T1 - T0) * (log10(temp) - T0) + C0);
 }
 
+// The exact integrator (COOL_EXACT): the temperature after a step of
+// cooling number tau (= ce dt, ce = Lambda n^2 / E_th at temp) of a cell at
+// temp >= T_0 whose find_coef value is lam.  At fixed density the
+// sub-cycled integrator's equation, d ln T/dt = -ce(T), becomes
+// dT/dt = -kappa Lambda(T) in its limit of infinitely many sub-steps, and
+// find_coef's log-linear interpolation makes Lambda a power law on each
+// table segment (held constant above the table), so the step integrates in
+// closed form (exact integration of a piecewise power-law cooling function,
+// Townsend 2009, ApJS 181, 391).  With a = 1 - slope of temp's segment i,
+// the cell stays in it while tau <= (1 - (T_i/temp)^a)/a and ends at
+// temp (1 - a tau)^(1/a); otherwise it reaches T_i with a budget
+// B = (tau - tau_i) temp/lam of G left, G(T_new) = G(T_i) - B, found in the
+// segment j whose nodes bracket it.  Nothing cools below T_0: a cell that
+// reaches it ends there.
+__device__ __forceinline__ double cool_exact_T(const CoolTable& t, double temp, double lam, double tau) {
+  int lo = 1, hi = t.n;  // first node above temp (n: none), as find_coef
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (t.T[mid] > temp) hi = mid; else lo = mid + 1;
+  }
+  const int i = lo - 1;
+  const double a = 1.0 - t.slope[i], xlo = t.T[i] / temp;
+  const double tau_i = fabs(a) < 1e-9 ? -log(xlo) : (1.0 - pow(xlo, a)) / a;
+  if (tau <= tau_i) return temp * (fabs(a) < 1e-9 ? exp(-tau) : pow(1.0 - a * tau, 1.0 / a));
+  const double G = t.gcum[i] - (tau - tau_i) * temp / lam;
+  if (!(G > 0.0)) return t.T[0];
+  lo = 0;
+  hi = i - 1;  // last node j < i with G(T_j) <= G
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (t.gcum[mid] <= G) lo = mid; else hi = mid - 1;
+  }
+  const double aj = 1.0 - t.slope[lo], q = (G - t.gcum[lo]) * pow(10.0, t.C[lo]) / t.T[lo];
+  return t.T[lo] * (fabs(aj) < 1e-9 ? exp(q) : pow(1.0 + aj * q, 1.0 / aj));
+}
+
 // apply_cooling for one interior cell (:68-112), and the sub-cycled
 // integrator built on it (nsub equal sub-steps; nsub = 1 is the reference
-// formula).  w is the primitive state (w[4] updated), u4 the total energy.
+// formula); COOL_EXACT takes the same single step when ce dt <= cool_sub_frac
+// and the closed form above otherwise.  w is the primitive state (w[4]
+// updated), u4 the total energy.
 __device__ __forceinline__ void cool_cell(const Params& p, double* w, double& u4, double dt) {
   const double g = p.gamma;
   const double Tmin = p.cool.T[0];
@@ -355,6 +400,13 @@ __device__ __forceinline__ void cool_cell(const Params& p, double* w, double& u4
   double aloss = cool_coef(p.cool, temp);
   const double numdens = w[0] / (p.mu0 * AMU);
   double ce = aloss * (numdens * numdens) / ETH;
+  if (p.cooling == COOL_EXACT && ce * dt > p.cool_sub_frac) {
+    const double Tn = cool_exact_T(p.cool, temp, aloss, ce * dt);
+    w[4] = w[4] * (Tn / temp);
+    ETH = w[4] / (g - 1.0);
+    u4 = EK + ETH;
+    return;
+  }
   int nsub = 1;
   if (p.cooling == COOL_SUBCYCLE && ce * dt > p.cool_sub_frac) {
     const double q = ceil(ce * dt / p.cool_sub_frac);

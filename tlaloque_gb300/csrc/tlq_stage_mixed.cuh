@@ -118,6 +118,41 @@ __device__ __forceinline__ bool cools_at(const Params& p, float temp, const doub
   return T >= p.cool.T[0];
 }
 
+// The exact integrator (COOL_EXACT) in FP32: the same closed form as
+// cool_exact_T (tlq_physics.cuh), returning the fractional temperature
+// change T_new/temp - 1 (in [T_0/temp - 1, 0]).  The change is formed with
+// log1pf/expm1f, which keep their full accuracy under --use_fast_math: with
+// tau just above the single-step limit the change is ~1e-3 of T, and a
+// power or exponential rounded near 1 would carry ~1e-4 of it.  Sums that
+// meet products use explicit-rounding intrinsics (one contraction choice in
+// every kernel that inlines this).
+__device__ __forceinline__ float cool_exact_dropf(const CoolTable& t, float temp, float lam, float tau) {
+  int lo = 1, hi = t.n;  // first node above temp (n: none), as find_coef
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (t.Tf[mid] > temp) hi = mid; else lo = mid + 1;
+  }
+  const int i = lo - 1;
+  const float a = __fsub_rn(1.0f, t.slopef[i]);
+  const float lxlo = logf(t.Tf[i] / temp);  // <= 0
+  const bool flat = fabsf(a) < 1e-6f;
+  const float tau_i = flat ? -lxlo : -expm1f(__fmul_rn(a, lxlo)) / a;
+  if (tau <= tau_i) return flat ? expm1f(-tau) : expm1f(log1pf(-__fmul_rn(a, tau)) / a);
+  const float G = __fsub_rn(t.gcumf[i], __fmul_rn(__fsub_rn(tau, tau_i), temp) / lam);
+  if (!(G > 0.0f)) return __fsub_rn(t.Tf[0] / temp, 1.0f);
+  lo = 0;
+  hi = i - 1;  // last node j < i with G(T_j) <= G
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (t.gcumf[mid] <= G) lo = mid; else hi = mid - 1;
+  }
+  const float aj = __fsub_rn(1.0f, t.slopef[lo]);
+  const float q = __fmul_rn(__fsub_rn(G, t.gcumf[lo]), exp10f(t.Cf[lo])) / t.Tf[lo];
+  const float lj = logf(t.Tf[lo] / temp);
+  const float r = fabsf(aj) < 1e-6f ? q : log1pf(__fmul_rn(aj, q)) / aj;  // ln(T_new/T_j)
+  return fmaxf(expm1f(__fadd_rn(lj, r)), __fsub_rn(t.Tf[0] / temp, 1.0f));
+}
+
 __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv_muamu, float gm1, float* w,
                                             double& u4, float dt, const double* u) {
   const CoolTable& t = p.cool;
@@ -131,6 +166,12 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   float ce = (aloss * n) * (n / ETH);
   int nsub = 1;
   const float frac = p.f_cool_sub_frac;
+  if (p.cooling == COOL_EXACT && ce * dt > frac) {
+    const float dp = __fmul_rn(w[4], cool_exact_dropf(t, temp, aloss, ce * dt));
+    w[4] = __fadd_rn(w[4], dp);
+    u4 = u4 + f2d(dp / gm1);
+    return;
+  }
   if (p.cooling == COOL_SUBCYCLE && ce * dt > frac) {
     const float q = ceilf(ce * dt / frac);
     nsub = (q > (float)p.cool_max_sub) ? p.cool_max_sub : (int)q;

@@ -4,13 +4,13 @@
 // In the step, stage 2 cools the cells the exact integrator takes in one
 // step and leaves the other cells that cool (temp >= the table's first
 // temperature, cooling.f90:71) and the CFL reduction to three passes
-// (k_cool_sort, k_cool_net, k_cool_fallback_dt): for a cell inside the
-// training box the network predicts y = -ln(T_new/T)/tau from
+// (k_cool_sort, k_cool_net, k_cool_dt): for a cell inside the training box
+// the network predicts r with ln(T/T_new) = tau (1 + tau r) from
 // (log10 n, log10 T, log10 tau); the prediction is accepted when
-// |T_pred - T_int| <= 1e-3 T, T_int the closed-form solution of
-// dT/dt = -(gamma-1) n Lambda(T)/k_B for the piecewise power-law table
-// (Townsend 2009, ApJS 181, 391: exact integration of a power-law cooling
-// function); otherwise the cell is cooled by the sub-cycled integrator.
+// |T_pred - T_ex| <= tol T, T_ex the exact integrator's temperature (the
+// closed-form solution of dT/dt = -(gamma-1) n Lambda(T)/k_B for the
+// piecewise power-law table, cool_exact_dropf); otherwise, and for a cell
+// outside the box, the cell takes T_ex.
 // Built with --use_fast_math (FP32 part of the mixed form).
 #include <algorithm>
 #include <chrono>
@@ -30,49 +30,11 @@ struct SurrogateArgs {
   const mlp::SmemWeights* img;  // the network's image (launch_pack_weights)
   float norm[6];        // centre, half-width per feature
   float box[6];         // training box (lo, hi per feature)
-  const float* gcum;    // closed-form integral at the table nodes
-  const float* gslope;  // per-segment power-law slope
   unsigned long long* counts;
 };
 
-// Table segment of T >= T_0: i with T_i <= T < T_{i+1}, n-1 above the last node.
-__device__ __forceinline__ int seg_of(const CoolTable& t, float T) {
-  int lo = 1, hi = t.n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (t.Tf[mid] > T) hi = mid; else lo = mid + 1;
-  }
-  return lo - 1;
-}
-
-// G(T) = int_{T_0}^{T} dT'/Lambda(T') for the log-linear table.
-__device__ __forceinline__ float g_of(const CoolTable& t, const SurrogateArgs& sa, float T) {
-  const int i = seg_of(t, T);
-  const float Ti = t.Tf[i], Li = exp10f(t.Cf[i]);
-  if (i >= t.n - 1) return sa.gcum[t.n - 1] + (T - Ti) / Li;
-  const float a = 1.0f - sa.gslope[i];
-  const float r = T / Ti;
-  const float part = fabsf(a) < 1e-4f ? (Ti / Li) * __logf(r) : (Ti / Li) * (__powf(r, a) - 1.0f) / a;
-  return sa.gcum[i] + part;
-}
-
-// Inverse of G for G >= 0.
-__device__ __forceinline__ float g_inv(const CoolTable& t, const SurrogateArgs& sa, float G) {
-  int lo = 1, hi = t.n;  // first node with gcum > G
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (sa.gcum[mid] > G) hi = mid; else lo = mid + 1;
-  }
-  const int j = lo - 1;
-  const float Tj = t.Tf[j], Lj = exp10f(t.Cf[j]);
-  if (j >= t.n - 1) return Tj + (G - sa.gcum[t.n - 1]) * Lj;
-  const float a = 1.0f - sa.gslope[j];
-  const float q = (G - sa.gcum[j]) * Lj / Tj;
-  return fabsf(a) < 1e-4f ? Tj * __expf(q) : Tj * __powf(fmaxf(1.0f + a * q, 0.0f), 1.0f / a);
-}
-
 constexpr int CT = 128;      // threads per block of the network pass
-constexpr int FT = 128;      // threads per block of the fallback pass
+constexpr int FT = 128;      // threads per block of the dt pass
 constexpr int PB = 152 * 3;  // blocks of each pass (at most): one resident wave of the network pass
 
 // Blocks of each cooling pass for a mesh: enough for its cells to cool at
@@ -101,19 +63,18 @@ __device__ __forceinline__ long long interior_offset(const Params& p, const Layo
 // Pass 1 (sort): stage 2 queued the interior cells that cool (temp >= the
 // table's first temperature, cooling.f90:71) beyond a single step of the
 // exact integrator (it cooled the cells whose tau is at most the
-// integrator's sub-step itself, with this pass's arithmetic).  A cell inside
-// the training box goes to the network queue, the others to the fallback
-// queue; a queued cell whose tau is at most the sub-step after all takes the
-// single exponential step here.
+// integrator's single-step limit itself, with this pass's arithmetic).  A
+// cell inside the training box goes to the network queue; a cell outside it
+// takes the exact integrator here; a queued cell whose tau is at most the
+// single-step limit after all takes the single exponential step here.
 // Pass 2 (network): the network queue densely, 32 cells to a warp (a warp
 // of the sort pass holds a few network cells at most, and its matrix tiles
 // would run for all 32 rows): the prediction, accepted when the residual
-// check passes; the others go to the fallback queue, and so do the cells
-// whose cooling reaches the table's first temperature within the step
-// (closed form: G_t <= 0): there the reference integrator's last sub-step
-// decides how far below that temperature the cell ends.
+// check against the exact integrator passes, else the exact integrator's
+// temperature (which the check has just computed).
 // Both passes fold the block maxima of the signal speeds of the cells they
-// cooled into the clock's (stage 2 left out the cells it queued).
+// cooled into the clock's (stage 2 left out the cells it queued); pass 3
+// finishes the dt reduction and empties the queues.
 // The state the step just wrote: U1 or U0 by the clock's buffer parity (the
 // clock has not advanced yet), so that one captured launch serves both
 // parities.
@@ -124,7 +85,7 @@ __device__ __forceinline__ double* step_output(double* U0, double* U1, const Clo
 // Everything one mesh's cooling passes need (a kernel argument for one
 // mesh, a device array entry for a batch of them).
 struct CoolJob {
-  Params p;  // the run's parameters, cooling = the sub-cycled integrator (the fallback)
+  Params p;  // the run's parameters, cooling = the exact integrator (the fallback)
   Layout L;
   double* U0;
   double* U1;
@@ -133,8 +94,6 @@ struct CoolJob {
   SurrogateArgs sa;
   const unsigned* cqueue;  // cells stage 2 queued (they cool)
   unsigned* cqcount;
-  unsigned* queue;  // cells handed to the exact integrator
-  unsigned* qcount;
   unsigned* nqueue;  // cells for the network
   unsigned* nqcount;
   unsigned blk0, nblk;  // this mesh's blocks of each pass: [blk0, blk0 + nblk)
@@ -257,19 +216,19 @@ __device__ void cool_sort_mesh(const CoolJob& j, double* red, unsigned nblocks, 
     CellCool c;
     cell_cool(p, j.sa, u, dtf, c);
     const bool need = valid && c.need;
-    // tau at most the integrator's sub-step: the exact integrator is a single
-    // exponential step, cheaper and exact, and the network has nothing to gain
+    // tau at most the single-step limit: the exact integrator is a single
+    // exponential step, and the network has nothing to gain; outside the
+    // training box the exact integrator's closed form (p.cooling: COOL_EXACT)
     const bool single = need && !(c.tau > p.f_cool_sub_frac);
-    if (single) {
+    const bool net = need && !single && c.inbox;
+    const bool ext = need && !single && !c.inbox;
+    if (single || ext) {
       cool_cell_f(p, p.f_cT, p.f_inv_muamu, gm1, c.w, u[4], dtf, u);
       U[4 * L.plane + o] = u[4];
       speeds_max(c.w, gf, m0, m1, m2);
     }
-    const bool net = need && !single && c.inbox;
-    const bool fb = need && !single && !c.inbox;
     warp_append(net, cidx, j.nqueue, j.nqcount);
-    warp_append(fb, cidx, j.queue, j.qcount);
-    fell += fb ? 1 : 0;
+    fell += ext ? 1 : 0;
     one += single ? 1 : 0;
   }
   add_counts(j.sa, 0, fell, one);
@@ -329,26 +288,25 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
     }
     bool ok = false;
     if (valid) {
-      const float T = c.T, tau = c.tau, lam = c.lam;
-      const float Gt = g_of(tab, sa, T) - tau * T / lam;  // budget (gamma-1) n dt / k_B = tau T / Lambda(T)
-      if (Gt > 0.0f) {
-        const float Tint = g_inv(tab, sa, Gt);
-        // the network's r: ln(T_new/T) = -(tau + tau^2 r); q = T_new/T - 1
-        // without cancellation, clamped at the table's first temperature
-        const float qf = fmaxf(expm1f(-(1.0f + tau * y) * tau), tab.Tf[0] / T - 1.0f);
-        ok = fabsf(T * qf - (Tint - T)) <= p.f_mlp_tol * T;
-        if (ok) {
-          const float dp = c.w[4] * qf;
-          c.w[4] = c.w[4] + dp;
-          U[4 * L.plane + o] = u[4] + f2d(dp / gm1);
-        }
+      const float T = c.T, tau = c.tau;
+      // the exact integrator's change and the network's, T_new/T - 1 (the
+      // network's r: ln(T_new/T) = -(tau + tau^2 r); clamped at the table's
+      // first temperature, where cooling stops)
+      const float qx = cool_exact_dropf(tab, T, c.lam, tau);
+      const float qf = fmaxf(expm1f(-(1.0f + tau * y) * tau), __fsub_rn(tab.Tf[0] / T, 1.0f));
+      ok = fabsf(qf - qx) <= p.f_mlp_tol;
+      if (ok) {
+        const float dp = __fmul_rn(c.w[4], qf);
+        c.w[4] = __fadd_rn(c.w[4], dp);
+        U[4 * L.plane + o] = u[4] + f2d(dp / gm1);
+      } else {
+        cool_cell_f(p, p.f_cT, p.f_inv_muamu, gm1, c.w, u[4], dtf, u);  // the exact integrator
+        U[4 * L.plane + o] = u[4];
       }
+      speeds_max(c.w, gf, m0, m1, m2);
     }
-    const bool fb = valid && !ok;
-    warp_append(fb, cidx, j.queue, j.qcount);
     used += ok ? 1 : 0;
-    fell += fb ? 1 : 0;
-    if (ok) speeds_max(c.w, gf, m0, m1, m2);
+    fell += (valid && !ok) ? 1 : 0;
   }
   add_counts(sa, used, fell, 0);
   cfl_contribute<CT>(f2d(m0), f2d(m1), f2d(m2), j.clk, red);
@@ -375,50 +333,27 @@ __global__ void __launch_bounds__(CT, 3) k_cool_net(const __grid_constant__ Cool
   cool_net_mesh(j, W, red, j.nblk, blockIdx.x - j.blk0);
 }
 
-__device__ void cool_fallback_mesh(const CoolJob& j, double* red, int* flag, unsigned nblocks, unsigned bid) {
-  const Params& p = j.p;
-  const Layout& L = j.L;
+__device__ void cool_dt_mesh(const CoolJob& j, double* red, int* flag, unsigned nblocks) {
   Clock* clk = j.clk;
   if (!(clk->t < clk->tfin)) return;
-  double* __restrict__ U = step_output(j.U0, j.U1, clk, j.it_base);
-  const unsigned* __restrict__ queue = j.queue;
-  const unsigned nq = *j.qcount;
-  const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
-  const float cT = p.f_cT;
-  const float inv_muamu = p.f_inv_muamu;
-  const float dtf = d2f(clk->dt);
-  float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-  for (unsigned q = bid * FT + threadIdx.x; q < nq; q += nblocks * FT) {
-    const long long o = interior_offset(p, L, (long long)queue[q]);
-    double u[5];
-#pragma unroll
-    for (int e = 0; e < 5; ++e) u[e] = U[e * L.plane + o];
-    float cf[5], w[5];
-    mixed_cell(gm1, u, 1, cf, w);
-    cool_cell_f(p, cT, inv_muamu, gm1, w, u[4], dtf, u);
-    U[4 * L.plane + o] = u[4];
-    speeds_max(w, gf, m0, m1, m2);
-  }
-  cfl_reduce_finalize_n<FT>(f2d(m0), f2d(m1), f2d(m2), clk, p, true, red, flag, nblocks);
+  cfl_reduce_finalize_n<FT>(0.0, 0.0, 0.0, clk, j.p, true, red, flag, nblocks);
   if (*flag && threadIdx.x == 0) {
-    *j.qcount = 0u;
     *j.cqcount = 0u;
     *j.nqcount = 0u;
   }
 }
 
-// Pass 3 (fallback): the queued cells through the exact integrator (the
-// sub-cycled cooling with the run's sub-step settings), then the dt
-// reduction over the block maxima of stage 2 and the three passes; the last
+// Pass 3: the dt reduction over the block maxima of stage 2 and the two
+// cooling passes (this pass's blocks only take their tickets); the last
 // block of a mesh empties its queues.  One mesh (jobs null: `one`) or njobs
 // meshes, as the other passes.
-__global__ void __launch_bounds__(FT) k_cool_fallback_dt(const __grid_constant__ CoolJob one,
-                                                         const CoolJob* __restrict__ jobs, int njobs) {
+__global__ void __launch_bounds__(FT) k_cool_dt(const __grid_constant__ CoolJob one, const CoolJob* __restrict__ jobs,
+                                                int njobs) {
   __shared__ double red[96];
   __shared__ int flag;
   __shared__ SmemJob sj;
   const CoolJob& j = stage_job(sj, job_of_block(one, jobs, njobs, blockIdx.x));
-  cool_fallback_mesh(j, red, &flag, j.nblk, blockIdx.x - j.blk0);
+  cool_dt_mesh(j, red, &flag, j.nblk);
 }
 
 }  // namespace
@@ -426,13 +361,12 @@ __global__ void __launch_bounds__(FT) k_cool_fallback_dt(const __grid_constant__
 size_t cool_job_bytes() { return sizeof(CoolJob); }
 
 void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, double* U1, long long it_base, Clock* clk,
-                   const void* img, const float norm[6], const double box[6],
-                   const float* gcum, const float* gslope, unsigned long long* counts, const unsigned* cqueue,
-                   unsigned* cqcount, unsigned* queue, unsigned* qcount, unsigned* nqueue, unsigned* nqcount,
-                   int blk0, int nblk) {
+                   const void* img, const float norm[6], const double box[6], unsigned long long* counts,
+                   const unsigned* cqueue, unsigned* cqcount, unsigned* nqueue, unsigned* nqcount, int blk0,
+                   int nblk) {
   CoolJob j{};
   j.p = p;
-  j.p.cooling = COOL_SUBCYCLE;  // the fallback: the sub-cycled integrator with the run's sub-step settings
+  j.p.cooling = COOL_EXACT;  // the fallback: the exact integrator (single step up to the run's cool_sub_frac)
   j.L = L;
   j.U0 = U0;
   j.U1 = U1;
@@ -443,13 +377,9 @@ void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, doub
     j.sa.norm[q] = norm[q];
     j.sa.box[q] = (float)box[q];
   }
-  j.sa.gcum = gcum;
-  j.sa.gslope = gslope;
   j.sa.counts = counts;
   j.cqueue = cqueue;
   j.cqcount = cqcount;
-  j.queue = queue;
-  j.qcount = qcount;
   j.nqueue = nqueue;
   j.nqcount = nqcount;
   j.blk0 = (unsigned)blk0;
@@ -459,20 +389,18 @@ void fill_cool_job(void* dst, const Params& p, const Layout& L, double* U0, doub
 
 cudaError_t launch_cool_mlp_dt(const Params& p, const Layout& L, double* U0, double* U1, long long it_base,
                                Clock* clk, const void* img, const float norm[6], const double box[6],
-                               const float* gcum, const float* gslope, unsigned long long* counts,
-                               const unsigned* cqueue, unsigned* cqcount, unsigned* queue, unsigned* qcount,
+                               unsigned long long* counts, const unsigned* cqueue, unsigned* cqcount,
                                unsigned* nqueue, unsigned* nqcount, cudaStream_t s) {
   const int nb = pass_blocks(p);
   CoolJob j;
-  fill_cool_job(&j, p, L, U0, U1, it_base, clk, img, norm, box, gcum, gslope, counts, cqueue, cqcount, queue, qcount,
-                nqueue, nqcount, 0, nb);
+  fill_cool_job(&j, p, L, U0, U1, it_base, clk, img, norm, box, counts, cqueue, cqcount, nqueue, nqcount, 0, nb);
   k_cool_sort<<<nb, CT, 0, s>>>(j, nullptr, 1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_cool_net<<<nb, CT, 0, s>>>(j, nullptr, 1);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cool_fallback_dt<<<nb, FT, 0, s>>>(j, nullptr, 1);
+  k_cool_dt<<<nb, FT, 0, s>>>(j, nullptr, 1);
   return cudaGetLastError();
 }
 
@@ -487,7 +415,7 @@ cudaError_t launch_cool_mlp_dt_batch(const void* jobs, int njobs, int nblocks, c
   k_cool_net<<<nblocks, CT, 0, s>>>(none, d, njobs);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cool_fallback_dt<<<nblocks, FT, 0, s>>>(none, d, njobs);
+  k_cool_dt<<<nblocks, FT, 0, s>>>(none, d, njobs);
   return cudaGetLastError();
 }
 
@@ -538,36 +466,6 @@ void init_params(std::vector<float>& P, unsigned long long seed) {
 }
 
 }  // namespace
-
-// Closed-form integral of 1/Lambda over the table (FP64), for the residual check.
-int tlq_surrogate_prepare_table(tlq_ctx* ctx, const double* T, const double* logL, int n) {
-  ctx->cool_tmin = T[0];
-  std::vector<float> gc(n), sl(n);
-  double acc = 0.0;
-  for (int i = 0; i < n; ++i) {
-    gc[i] = (float)acc;
-    if (i + 1 < n) {
-      const double s = (logL[i + 1] - logL[i]) / (std::log10(T[i + 1]) - std::log10(T[i]));
-      sl[i] = (float)s;
-      const double Li = std::pow(10.0, logL[i]), a = 1.0 - s, r = T[i + 1] / T[i];
-      acc += std::fabs(a) < 1e-12 ? (T[i] / Li) * std::log(r) : (T[i] / Li) * (std::pow(r, a) - 1.0) / a;
-    } else {
-      sl[i] = 0.0f;
-    }
-  }
-  cudaFree(ctx->gcum);
-  cudaFree(ctx->gslope);
-  ctx->gcum = ctx->gslope = nullptr;
-  SCK(cudaMalloc(&ctx->gcum, n * sizeof(float)));
-  SCK(cudaMalloc(&ctx->gslope, n * sizeof(float)));
-  SCK(cudaMemcpy(ctx->gcum, gc.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-  SCK(cudaMemcpy(ctx->gslope, sl.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-  if (!ctx->cool_counts) {
-    SCK(cudaMalloc(&ctx->cool_counts, 3 * sizeof(unsigned long long)));
-    SCK(cudaMemset(ctx->cool_counts, 0, 3 * sizeof(unsigned long long)));
-  }
-  return TLQ_OK;
-}
 
 extern "C" {
 

@@ -20,7 +20,7 @@ OK, ERR_CUDA, ERR_CONFIG, ERR_NONFINITE_DT, ERR_NEG_DENSITY, ERR_TIMEOUT, ERR_AR
 BC_OUTFLOW, BC_REFLECTIVE, BC_PERIODIC, BC_INFLOW = 1, 2, 3, 4
 LIMITER_NONE, LIMITER_VANLEER, LIMITER_MINMOD, LIMITER_UMIST, LIMITER_WOODWARD, LIMITER_SUPERBEE = 1, 2, 3, 4, 5, 6
 SOLVER_HLLC, SOLVER_HLL = 0, 1
-COOL_NONE, COOL_REF, COOL_SUBCYCLE, COOL_MLP = 0, 1, 2, 3
+COOL_NONE, COOL_REF, COOL_SUBCYCLE, COOL_MLP, COOL_EXACT = 0, 1, 2, 3, 4
 MLP_NPARAM = 8641
 PREC_FP64, PREC_MIXED = 0, 1
 GBC_ZERO, GBC_MULTIPOLE = 0, 1
