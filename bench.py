@@ -559,7 +559,6 @@ def main():
                                       "the exact integrator's single exponential step directly (single_step)"}
         head = sur
         if not args.no_surrogate_active:
-            sur["ctx"].close()
             surrogate["active"] = surrogate_active(net, sub)
     value = head["value"]
     ms_max = head["ms"]

@@ -54,20 +54,27 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 4-D map {x, y, z, var} over a SoA array with `nvar` planes; box = tile + halo 2.
-int make_map(tlq_ctx* ctx, CUtensorMap* m, double* base, int nvar) {
+// 4-D map {x, y, z, var} over a SoA array with `nvar` planes of elements of
+// `esize` bytes (8: FP64, 4: FP32); box = the tile plus the halo its kernel
+// reads: the plain form's halo-2 box; in the mixed form stage 1's box of U
+// (2 cells in x, 1 in y: halo1 = true) and stage 2's halo-2 box of UPP's
+// FP32 primitives.
+int make_map(tlq_ctx* ctx, CUtensorMap* m, void* base, int nvar, int esize = 8, bool halo1 = false) {
   auto fn = encode_fn();
   if (!fn) return fail(ctx, TLQ_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
   const Layout& L = ctx->L;
   cuuint64_t dims[4] = {(cuuint64_t)(ctx->cfg.nx + 4), (cuuint64_t)(ctx->cfg.ny + 4), (cuuint64_t)(ctx->cfg.nz + 4),
                         (cuuint64_t)nvar};
-  cuuint64_t strides[3] = {(cuuint64_t)L.px * 8, (cuuint64_t)L.px * L.nyg * 8, (cuuint64_t)L.plane * 8};
-  // the halo-2 box of one tile of the form's kernels
+  const cuuint64_t es = (cuuint64_t)esize;
+  cuuint64_t strides[3] = {(cuuint64_t)L.px * es, (cuuint64_t)L.px * L.nyg * es, (cuuint64_t)L.plane * es};
   const bool mixed = ctx->cfg.precision == TLQ_PREC_MIXED;
-  cuuint32_t box[4] = {(cuuint32_t)(mixed ? MHX : HX), (cuuint32_t)(mixed ? MHY : HY), 1, (cuuint32_t)nvar};
+  const cuuint32_t bx = (cuuint32_t)(mixed ? MHX : HX);
+  const cuuint32_t by = (cuuint32_t)(mixed ? (halo1 ? MTY + 2 : MHY) : HY);
+  cuuint32_t box[4] = {bx, by, 1, (cuuint32_t)nvar};
   cuuint32_t estr[4] = {1, 1, 1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = fn(m, esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(ctx, TLQ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return TLQ_OK;
 }
@@ -205,6 +212,8 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.zlen = ctx->zlen;
   a.phi = ctx->cfg.self_gravity ? ctx->phit : ctx->phi;
   a.lapf = ctx->lapf;
+  // the mixed form keeps UPP as FP32 primitives in the same allocation
+  a.uppf = reinterpret_cast<float*>(ctx->UPP);
   // stage 1: U[par] -> UPP
   a.uold = ctx->U[par];
   a.out = ctx->UPP;
@@ -432,9 +441,10 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
     return bail(TLQ_ERR_NOMEM);
   if (prepare_stage_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
   if (cfg->precision == TLQ_PREC_MIXED && prepare_mixed_kernels() != cudaSuccess) return bail(TLQ_ERR_CUDA);
-  int r = make_map(ctx, &ctx->tm_U[0], ctx->U[0], 5);
-  if (!r) r = make_map(ctx, &ctx->tm_U[1], ctx->U[1], 5);
-  if (!r) r = make_map(ctx, &ctx->tm_UPP, ctx->UPP, 5);
+  const bool mixed = cfg->precision == TLQ_PREC_MIXED;
+  int r = make_map(ctx, &ctx->tm_U[0], ctx->U[0], 5, 8, mixed);
+  if (!r) r = make_map(ctx, &ctx->tm_U[1], ctx->U[1], 5, 8, mixed);
+  if (!r) r = make_map(ctx, &ctx->tm_UPP, ctx->UPP, 5, mixed ? 4 : 8);
   if (!r) r = make_map(ctx, &ctx->tm_P, ctx->Pc, 1);
   if (r) return bail(r);
   for (int q = 0; q < 6; ++q) cudaEventCreate(&ctx->ev[q]);

@@ -40,8 +40,9 @@ struct Item {  // one tile of one member
 
 // The shared memory of a persistent block: the stage's smem plus the
 // current member's arguments (read by every cell of the tile).
+template <int STAGE>
 struct BatchSmem {
-  MixedSmem s;
+  MixedSmem<STAGE> s;
   alignas(16) StageArgs a;
 };
 
@@ -50,10 +51,10 @@ __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
 }
 
 template <int STAGE, int LIM = -1, int SOLV = -1>
-__global__ void __launch_bounds__(MNT, MIXED_BLOCKS_PER_SM)
+__global__ void __launch_bounds__(MNT, MixedBlocks<STAGE>::value)
     stage_kernel_mixed_batch(const MemberDesc* __restrict__ mem, const Item* __restrict__ items, int nitems) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
-  BatchSmem& bs = *reinterpret_cast<BatchSmem*>(smem_bytes);
+  BatchSmem<STAGE>& bs = *reinterpret_cast<BatchSmem<STAGE>*>(smem_bytes);
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const Item it = items[w];
     const MemberDesc& m = mem[it.member];
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(MNT, MIXED_BLOCKS_PER_SM)
     // the tile's copies have all completed: retire the barriers before the
     // next tile initialises them again
     if (threadIdx.x == 0)
-      for (int q = 0; q < MRAW; ++q) mbar_inval(&bs.s.bar[q]);
+      for (int q = 0; q < MixedSmemSel<STAGE>::nbar; ++q) mbar_inval(&bs.s.bar[q]);
     __syncthreads();
   }
 }
@@ -95,12 +96,12 @@ static_assert(alignof(MemberDesc) >= 64, "tensor maps 64-byte aligned");
 constexpr int SPEC_LIM = LIM_VANLEER, SPEC_SOLV = SOLVER_HLLC;  // as the single-mesh kernels
 
 cudaError_t prepare_batch_kernels() {
-  const int smem = (int)sizeof(BatchSmem);
   const void* ks[4] = {(const void*)stage_kernel_mixed_batch<1>, (const void*)stage_kernel_mixed_batch<2>,
                        (const void*)stage_kernel_mixed_batch<1, SPEC_LIM, SPEC_SOLV>,
                        (const void*)stage_kernel_mixed_batch<2, SPEC_LIM, SPEC_SOLV>};
-  for (const void* k : ks) {
-    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  for (int q = 0; q < 4; ++q) {
+    const int smem = (int)(q % 2 == 0 ? sizeof(BatchSmem<1>) : sizeof(BatchSmem<2>));
+    const cudaError_t e = cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -168,6 +169,7 @@ void fill_desc(tlq_batch* b, int i) {
       a.lapf = c->lapf;
       a.uold = c->U[par];
       a.out = (st == 1) ? c->UPP : c->U[par ^ 1];
+      a.uppf = reinterpret_cast<float*>(c->UPP);  // stage 1 writes UPP as FP32 primitives
       a.pout = (st == 1) ? nullptr : c->Pc;
       a.use_p = 0;
       a.cqueue = (st == 2) ? c->mlp_cqueue : nullptr;
@@ -212,9 +214,13 @@ int upload_items(tlq_batch* b, const std::vector<Item>& v) {
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  int per_sm = 0;
+  // one persistent grid serves both stages: the smaller residency of the two
+  int per_sm = 0, per_sm1 = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tlq::stage_kernel_mixed_batch<2>, tlq::MNT,
-                                                sizeof(tlq::BatchSmem));
+                                                sizeof(tlq::BatchSmem<2>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, tlq::stage_kernel_mixed_batch<1>, tlq::MNT,
+                                                sizeof(tlq::BatchSmem<1>));
+  per_sm = std::min(per_sm, per_sm1);
   b->blocks = std::max(1, std::min(b->nitems, nsm * std::max(per_sm, 1)));
   return TLQ_OK;
 }
@@ -261,20 +267,20 @@ int refresh_desc(tlq_batch* b, const std::vector<int>& which = {}) {
 // that use it (their stage 2 queued the cooling cells and left the dt
 // reduction to them; refresh_desc wrote their arguments).
 int enqueue_batch_step(tlq_batch* b) {
-  const size_t smem = sizeof(tlq::BatchSmem);
+  const size_t smem1 = sizeof(tlq::BatchSmem<1>), smem2 = sizeof(tlq::BatchSmem<2>);
   // the specialised kernels when every member uses their limiter and solver
   bool spec = true;
   for (tlq_ctx* c : b->m) spec = spec && c->P.limiter == tlq::SPEC_LIM && c->P.solver == tlq::SPEC_SOLV;
   if (spec) {
     tlq::stage_kernel_mixed_batch<1, tlq::SPEC_LIM, tlq::SPEC_SOLV>
-        <<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+        <<<b->blocks, tlq::MNT, smem1, b->stream>>>(b->d_desc, b->d_items, b->nitems);
     BCK(cudaGetLastError());
     tlq::stage_kernel_mixed_batch<2, tlq::SPEC_LIM, tlq::SPEC_SOLV>
-        <<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+        <<<b->blocks, tlq::MNT, smem2, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   } else {
-    tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+    tlq::stage_kernel_mixed_batch<1><<<b->blocks, tlq::MNT, smem1, b->stream>>>(b->d_desc, b->d_items, b->nitems);
     BCK(cudaGetLastError());
-    tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::MNT, smem, b->stream>>>(b->d_desc, b->d_items, b->nitems);
+    tlq::stage_kernel_mixed_batch<2><<<b->blocks, tlq::MNT, smem2, b->stream>>>(b->d_desc, b->d_items, b->nitems);
   }
   BCK(cudaGetLastError());
   if (b->ncool) BCK(tlq::launch_cool_mlp_dt_batch(b->d_cool, b->ncool, b->cool_blocks, b->stream));

@@ -39,7 +39,7 @@ cudaError_t launch_stage(int stage, int precision, const CUtensorMap& tm_in, con
 // Mixed-precision stage kernels (tlq_mixed.cu).
 cudaError_t prepare_mixed_kernels();
 cudaError_t prepare_batch_kernels();  // tlq_batch.cu
-size_t mixed_smem_bytes();
+size_t mixed_smem_bytes(int stage);
 cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageArgs& a, dim3 grid, cudaStream_t s);
 // The first dt of the mixed form (its FP32 signal speeds; tlq_mixed.cu).
 cudaError_t launch_init_dt_mixed(const Params& p, const Layout& L, const double* U, Clock* clk, int nblocks,

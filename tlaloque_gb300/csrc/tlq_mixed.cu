@@ -7,26 +7,26 @@
 
 namespace tlq {
 
-size_t mixed_smem_bytes() { return sizeof(MixedSmem); }
+size_t mixed_smem_bytes(int stage) { return stage == 1 ? sizeof(MixedSmem<1>) : sizeof(MixedSmem<2>); }
 
 // The specialised instance: van Leer with HLLC, the reference's default
 // pairing (user/parameters.f90); every other pairing runs the generic one.
 constexpr int SPEC_LIM = LIM_VANLEER, SPEC_SOLV = SOLVER_HLLC;
 
 cudaError_t prepare_mixed_kernels() {
-  const int smem = (int)sizeof(MixedSmem);
   const void* ks[4] = {(const void*)stage_kernel_mixed<1>, (const void*)stage_kernel_mixed<2>,
                        (const void*)stage_kernel_mixed<1, SPEC_LIM, SPEC_SOLV>,
                        (const void*)stage_kernel_mixed<2, SPEC_LIM, SPEC_SOLV>};
-  for (const void* k : ks) {
-    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  for (int q = 0; q < 4; ++q) {
+    const int smem = (int)mixed_smem_bytes(q % 2 == 0 ? 1 : 2);
+    const cudaError_t e = cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
 cudaError_t launch_stage_mixed(int stage, const CUtensorMap& tm_in, const StageArgs& a, dim3 grid, cudaStream_t s) {
-  const size_t smem = sizeof(MixedSmem);
+  const size_t smem = mixed_smem_bytes(stage);
   const bool spec = a.p.limiter == SPEC_LIM && a.p.solver == SPEC_SOLV;
   if (stage == 1) {
     if (spec)

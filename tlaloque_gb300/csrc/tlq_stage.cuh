@@ -24,14 +24,21 @@ constexpr int HX = TX + 4, HY = TY + 4;  // halo-2 box
 constexpr int PLANE_BOX = HY * HX;
 
 // Tile of the mixed-form kernels (its own constants, so that it can be tuned
-// apart from the plain form's): 16 x 8 columns on 128 threads.  Measured
-// alternative: 16 x 7 (the plane's 359 faces in three rounds of 128 threads
-// instead of 408 in four) was 2 % slower at 256^3 -- fewer cells per tile
-// outweighed the shorter face phase.
-constexpr int MTX = 16, MTY = 8, MNT = 128;
+// apart from the plain form's): MTX x MTY columns on MNT threads, a multiple
+// of 16 columns wide (the FP32 box of a tile starts on a 64-byte boundary).
+#ifndef TLQ_MTX
+#define TLQ_MTX 16
+#endif
+#ifndef TLQ_MTY
+#define TLQ_MTY 8
+#endif
+#ifndef TLQ_MNT
+#define TLQ_MNT 128
+#endif
+constexpr int MTX = TLQ_MTX, MTY = TLQ_MTY, MNT = TLQ_MNT;
 constexpr int MHX = MTX + 4, MHY = MTY + 4;  // halo-2 box
-constexpr int MPLANE_BOX = MHY * MHX;
 static_assert(MTX * MTY <= MNT, "one cell per thread");
+static_assert(MTX % 16 == 0 && MNT % 32 == 0, "tile shape");
 constexpr int NRING = 4;
 constexpr long long WAIT_LIMIT = 1LL << 24;  // mbarrier polls before giving up
 
@@ -46,6 +53,7 @@ struct StageArgs {
   int zlen;            // planes per block
   int use_p;           // STAGE 1 with cooling: interior pressure from the P plane
   float* lapf;         // mixed form: eta * Laplacian of U (FP32, written by stage 1, read by stage 2)
+  float* uppf;         // mixed form, STAGE 1: UPP as FP32 primitives (rho, u, v, w, p), read by stage 2
   unsigned* cqueue;    // mixed form with the cooling surrogate: stage 2 queues the cells that cool
   unsigned* cqcount;   // (beyond a single step of the exact integrator, which it takes itself)
   unsigned long long* cool_counts;  // [2]: the cells stage 2 cooled in a single step

@@ -19,31 +19,86 @@
 namespace tlq {
 
 
-// Shared memory per block is kept under 57 KB so that 4 blocks fit an SM:
-constexpr int MRAW = 1;  // TMA landing slot (raw FP64 plane); the next plane is requested as soon as the
-                         // previous one is converted, a whole plane's work (~10 us) ahead of its use
-constexpr int MCU = 3;   // FP32 conserved-state ring (faces: planes k, k+1; stage-1 Laplacian: k-1..k+1)
-constexpr int MIXED_BLOCKS_PER_SM = 4;
+// Geometry of the planes a stage stages in shared memory (x fastest, tile
+// cell (tx, ty) at (OY + ty, 2 + tx)).  Stage 1 (first-order fluxes of U and
+// the viscosity Laplacian of U) needs a 1-cell halo; its box is 2 cells wide
+// in x all the same (a TMA box of FP64 values starts on a 16-byte boundary,
+// an even cell index) and 1 cell high in y.  Stage 2 (second-order fluxes of
+// UPP) needs 2 cells on each side.
+template <int S>
+struct MGeo {
+  static constexpr int OY = (S == 1) ? 1 : 2;
+  static constexpr int PX = MTX + 4, PY = MTY + 2 * OY, PB = PX * PY;
+};
 
-// Ring slots of plane q.  Planes start at k0 - 2 >= -1, so q can be
-// negative; C++ '%' keeps the sign of q, hence the offset.
-__device__ __forceinline__ int raw_slot(int q) { return (q + 4 * MRAW) % MRAW; }
+// One plane of FP32 values (5 variables), 128-byte aligned: the TMA writes
+// stage 2's planes straight into these.
+template <int S>
+struct alignas(128) PlaneF {
+  float v[5][MGeo<S>::PY][MGeo<S>::PX];
+};
 
+// Blocks per SM each stage is built for (registers per thread <= 65536 /
+// (blocks x MNT)); the shared memory of both fits 5 blocks of 128 threads.
+#ifndef TLQ_MB1
+#define TLQ_MB1 5
+#endif
+#ifndef TLQ_MB2
+#define TLQ_MB2 5
+#endif
+template <int S>
+struct MixedBlocks {
+  static constexpr int value = (S == 1) ? TLQ_MB1 : TLQ_MB2;
+};
 
-__device__ __forceinline__ int cu_slot(int q) { return (q + 4 * MCU) % MCU; }
-
-struct MixedSmem {
-  double raw[MRAW][5 * MPLANE_BOX];  // TMA landing zone
-  float cu[MCU][5][MHY][MHX];         // conserved state of the ring planes (FP32)
-  float prm[NRING][5][MHY][MHX];      // primitives of the ring planes (FP32)
+// Stage 1: U arrives in FP64 (one TMA landing slot; the next plane is
+// requested as soon as this one is converted, a whole plane's work ahead of
+// its use), converted per plane to FP32 conserved values (3-plane ring: the
+// Laplacian of plane k reads k-1..k+1) and primitives (2-plane ring: the
+// faces of plane k read k and k+1).
+struct MixedSmem1 {
+  double raw[5 * MGeo<1>::PB];
+  PlaneF<1> cu[3];
+  PlaneF<1> prm[2];
   float fx[5][MTY][MTX + 1];
   float fy[5][MTY + 1][MTX];
   float fz[2][5][MTY][MTX];
-  uint64_t bar[MRAW];
+  uint64_t bar[1];
   double red[96];
   int flag;
   int abort;
 };
+// Stage 2: UPP's FP32 primitives land by TMA in a 4-plane ring (the faces of
+// plane k read k-1..k+2; plane k+3 is requested into k-1's slot once those
+// faces are done); the conserved values HLLC takes at cell centres, formed
+// from them on the faces' cross-shaped region, in a 2-plane ring (k, k+1).
+struct MixedSmem2 {
+  PlaneF<2> prm[4];
+  PlaneF<2> cu[2];
+  float fx[5][MTY][MTX + 1];
+  float fy[5][MTY + 1][MTX];
+  float fz[2][5][MTY][MTX];
+  uint64_t bar[4];
+  double red[96];
+  int flag;
+  int abort;
+};
+template <int S>
+struct MixedSmemSel;
+template <>
+struct MixedSmemSel<1> {
+  using type = MixedSmem1;
+  static constexpr int nbar = 1;
+};
+template <>
+struct MixedSmemSel<2> {
+  using type = MixedSmem2;
+  static constexpr int nbar = 4;
+};
+template <int S>
+using MixedSmem = typename MixedSmemSel<S>::type;
+
+__device__ __forceinline__ int cu_slot(int q) { return (q + 12) % 3; }
 
 // One cell: FP64 conserved (stride vs) -> FP32 conserved and primitives.
 // The pressure of a cell whose kinetic energy exceeds 0.99 of its total
@@ -200,207 +255,283 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
   u4 = u4 + f2d(__fsub_rn(w[4], p0) / gm1);
 }
 
-// One tile (MTX x MTY columns, z-chunk bz of zlen planes) of a stage: the
+// The face-ghost images of a stage-1 cell (borders(UPP, 2), boundaries.f90
+// non-MPI branches) as FP32 primitives of UPP: the FP64 image of v (normal
+// momentum negated at a reflective face) with the winds applied at the ghost
+// cell, through mixed_cell -- what stage 2 forms from UPP.
+__device__ __forceinline__ void write_ghost_prims(const Params& p, const Layout& L, float* out, float gm1, int i,
+                                                  int j, int k, const double* v) {
+  const int c3[3] = {i, j, k};
+  const int n3[3] = {p.nx, p.ny, p.nz};
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    int tgt[4], flp[4];
+    const int m = ghost_targets(2, p.bc[2 * ax], p.bc[2 * ax + 1], c3[ax], n3[ax], tgt, flp);
+    for (int q = 0; q < m; ++q) {
+      int g3[3] = {i, j, k};
+      g3[ax] = tgt[q];
+      double g[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) g[e] = (flp[q] && e == ax + 1) ? -v[e] : v[e];
+      winds_cell(p, g3[0], g3[1], g3[2], g);
+      float cf[5], w[5];
+      mixed_cell(gm1, g, 1, cf, w);
+      const long long o = L.at(g3[0], g3[1], g3[2]);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) out[e * L.plane + o] = w[e];
+    }
+  }
+}
+
+// One face flux, direction d (1 x, 2 y, 3 z), from the primitives of the
+// four cells along d (w0..w3; stage 1 reads only w1, w2) and the conserved
+// values of the two cells beside the face, each `VS` floats between
+// variables.  Every face of both stages and of the batched kernels goes
+// through this one copy of the code.
+template <int STAGE, int LIM, int SOLV, int VS>
+__device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, int d, const float* w0,
+                                          const float* w1, const float* w2, const float* w3, const float* uL,
+                                          const float* uR, float* ff) {
+  float wll[5], wl[5], wr[5], wrr[5], UL[5], UR[5];
+#pragma unroll
+  for (int e = 0; e < 5; ++e) {
+    wl[e] = w1[e * VS];
+    wr[e] = w2[e * VS];
+    UL[e] = uL[e * VS];
+    UR[e] = uR[e * VS];
+  }
+  if (STAGE == 2) {
+#pragma unroll
+    for (int e = 0; e < 5; ++e) {
+      wll[e] = w0[e * VS];
+      wrr[e] = w3[e * VS];
+    }
+    limiter(wll, wl, wr, wrr, LIM >= 0 ? LIM : p.limiter);
+  }
+  if (!riemann(SOLV >= 0 ? SOLV : p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
+#pragma unroll
+    for (int e = 0; e < 5; ++e) ff[e] = NAN;
+  }
+}
+
+// All x, y and z faces of plane k of a tile as one flat task list (x faces
+// (MTX+1) x MTY, y faces MTX x (MTY+1), z faces MTX x MTY: no face twice);
+// xy false: only the z faces (the plane below a z-chunk).  prm(q) / cu(q):
+// the planes of primitives / conserved values of plane q.
+template <int STAGE, int LIM, int SOLV, class Smem, class PrmOf, class CuOf>
+__device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, int j0, int k, bool xy, float gf,
+                                            float g1f, PrmOf prm, CuOf cu) {
+  using G = MGeo<STAGE>;
+  constexpr int OY = G::OY, PX = G::PX, VS = G::PB;
+  constexpr int NXF = (MTX + 1) * MTY, NYF = MTX * (MTY + 1), NZF = MTX * MTY;
+  const int tbeg = xy ? 0 : NXF + NYF;
+  const float* pk = prm(k);
+  const float* ck = cu(k);
+  for (int t = tbeg + (int)threadIdx.x; t < NXF + NYF + NZF; t += MNT) {
+    int d, fxl, fyl;
+    const float *w0, *w1, *w2, *w3, *uL, *uR;
+    bool valid;
+    if (t < NXF) {
+      d = 1;
+      fxl = t % (MTX + 1);
+      fyl = t / (MTX + 1);
+      w1 = pk + (fyl + OY) * PX + fxl + 1;  // cell i0 - 1 + fxl
+      w0 = w1 - 1;
+      w2 = w1 + 1;
+      w3 = w1 + 2;
+      uL = ck + (fyl + OY) * PX + fxl + 1;
+      uR = uL + 1;
+      valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
+    } else if (t < NXF + NYF) {
+      d = 2;
+      const int u = t - NXF;
+      fxl = u % MTX;
+      fyl = u / MTX;
+      w1 = pk + (fyl - 1 + OY) * PX + fxl + 2;  // cell j0 - 1 + fyl
+      w0 = w1 - PX;
+      w2 = w1 + PX;
+      w3 = w1 + 2 * PX;
+      uL = ck + (fyl - 1 + OY) * PX + fxl + 2;
+      uR = uL + PX;
+      valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
+    } else {
+      d = 3;
+      const int u = t - NXF - NYF;
+      fxl = u % MTX;
+      fyl = u / MTX;
+      const int o = (fyl + OY) * PX + fxl + 2;
+      w0 = prm(k - 1) + o;
+      w1 = pk + o;
+      w2 = prm(k + 1) + o;
+      w3 = prm(k + 2) + o;
+      uL = ck + o;
+      uR = cu(k + 1) + o;
+      valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
+    }
+    if (!valid) continue;
+    float ff[5];
+    face_flux<STAGE, LIM, SOLV, VS>(p, gf, g1f, d, w0, w1, w2, w3, uL, uR, ff);
+    if (d == 1) {
+#pragma unroll
+      for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
+    } else if (d == 2) {
+#pragma unroll
+      for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
+    }
+  }
+}
+
+// The flux divergence of tile cell (tx, ty) of plane k (minus the gravity
+// source, -dt S, when gravity is on): dU of Godunov (HLLC.f90:37-40).
+template <int STAGE, class Smem>
+__device__ __forceinline__ void flux_divergence(const Params& p, const Smem& s, int k, int tx, int ty, float dtf,
+                                                float dtdx, float dtdy, float dtdz, const float* wc, const double* ph,
+                                                float* dU) {
+  const int cur = (k + 1) & 1, prv = k & 1;
+#pragma unroll
+  for (int e = 0; e < 5; ++e)
+    dU[e] = dtdx * (s.fx[e][ty][tx + 1] - s.fx[e][ty][tx]) + dtdy * (s.fy[e][ty + 1][tx] - s.fy[e][ty][tx]) +
+            dtdz * (s.fz[cur][e][ty][tx] - s.fz[prv][e][ty][tx]);
+  if (p.gravity) {
+    // S_Solver (sources.f90:885-893) from the cell's primitives wc
+    const float fg1 = (d2f(ph[0]) - d2f(ph[1])) * p.f_hdx;
+    const float fg2 = (d2f(ph[2]) - d2f(ph[3])) * p.f_hdy;
+    const float fg3 = (d2f(ph[4]) - d2f(ph[5])) * p.f_hdz;
+    float sv[5];
+    sv[0] = 0.0f;
+    sv[1] = -wc[0] * fg1;
+    sv[2] = -wc[0] * fg2;
+    sv[3] = -wc[0] * fg3;
+    sv[4] = -wc[0] * (wc[1] * fg1 + wc[2] * fg2 + wc[3] * fg3);
+#pragma unroll
+    for (int e = 0; e < 5; ++e) dU[e] -= dtf * sv[e];
+  }
+}
+
+// Bounded TMA/mbarrier bookkeeping of one tile: every thread waits for every
+// plane in order and tracks the slots' phases; a wait that runs out sets the
+// block's abort flag.
+struct PlaneWaits {
+  uint32_t phase = 0;
+  int waited;
+  bool failed = false;
+  __device__ __forceinline__ void wait(uint64_t* bars, int nslot, int q, int* abort) {
+    if (failed) return;
+    const int slot = q & (nslot - 1);
+    if (!mbar_wait_bounded(&bars[slot], (phase >> slot) & 1u, WAIT_LIMIT)) {
+      failed = true;
+      *abort = 1;
+      return;
+    }
+    phase ^= 1u << slot;
+    waited = q;
+  }
+  // after an abort, thread 0 lets the copies it issued land (bounded)
+  __device__ __forceinline__ void drain(uint64_t* bars, int nslot, int issued) {
+    for (int q = waited + 1; q <= issued; ++q) {
+      const int slot = q & (nslot - 1);
+      mbar_wait_bounded(&bars[slot], (phase >> slot) & 1u, WAIT_LIMIT);
+      phase ^= 1u << slot;
+    }
+  }
+};
+
+// One tile (MTX x MTY columns, z-chunk bz of zlen planes) of stage 1: the
 // body of the single-mesh kernel and of each work item of the batched
-// persistent kernel.  LIM / SOLV >= 0 fix the limiter and the Riemann solver
-// at compile time (their switches fold away and the face code becomes one
-// straight block the compiler can schedule); -1 reads them from the params.  nblk / bid: the mesh's tiles and this one's index, for
-// the dt reduction.  Leaves every TMA copy it issued completed.
-template <int STAGE, int LIM = -1, int SOLV = -1>
-__device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArgs& a, MixedSmem& s, int bx, int by,
-                                           int bz, unsigned nblk, unsigned bid) {
-  constexpr int H = STAGE;
+// persistent kernel.  Streams U (FP64) with a 1-cell halo; writes UPP as
+// FP32 primitives (and its face-ghost images), and eta * Laplacian(U) in
+// FP32 for stage 2.  Leaves every TMA copy it issued completed.
+template <int LIM, int SOLV>
+__device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageArgs& a, MixedSmem1& s, int bx, int by,
+                                            int bz) {
+  using G = MGeo<1>;
   const Params& p = a.p;
   const Layout& L = a.L;
   const int tid = threadIdx.x;
   const int i0 = 1 + bx * MTX, j0 = 1 + by * MTY;
   const int k0 = 1 + bz * a.zlen;
   const int k1 = min(p.nz, k0 + a.zlen - 1);
-  Clock* clk = a.clk;
-
+  const Clock* clk = a.clk;
   if (!(clk->t < clk->tfin)) return;  // the loop condition of mainHD.f90:61 (uniform)
-  const double dtstep = clk->dt;
-  const float dtstep_f = d2f(dtstep);
-  const float dtf = (STAGE == 1) ? 0.5f * dtstep_f : dtstep_f;
+  const float dtf = 0.5f * d2f(clk->dt);  // dth = dt/2 (mainHD.f90:78)
   const float gf = p.f_gamma, gm1 = gf - 1.0f, g1f = p.f_g1;
   const float dtdx = dtf * p.f_inv_dx, dtdy = dtf * p.f_inv_dy, dtdz = dtf * p.f_inv_dz;
-  const int last_plane = k1 + H;
+  const int last = k1 + 1;
   const long long pxy = (long long)L.px * L.nyg;
 
   if (tid == 0) {
-    for (int q = 0; q < MRAW; ++q) mbar_init(&s.bar[q], 1);
+    mbar_init(&s.bar[0], 1);
     s.abort = 0;
     fence_mbar_init();
   }
   __syncthreads();
-
-  int issued = k0 - H - 1;
-  auto issue = [&](int q) {
-    const int slot = raw_slot(q);
+  int issued = k0 - 2;
+  auto issue = [&](int q) {  // thread 0
     fence_proxy_async();
-    mbar_arrive_expect_tx(&s.bar[slot], 5u * MPLANE_BOX * 8u);
-    tma_load_4d(s.raw[slot], tm, &s.bar[slot], bx * MTX, by * MTY, q + 1, 0);
+    mbar_arrive_expect_tx(&s.bar[0], 5u * G::PB * 8u);
+    tma_load_4d(s.raw, tm, &s.bar[0], bx * MTX, by * MTY + 1, q + 1, 0);
     issued = q;
   };
-  uint32_t phase = 0;
-  int waited = k0 - H - 1;
-  bool failed = false;
-  auto wait_plane = [&](int q) {
-    if (failed) return;
-    const int slot = raw_slot(q);
-    if (!mbar_wait_bounded(&s.bar[slot], (phase >> slot) & 1u, WAIT_LIMIT)) {
-      failed = true;
-      s.abort = 1;
-      return;
-    }
-    phase ^= 1u << slot;
-    waited = q;
-  };
-
+  PlaneWaits pw;
+  pw.waited = k0 - 2;
+  // U of plane q (landed) -> FP32 conserved and primitives on the cells its
+  // faces and Laplacian read
   auto convert = [&](int q) {
-    const double* r0 = s.raw[raw_slot(q)];
-    const int sl = q & 3, sc = cu_slot(q);
-    constexpr int RW = MTX + 2 * H;
-    constexpr int NROW = RW * MTY, NCOL = MTX * 2 * H;
+    float* C = &s.cu[cu_slot(q)].v[0][0][0];
+    float* W = &s.prm[q & 1].v[0][0][0];
+    constexpr int NROW = (MTX + 2) * MTY, NCOL = 2 * MTX;
     for (int t = tid; t < NROW + NCOL; t += MNT) {
       int lx, ly;
       if (t < NROW) {
-        lx = 2 - H + t % RW;
-        ly = 2 + t / RW;
+        lx = 1 + t % (MTX + 2);
+        ly = 1 + t / (MTX + 2);
       } else {
-        const int u = t - NROW, r2 = u / MTX;
+        const int u = t - NROW;
         lx = 2 + u % MTX;
-        ly = (r2 < H) ? (2 - H + r2) : (MTY + 2 + r2 - H);
+        ly = (u < MTX) ? 0 : MTY + 1;
       }
+      const int o = ly * G::PX + lx;
       float cf[5], w[5];
-      mixed_cell(gm1, r0 + ly * MHX + lx, MPLANE_BOX, cf, w);
+      mixed_cell(gm1, s.raw + o, G::PB, cf, w);
 #pragma unroll
       for (int e = 0; e < 5; ++e) {
-        s.cu[sc][e][ly][lx] = cf[e];
-        s.prm[sl][e][ly][lx] = w[e];
+        C[e * G::PB + o] = cf[e];
+        W[e * G::PB + o] = w[e];
       }
     }
   };
+  auto prm = [&](int q) { return &s.prm[q & 1].v[0][0][0]; };
+  auto cu = [&](int q) { return &s.cu[cu_slot(q)].v[0][0][0]; };
 
-  auto faces = [&](int k, bool xy) {
-    constexpr int NXF = (MTX + 1) * MTY, NYF = MTX * (MTY + 1), NZF = MTX * MTY;
-    const int tbeg = xy ? 0 : NXF + NYF;
-    const int sk = k & 3;
-    constexpr int VS = MPLANE_BOX;
-    for (int t = tbeg + tid; t < NXF + NYF + NZF; t += MNT) {
-      int d, fxl, fyl;
-      const float *w0, *w1, *w2, *w3, *uL, *uR;
-      bool valid;
-      if (t < NXF) {
-        d = 1;
-        fxl = t % (MTX + 1);
-        fyl = t / (MTX + 1);
-        const int ly = fyl + 2;
-        w0 = &s.prm[sk][0][ly][fxl];
-        w1 = w0 + 1; w2 = w0 + 2; w3 = w0 + 3;
-        uL = &s.cu[cu_slot(k)][0][ly][fxl + 1];
-        uR = uL + 1;
-        valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
-      } else if (t < NXF + NYF) {
-        d = 2;
-        const int u = t - NXF;
-        fxl = u % MTX;
-        fyl = u / MTX;
-        const int lx = fxl + 2;
-        w0 = &s.prm[sk][0][fyl][lx];
-        w1 = w0 + MHX; w2 = w0 + 2 * MHX; w3 = w0 + 3 * MHX;
-        uL = &s.cu[cu_slot(k)][0][fyl + 1][lx];
-        uR = uL + MHX;
-        valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
-      } else {
-        d = 3;
-        const int u = t - NXF - NYF;
-        fxl = u % MTX;
-        fyl = u / MTX;
-        const int lx = fxl + 2, ly = fyl + 2;
-        w0 = &s.prm[(k - 1) & 3][0][ly][lx];
-        w1 = &s.prm[k & 3][0][ly][lx];
-        w2 = &s.prm[(k + 1) & 3][0][ly][lx];
-        w3 = &s.prm[(k + 2) & 3][0][ly][lx];
-        uL = &s.cu[cu_slot(k)][0][ly][lx];
-        uR = &s.cu[cu_slot(k + 1)][0][ly][lx];
-        valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
-      }
-      if (!valid) continue;
-      float wll[5], wl[5], wr[5], wrr[5], UL[5], UR[5], ff[5];
-#pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        wl[e] = w1[e * VS];
-        wr[e] = w2[e * VS];
-        UL[e] = uL[e * VS];
-        UR[e] = uR[e * VS];
-      }
-      if (STAGE == 2) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) {
-          wll[e] = w0[e * VS];
-          wrr[e] = w3[e * VS];
-        }
-        limiter(wll, wl, wr, wrr, LIM >= 0 ? LIM : p.limiter);
-      }
-      if (!riemann(SOLV >= 0 ? SOLV : p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) ff[e] = NAN;
-      }
-      if (d == 1) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
-      } else if (d == 2) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
-      } else {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
-      }
-    }
-  };
-
-  // ---- prologue: planes k0-H .. k0+H-1 ---------------------------------------
-  if (tid == 0)
-    for (int q = k0 - H; q <= min(k0 - H + MRAW - 1, last_plane); ++q) issue(q);
+  // prologue: planes k0-1 and k0
   bool aborted = false;
-  for (int q = k0 - H; q <= k0 + H - 1; ++q) {
-    wait_plane(q);
+  for (int q = k0 - 1; q <= k0; ++q) {
+    if (tid == 0) issue(q);
+    pw.wait(s.bar, 1, q, &s.abort);
     convert(q);
     __syncthreads();
     if (s.abort) { aborted = true; break; }
-    if (tid == 0 && q + MRAW <= last_plane && q + MRAW > issued) issue(q + MRAW);
   }
+  if (!aborted && tid == 0 && k0 + 1 <= last) issue(k0 + 1);
 
   const int tx = tid % MTX, ty = tid / MTX;
   const int i = i0 + tx, j = j0 + ty;
   const bool cell_ok = (ty < MTY) && (i <= p.nx) && (j <= p.ny);
-  float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
-  unsigned nsingle = 0;  // stage 2 with the surrogate: cells cooled in a single step
-  const float cT = p.f_cT;
-  const float inv_muamu = p.f_inv_muamu;
   const float etaf = p.f_eta;
-  const float hdx = p.f_hdx, hdy = p.f_hdy, hdz = p.f_hdz;
-
   // k = k0 - 1 computes only the z face below the chunk, through the same
   // (single) copy of the face code as every other plane, so that a cell's
   // arithmetic does not depend on where the z-chunks begin
   for (int k = k0 - 1; k <= k1 && !aborted; ++k) {
     const bool first = k < k0;
-    // Global operands of this cell's update, requested now so that their
-    // latency hides behind the conversion and face phases.
     const long long c = L.at(i, j, k);
     double uc[5];
-    float lv[5];
     double ph[6];
-    bool queued = false;  // stage 2 with the surrogate: handed to the cooling passes
     if (cell_ok && !first) {
 #pragma unroll
       for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
-      if (STAGE == 2) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) lv[e] = a.lapf[e * L.plane + c];
-      }
       if (p.gravity) {
         ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
         ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
@@ -408,120 +539,234 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
       }
     }
     if (!first) {
-      wait_plane(k + H);
-      // stage 1: the previous plane's Laplacian read the ring slot this
-      // conversion overwrites (a 3-plane ring)
-      if (STAGE == 1) __syncthreads();
-      convert(k + H);
-      __syncthreads();  // S1
+      pw.wait(s.bar, 1, k + 1, &s.abort);
+      __syncthreads();  // the previous plane's epilogue read the ring slots this conversion overwrites
+      convert(k + 1);
+      __syncthreads();
       if (s.abort) { aborted = true; break; }
-      if (tid == 0 && k + H + MRAW <= last_plane && k + H + MRAW > issued) issue(k + H + MRAW);
+      if (tid == 0 && k + 2 <= last) issue(k + 2);
     }
-    faces(k, !first);
-    __syncthreads();  // S2
+    mixed_faces<1, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, prm, cu);
+    __syncthreads();
+    if (first || !cell_ok) continue;
+
+    const int lx = tx + 2, ly = ty + 1;
+    float wc[5];
+#pragma unroll
+    for (int e = 0; e < 5; ++e) wc[e] = s.prm[k & 1].v[e][ly][lx];
+    float dU[5];
+    flux_divergence<1>(p, s, k, tx, ty, dtf, dtdx, dtdy, dtdz, wc, ph, dU);
+    // FP64 accumulation: UPP = U - dU (Godunov's centre value is U)
+    double up[5];
+#pragma unroll
+    for (int e = 0; e < 5; ++e) up[e] = uc[e] - f2d(dU[e]);
+    // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U this
+    // stage streams (= the old U of stage 2), in FP32 from the ring
+    {
+      const float* A0 = cu(k - 1);
+      const float* A1 = cu(k);
+      const float* A2 = cu(k + 1);
+      const int o = ly * G::PX + lx;
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        const int oe = e * G::PB + o;
+        const float lap = ((A1[oe + 1] + A1[oe - 1]) + (A1[oe + G::PX] + A1[oe - G::PX])) +
+                          ((A2[oe] + A0[oe]) - 6.0f * A1[oe]);
+        a.lapf[e * L.plane + c] = etaf * lap;
+      }
+    }
+    if (near_boundary_or_wind(p, i, j, k)) {
+      write_ghost_prims(p, L, a.uppf, gm1, i, j, k, up);  // borders(UPP, 2)
+      winds_cell(p, i, j, k, up);
+    }
+    float cf[5], w[5];
+    mixed_cell(gm1, up, 1, cf, w);  // UPP's primitives, as stage 2 reads them
+#pragma unroll
+    for (int e = 0; e < 5; ++e) a.uppf[e * L.plane + c] = w[e];
+  }
+  if (aborted && tid == 0) {
+    atomicOr(&const_cast<Clock*>(clk)->status, ST_TIMEOUT);
+    pw.drain(s.bar, 1, issued);
+  }
+}
+
+// One tile of stage 2: streams UPP's FP32 primitives with a 2-cell halo;
+// writes U of the next step (FP64) and its face-ghost images, cools, and
+// reduces the signal speeds for the next dt.  nblk / bid: the mesh's tiles
+// and this one's index, for the dt reduction.  Leaves every TMA copy it
+// issued completed.
+template <int LIM, int SOLV>
+__device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageArgs& a, MixedSmem2& s, int bx, int by,
+                                            int bz, unsigned nblk, unsigned bid) {
+  using G = MGeo<2>;
+  const Params& p = a.p;
+  const Layout& L = a.L;
+  const int tid = threadIdx.x;
+  const int i0 = 1 + bx * MTX, j0 = 1 + by * MTY;
+  const int k0 = 1 + bz * a.zlen;
+  const int k1 = min(p.nz, k0 + a.zlen - 1);
+  Clock* clk = a.clk;
+  if (!(clk->t < clk->tfin)) return;  // the loop condition of mainHD.f90:61 (uniform)
+  const float dtf = d2f(clk->dt);
+  const float gf = p.f_gamma, gm1 = gf - 1.0f, g1f = p.f_g1;
+  const float igm1 = __frcp_rn(gm1);
+  const float dtdx = dtf * p.f_inv_dx, dtdy = dtf * p.f_inv_dy, dtdz = dtf * p.f_inv_dz;
+  const int last = k1 + 2;
+  const long long pxy = (long long)L.px * L.nyg;
+
+  if (tid == 0) {
+    for (int q = 0; q < 4; ++q) mbar_init(&s.bar[q], 1);
+    s.abort = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+  int issued = k0 - 3;
+  auto issue = [&](int q) {  // thread 0: plane q into slot q & 3
+    const int slot = q & 3;
+    fence_proxy_async();
+    mbar_arrive_expect_tx(&s.bar[slot], 5u * G::PB * 4u);
+    tma_load_4d(&s.prm[slot], tm, &s.bar[slot], bx * MTX, by * MTY, q + 1, 0);
+    issued = q;
+  };
+  PlaneWaits pw;
+  pw.waited = k0 - 3;
+  auto prm = [&](int q) { return &s.prm[q & 3].v[0][0][0]; };
+  auto cu = [&](int q) { return &s.cu[q & 1].v[0][0][0]; };
+  // conserved values of plane q (landed) on the cells beside its faces
+  auto conserved = [&](int q) {
+    const float* W = prm(q);
+    float* C = &s.cu[q & 1].v[0][0][0];
+    constexpr int NROW = (MTX + 2) * MTY, NCOL = 2 * MTX;
+    for (int t = tid; t < NROW + NCOL; t += MNT) {
+      int lx, ly;
+      if (t < NROW) {
+        lx = 1 + t % (MTX + 2);
+        ly = 2 + t / (MTX + 2);
+      } else {
+        const int u = t - NROW;
+        lx = 2 + u % MTX;
+        ly = (u < MTX) ? 1 : MTY + 2;
+      }
+      const int o = ly * G::PX + lx;
+      const float r = W[o], vx = W[G::PB + o], vy = W[2 * G::PB + o], vz = W[3 * G::PB + o], pr = W[4 * G::PB + o];
+      const float k2 = __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx)));
+      C[o] = r;
+      C[G::PB + o] = __fmul_rn(r, vx);
+      C[2 * G::PB + o] = __fmul_rn(r, vy);
+      C[3 * G::PB + o] = __fmul_rn(r, vz);
+      C[4 * G::PB + o] = __fmaf_rn(pr, igm1, __fmul_rn(__fmul_rn(0.5f, r), k2));
+    }
+  };
+
+  // prologue: planes k0-2 .. k0+1 (the first z face, k0 - 1/2, reads them)
+  if (tid == 0)
+    for (int q = k0 - 2; q <= k0 + 1; ++q) issue(q);
+  for (int q = k0 - 2; q <= k0 + 1; ++q) pw.wait(s.bar, 4, q, &s.abort);
+  conserved(k0 - 1);
+
+  const int tx = tid % MTX, ty = tid / MTX;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool cell_ok = (ty < MTY) && (i <= p.nx) && (j <= p.ny);
+  float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
+  unsigned nsingle = 0;  // with the surrogate: cells cooled in a single step
+  const float cT = p.f_cT;
+  const float inv_muamu = p.f_inv_muamu;
+  bool aborted = false;
+  for (int k = k0 - 1; k <= k1; ++k) {
+    const bool first = k < k0;
+    // Global operands of this cell's update, requested now so that their
+    // latency hides behind the face phase.
+    const long long c = L.at(i, j, k);
+    double uc[5];
+    float lv[5];
+    double ph[6];
+    bool queued = false;  // with the surrogate: handed to the cooling passes
+    if (cell_ok && !first) {
+#pragma unroll
+      for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) lv[e] = a.lapf[e * L.plane + c];
+      if (p.gravity) {
+        ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
+        ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
+        ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
+      }
+    }
+    if (!first) pw.wait(s.bar, 4, k + 2, &s.abort);
+    conserved(k + 1);
+    __syncthreads();
+    if (s.abort) { aborted = true; break; }
+    mixed_faces<2, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, prm, cu);
+    __syncthreads();
+    if (tid == 0 && k + 3 <= last) issue(k + 3);  // into plane k-1's slot: its faces are done
     if (first) continue;
 
     if (cell_ok) {
-      const int cur = (k + 1) & 1, prv = k & 1;
+      float wc[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) wc[e] = s.prm[k & 3].v[e][ty + 2][tx + 2];
       float dU[5];
-#pragma unroll
-      for (int e = 0; e < 5; ++e)
-        dU[e] = dtdx * (s.fx[e][ty][tx + 1] - s.fx[e][ty][tx]) + dtdy * (s.fy[e][ty + 1][tx] - s.fy[e][ty][tx]) +
-                dtdz * (s.fz[cur][e][ty][tx] - s.fz[prv][e][ty][tx]);
-      if (p.gravity) {
-        float w[5], sv[5];
-#pragma unroll
-        for (int e = 0; e < 5; ++e) w[e] = s.prm[k & 3][e][ty + 2][tx + 2];
-        const float fg1 = (d2f(ph[0]) - d2f(ph[1])) * hdx;
-        const float fg2 = (d2f(ph[2]) - d2f(ph[3])) * hdy;
-        const float fg3 = (d2f(ph[4]) - d2f(ph[5])) * hdz;
-        sv[0] = 0.0f;
-        sv[1] = -w[0] * fg1;
-        sv[2] = -w[0] * fg2;
-        sv[3] = -w[0] * fg3;
-        sv[4] = -w[0] * (w[1] * fg1 + w[2] * fg2 + w[3] * fg3);
-#pragma unroll
-        for (int e = 0; e < 5; ++e) dU[e] -= dtf * sv[e];
-      }
-      // FP64 accumulation: U' = U - dU (Godunov's centre value is U in both
-      // stages; `uold` is the stage-1 input and the stage-2 old state)
-      // Stage 2 away from the boundaries and the winds (which read or
-      // overwrite UP): U = U_old - dU + eta Lap in one FP64 addition of the
-      // FP32 increment (an FP64 addition costs ~64 FP32 slots on GB300).
-      // (the gate also keeps the winds' FP64 distance and density, which the
-      // compiler would otherwise evaluate for every cell, off the FP64 pipe)
+      flux_divergence<2>(p, s, k, tx, ty, dtf, dtdx, dtdy, dtdz, wc, ph, dU);
+      // FP64 accumulation: UP = U - dU (Godunov's centre value is the old U).
+      // Away from the boundaries and the winds (which read or overwrite UP):
+      // U = U_old - dU + eta Lap in one FP64 addition of the FP32 increment
+      // (an FP64 addition costs ~64 FP32 slots on GB300; the gate also keeps
+      // the winds' FP64 distance and density off the FP64 pipe)
       const bool special = near_boundary_or_wind(p, i, j, k);
-      const bool plain2 = STAGE == 2 && !special;
-      double up[5];
+      double un[5];
+      if (!special) {
 #pragma unroll
-      for (int e = 0; e < 5; ++e) up[e] = plain2 ? uc[e] : uc[e] - f2d(dU[e]);
-      if (STAGE == 1) {
-        // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U
-        // this stage streams (= the old U of stage 2), in FP32 from the ring
-        const int a0 = cu_slot(k - 1), a1 = cu_slot(k), a2 = cu_slot(k + 1);
-        const int lx = tx + 2, ly = ty + 2;
-#pragma unroll
-        for (int e = 0; e < 5; ++e) {
-          const float lap = ((s.cu[a1][e][ly][lx + 1] + s.cu[a1][e][ly][lx - 1]) +
-                             (s.cu[a1][e][ly + 1][lx] + s.cu[a1][e][ly - 1][lx])) +
-                            ((s.cu[a2][e][ly][lx] + s.cu[a0][e][ly][lx]) - 6.0f * s.cu[a1][e][ly][lx]);
-          a.lapf[e * L.plane + c] = etaf * lap;
-        }
-      }
-      if (special) {
-        write_ghosts(p, L, a.out, STAGE == 1 ? 2 : 1, i, j, k, up);
-        winds_cell(p, i, j, k, up);
-      }
-      if (STAGE == 1) {
-#pragma unroll
-        for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = up[e];
+        for (int e = 0; e < 5; ++e) un[e] = uc[e] + f2d(lv[e] - dU[e]);
       } else {
+        double up[5];
+#pragma unroll
+        for (int e = 0; e < 5; ++e) up[e] = uc[e] - f2d(dU[e]);
+        write_ghosts(p, L, a.out, 1, i, j, k, up);  // borders(UP, 1) with the winds
+        winds_cell(p, i, j, k, up);
         // step: U = UP + eta * (Laplacian of the old U), from stage 1
-        double un[5];
 #pragma unroll
-        for (int e = 0; e < 5; ++e) un[e] = plain2 ? up[e] + f2d(lv[e] - dU[e]) : up[e] + f2d(lv[e]);
-        float cf[5], w[5];
-        mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
-        if (p.cooling == COOL_MLP) {
-          // A cell whose tau (Lambda n^2 dt / E_th, formed as the cooling
-          // passes form it) is at most the integrator's sub-step takes the
-          // exact integrator's single exponential step here (the passes would
-          // do the same); the passes cool the others and take their signal
-          // speeds.
-          const float T = (w[4] / w[0]) * cT;
-          if (cools_at(p, T, un)) {
-            const float nd = w[0] * inv_muamu;
-            const float eth = w[4] / gm1;
-            const float lam = cool_coef_f(p.cool, T);
-            const float tau = (lam * nd) * (nd / eth) * dtstep_f;
-            if (tau > p.f_cool_sub_frac) {
-              queued = true;
-            } else {
-              cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
-              ++nsingle;
-            }
+        for (int e = 0; e < 5; ++e) un[e] = up[e] + f2d(lv[e]);
+      }
+      float cf[5], w[5];
+      mixed_cell(gm1, un, 1, cf, w);  // calc_prims(UPrim, U)
+      if (p.cooling == COOL_MLP) {
+        // A cell whose tau (Lambda n^2 dt / E_th, formed as the cooling
+        // passes form it) is at most the single-step limit takes the exact
+        // integrator's single exponential step here (the passes would do the
+        // same); the passes cool the others and take their signal speeds.
+        const float T = (w[4] / w[0]) * cT;
+        if (cools_at(p, T, un)) {
+          const float nd = w[0] * inv_muamu;
+          const float eth = w[4] / gm1;
+          const float lam = cool_coef_f(p.cool, T);
+          const float tau = (lam * nd) * (nd / eth) * dtf;
+          if (tau > p.f_cool_sub_frac) {
+            queued = true;
+          } else {
+            cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtf, un);
+            ++nsingle;
           }
-        } else if (p.cooling != COOL_NONE) {
-          cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtstep_f, un);
         }
-        {
-          // !(rho > 0) on the bits (no FP64 compare): sign set, zero or
-          // below the normal range, or not finite
-          const int hi = __double2hiint(un[0]);
-          if (hi < 0x00100000 || (hi & 0x7ff00000) == 0x7ff00000) atomicOr(&clk->status, ST_NEG_DENSITY);
-        }
+      } else if (p.cooling != COOL_NONE) {
+        cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtf, un);
+      }
+      {
+        // !(rho > 0) on the bits (no FP64 compare): sign set, zero or
+        // below the normal range, or not finite
+        const int hi = __double2hiint(un[0]);
+        if (hi < 0x00100000 || (hi & 0x7ff00000) == 0x7ff00000) atomicOr(&clk->status, ST_NEG_DENSITY);
+      }
 #pragma unroll
-        for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
-        if (!queued) {
-          const float cs = sqrtf(gf * w[4] / w[0]);
-          const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
-          m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
-          m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
-          m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
-        }
+      for (int e = 0; e < 5; ++e) a.out[e * L.plane + c] = un[e];
+      if (!queued) {
+        const float cs = sqrtf(gf * w[4] / w[0]);
+        const float v0 = fabsf(w[1]) + cs, v1 = fabsf(w[2]) + cs, v2 = fabsf(w[3]) + cs;
+        m0 = (v0 != v0 || v0 > m0) ? v0 : m0;
+        m1 = (v1 != v1 || v1 > m1) ? v1 : m1;
+        m2 = (v2 != v2 || v2 > m2) ? v2 : m2;
       }
     }
-    if (STAGE == 2 && p.cooling == COOL_MLP) {
+    if (p.cooling == COOL_MLP) {
       // warp-aggregated append to the cooling queue (interior cell index)
       const unsigned qm = __ballot_sync(0xffffffffu, queued);
       if (qm) {
@@ -540,38 +785,41 @@ __device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArg
   if (aborted) {
     if (tid == 0) {
       atomicOr(&clk->status, ST_TIMEOUT);
-      for (int q = waited + 1; q <= issued; ++q) {
-        const int slot = raw_slot(q);
-        mbar_wait_bounded(&s.bar[slot], (phase >> slot) & 1u, WAIT_LIMIT);
-        phase ^= 1u << slot;
-      }
+      pw.drain(s.bar, 4, issued);
     }
     d0 = d1 = d2 = NAN;
   }
-  if (STAGE == 2 && p.cooling == COOL_MLP && a.cool_counts) {
+  if (p.cooling == COOL_MLP && a.cool_counts) {
     unsigned v = nsingle;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if ((tid & 31) == 0 && v) atomicAdd(&a.cool_counts[2], (unsigned long long)v);
   }
-  if (STAGE == 2) {
-    if (p.cooling != COOL_MLP) {
-      cfl_reduce_finalize_n<MNT>(d0, d1, d2, clk, p, true, s.red, &s.flag, nblk);
-    } else {
-      // with the surrogate the cooling passes finish the reduction over
-      // these block maxima and their own
-      cfl_contribute<MNT>(d0, d1, d2, clk, s.red);
-    }
+  if (p.cooling != COOL_MLP) {
+    cfl_reduce_finalize_n<MNT>(d0, d1, d2, clk, p, true, s.red, &s.flag, nblk);
+  } else {
+    // with the surrogate the cooling passes finish the reduction over
+    // these block maxima and their own
+    cfl_contribute<MNT>(d0, d1, d2, clk, s.red);
   }
 }
 
 template <int STAGE, int LIM = -1, int SOLV = -1>
-__global__ void __launch_bounds__(MNT, MIXED_BLOCKS_PER_SM)
+__device__ __forceinline__ void mixed_tile(const CUtensorMap* tm, const StageArgs& a, MixedSmem<STAGE>& s, int bx,
+                                           int by, int bz, unsigned nblk, unsigned bid) {
+  if constexpr (STAGE == 1)
+    mixed_tile1<LIM, SOLV>(tm, a, s, bx, by, bz);
+  else
+    mixed_tile2<LIM, SOLV>(tm, a, s, bx, by, bz, nblk, bid);
+}
+
+template <int STAGE, int LIM = -1, int SOLV = -1>
+__global__ void __launch_bounds__(MNT, MixedBlocks<STAGE>::value)
     stage_kernel_mixed(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ StageArgs a) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
-  MixedSmem& s = *reinterpret_cast<MixedSmem*>(smem_bytes);
+  MixedSmem<STAGE>& s = *reinterpret_cast<MixedSmem<STAGE>*>(smem_bytes);
   mixed_tile<STAGE, LIM, SOLV>(&tm_in, a, s, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z,
-                    blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
+                               blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
 }
 
 }  // namespace tlq

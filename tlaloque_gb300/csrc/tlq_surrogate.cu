@@ -292,9 +292,14 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
       // the exact integrator's change and the network's, T_new/T - 1 (the
       // network's r: ln(T_new/T) = -(tau + tau^2 r); clamped at the table's
       // first temperature, where cooling stops)
+      // A cell whose cooling reaches the table's first temperature within
+      // the step (the exact change is the floor's, T_0/T - 1) takes the exact
+      // integrator: training leaves those pairs out, and the network's
+      // prediction, clamped at the floor, could only err on one side.
+      const float qfloor = __fsub_rn(tab.Tf[0] / T, 1.0f);
       const float qx = cool_exact_dropf(tab, T, c.lam, tau);
-      const float qf = fmaxf(expm1f(-(1.0f + tau * y) * tau), __fsub_rn(tab.Tf[0] / T, 1.0f));
-      ok = fabsf(qf - qx) <= p.f_mlp_tol;
+      const float qf = fmaxf(expm1f(-(1.0f + tau * y) * tau), qfloor);
+      ok = qx > qfloor && fabsf(qf - qx) <= p.f_mlp_tol;
       if (ok) {
         const float dp = __fmul_rn(c.w[4], qf);
         c.w[4] = __fadd_rn(c.w[4], dp);
