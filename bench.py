@@ -115,22 +115,27 @@ def make_workload(name: str):
     return cfg, U0, desc
 
 
-def bytes_per_zone(cfg, mixed: bool = False, surrogate: bool = False) -> dict:
-    """Algorithmic HBM bytes per zone-update of each stage kernel (FP64 state:
-    5 conserved variables x 8 B; the plain form carries the cooled interior
-    pressure (8 B written by stage 2, read by stage 1; the mixed form
-    recomputes it, and moves the viscosity Laplacian into stage 1 as an FP32
-    plane); point gravity reads phi once per stage).  With the surrogate the
-    cooling passes read and write only the cells stage 2 queued (those
-    cooling beyond a single step): their bytes scale with those cells, not
-    with the mesh, and are not counted per zone-update."""
+def bytes_per_zone(cfg, mixed: bool = False) -> dict:
+    """HBM bytes per zone-update of each stage kernel.  "alg": the scheme's
+    compulsory state traffic -- stage 1 reads U (40 B FP64) and writes UPP,
+    stage 2 reads UPP and U and writes the new U; UPP is FP32 (20 B) in the
+    mixed form, FP64 (40 B) in the plain one; point gravity reads the
+    potential (8 B) in each stage.  "moved": what the kernels must move on top
+    of that: the mixed form's viscosity term, eta Lap(U), formed by stage 1
+    from the U planes it streams and read by stage 2 (FP32, 20 B each way);
+    the plain form's carried cooled pressure (8 B each way).  Ghost and halo
+    re-reads are not counted (they lower the achieved fraction).  With the
+    surrogate the cooling passes read and write only the cells stage 2 queued
+    (those cooling beyond a single step): their bytes scale with those cells,
+    not with the mesh, and are not counted per zone-update."""
     from tlaloque_gb300 import tlq
-    cool = cfg.cooling != tlq.COOL_NONE and not mixed
-    grav = cfg.masses is not None and len(cfg.masses) > 0
-    lap = 20 if mixed else 0  # mixed: stage 1 writes eta*Lap(U) in FP32, stage 2 reads it
-    s1 = 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)        # U in, UPP out
-    s2 = 40 + 40 + 40 + lap + (8 if cool else 0) + (8 if grav else 0)   # UPP, U in; U out
-    return {"stage1": s1, "stage2": s2, "step": s1 + s2}
+    grav = 8 if ((cfg.masses is not None and len(cfg.masses) > 0) or getattr(cfg, "self_gravity", 0)) else 0
+    upp = 20 if mixed else 40
+    alg = {"stage1": 40 + upp + grav, "stage2": upp + 40 + 40 + grav}
+    extra = 20 if mixed else (8 if cfg.cooling != tlq.COOL_NONE else 0)
+    moved = {k: v + extra for k, v in alg.items()}
+    return {"alg": {**alg, "step": alg["stage1"] + alg["stage2"]},
+            "moved": {**moved, "step": moved["stage1"] + moved["stage2"]}}
 
 
 class ClockSampler:
@@ -402,7 +407,6 @@ def main():
     cfg, U0, desc = make_workload(args.workload)
     cfg.device = local
     peak, peak_kind = load_peaks()
-    bpz = bytes_per_zone(cfg)
     stream = torch.cuda.Stream()
     forms = {}
     import tempfile
@@ -514,7 +518,7 @@ def main():
              "mixed_vs_fp64": accuracy(mix, f64)}
     # the plain form's bound: the FP64 pipe (measured here, with the oracle's
     # op counts) next to its HBM fraction
-    bpz64 = bytes_per_zone(cfg)
+    bpz64 = bytes_per_zone(cfg)["alg"]
     forms["fp64"]["roofline"] = {
         "hbm_achieved_gbs": bpz64["step"] * f64["value"] / 1e9,
         "hbm_frac": bpz64["step"] * f64["value"] / 1e9 / peak}
@@ -567,14 +571,17 @@ def main():
     k1, k2 = mix["k1"], mix["k2"]
     dom = "stage2" if k2 >= k1 else "stage1"
     kms = max(k1, k2)
-    bpz_m = bytes_per_zone(cfg, mixed=True, surrogate=surrogate is not None)
+    bpz = bytes_per_zone(cfg, mixed=True)
+    bpz_m = bpz["alg"]
     achieved = bpz_m[dom] * cfg.cells / (kms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": f"stage_kernel_mixed<{2 if dom == 'stage2' else 1}>",
                 "ms_cool_passes": mix["kc"],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if peak_kind == "measured"
                 else peak_kind,
-                "traffic": None, "bytes_per_zone": bpz_m, "ms_stage1": k1, "ms_stage2": k2}
+                "traffic": None, "bytes_per_zone": bpz_m, "bytes_per_zone_moved": bpz["moved"],
+                "achieved_moved": bpz["moved"][dom] * cfg.cells / (kms / 1e3) / 1e9,
+                "ms_stage1": k1, "ms_stage2": k2}
     if mix["kg"] > 0:
         roofline["ms_multigrid"] = mix["kg"]
     try:

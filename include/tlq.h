@@ -120,14 +120,18 @@ typedef struct tlq_plane_wind {
  * 3-64-64-64-1 SiLU network maps (log10 n, log10 T, log10 tau), tau =
  * Lambda(T) n^2 dt / E_th the step's cooling number, to r with
  * ln(T/T_new) = tau (1 + tau r) (exact to first order in tau whatever r is).
- * It is trained on the GPU on pairs from the sub-cycled integrator (sub-steps
- * of sub_frac and sub_frac/2, Richardson-extrapolated in ln T, which
- * converges to the exact integrator).  In the step a cell whose tau exceeds
- * the context's cool_sub_frac and lies inside the training box takes
+ * It is trained on the GPU on pairs from the exact integrator (the sub-cycled
+ * integrator's limit of infinitely many sub-steps, in closed form; pairs from
+ * the sub-cycled integrator itself, sub-steps of sub_frac and sub_frac/2
+ * Richardson-extrapolated, remain available but keep a one-sided error of
+ * ~1e-5 T where cooling runs away, which a network trained on them
+ * inherits).  In the step a cell whose tau exceeds the context's
+ * cool_sub_frac and lies inside the training box takes
  * T_pred = max(T exp(-tau (1 + tau r)), T_0) when the a-posteriori energy
  * residual |T_pred - T_ex|/T <= cool_mlp_tol, T_ex the exact integrator's
- * temperature (TLQ_COOL_EXACT's closed form); every other such cell takes
- * T_ex.  Training ignores the pairs that reach the table's first temperature
+ * temperature (TLQ_COOL_EXACT's closed form), and its cooling does not reach
+ * the table's first temperature T_0 within the step; every other such cell
+ * takes T_ex.  Training ignores the pairs that reach the table's first temperature
  * T_0 within the step and weighs pairs with tau < 1e-5 by (tau/1e-5)^2 (their
  * r is lost to FP64 round-off). */
 #define TLQ_MLP_NPARAM 8641
@@ -139,8 +143,9 @@ typedef struct tlq_surrogate_opts {
   unsigned long long seed;
   double box[6];           /* training box: log10 n, log10 T, log10 tau (lo, hi pairs;
                               default -4 4, 4 8.5, -8 1) */
-  double sub_frac;         /* exact integrator: max tau per sub-step (default 2e-3) */
-  int max_sub;             /* exact integrator: max sub-steps (default 20000) */
+  double sub_frac;         /* the pairs' integrator: 0 (default) the exact closed form, > 0 the
+                              sub-cycled one with sub-steps of at most this tau, extrapolated */
+  int max_sub;             /* sub-cycled pairs: max sub-steps (default 20000) */
 } tlq_surrogate_opts;
 
 typedef struct tlq_surrogate_report {
@@ -236,9 +241,11 @@ void tlq_surrogate_opts_default(tlq_surrogate_opts* opts);
 int tlq_train_cooling_surrogate(tlq_ctx* ctx, const tlq_surrogate_opts* opts, tlq_surrogate_report* report);
 int tlq_get_cooling_surrogate(tlq_ctx* ctx, float* params, float* norm6, double* box6);
 int tlq_set_cooling_surrogate(tlq_ctx* ctx, const float* params, const float* norm6, const double* box6);
-/* Training pairs from the exact integrator (context's table and physics,
- * sub-steps sub_frac/max_sub): X = raw features (3 per pair), Y = targets,
- * raw = (n, T, T_new, dt) per pair (may be NULL).  Host arrays. */
+/* Training pairs (context's table and physics) from the exact integrator's
+ * closed form (sub_frac 0) or from the sub-cycled integrator (sub-steps of
+ * at most sub_frac and sub_frac/2, at most max_sub, extrapolated): X = raw
+ * features (3 per pair), Y = targets, raw = (n, T, T_new, dt) per pair (may
+ * be NULL).  Host arrays. */
 int tlq_cooling_pairs(tlq_ctx* ctx, long long n, unsigned long long seed, const double* box6, double sub_frac,
                       int max_sub, float* X, float* Y, double* raw);
 /* Context-free network pieces on host arrays (normalised features): loss

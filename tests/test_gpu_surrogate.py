@@ -278,3 +278,27 @@ def test_surrogate_gain_over_sub_cycling(trained):
     e_tight = rel_l1(eth(tight), eth(exact))
     print(f"clumpy48 tol 1e-5: err {e_tight:.3e} network {tight['mlp']} fallback {tight['fb']}")
     assert e_tight <= e_mlp and tight["fb"] >= mlp["fb"] and tight["mlp"] <= mlp["mlp"]
+
+
+def test_exact_pairs_match_oracle_closed_form(gpu_lib):
+    """The default training pairs: T_new from the exact integrator's closed
+    form (FP64 on the GPU) against the oracle's restatement, to 1e-12 (the
+    two math libraries' pow and log differ in the last bits)."""
+    cfg, _ = problems.wind_bubble(16)
+    box = (-4.0, 4.0, 4.0, 8.5, -8.0, 1.0)
+    with tlq.Context(cfg) as ctx:
+        X, Y, R = ctx.cooling_pairs(256, 5, box)
+    assert np.all(np.isfinite(Y))
+    ocfg = tlq.Config(**{**cfg.__dict__, "nx": 2, "ny": 2, "nz": 2, "winds": [], "masses": None,
+                         "cooling": tlq.COOL_EXACT})
+    o = Oracle(oracle_params(ocfg))
+    Tmin = cfg.cool_T[0]
+    checked = 0
+    for q in range(0, 256, 4):
+        nd, T, Tn_gpu, dt = R[q]
+        eth = nd * problems.KB * T / (cfg.gamma - 1.0)
+        tau = o.cool_coef(T) * nd * nd / eth * dt  # the pair's cooling number, in FP64
+        want = max(o.cool_exact_T(T, tau), Tmin)
+        assert abs(Tn_gpu - want) <= 1e-9 * want, (q, Tn_gpu, want)
+        checked += 1
+    assert checked == 64

@@ -260,15 +260,20 @@ __device__ __forceinline__ double uniform01(uint64_t seed, uint64_t i, int strea
 // step's cooling number Lambda(T) n^2 dt / E_th) stratified in i so that the
 // 32 samples of a warp need similar numbers of sub-steps; dt follows from
 // tau.  The pair is (features, r) with r = (y - 1)/tau, y = ln(T/T_new)/tau,
-// T_new from the finely sub-cycled FP64 integrator (cool_cell with the
-// params' sub-step settings).  ln(T/T_new) = tau + tau^2 r is exact to first
+// T_new from the exact integrator's closed form (params' cooling
+// COOL_EXACT, FP64) or from the finely sub-cycled FP64 integrator (cool_cell
+// with the params' sub-step settings).  ln(T/T_new) = tau + tau^2 r is exact to first
 // order whatever r is (y -> 1 as tau -> 0; r -> -(s-1)/2, s the local slope
 // of the table), and r is O(1) everywhere; below tau ~ 1e-5 r is lost to
 // FP64 round-off (ln(T/T_new) - tau ~ 1e-16 against tau^2), so those pairs
 // are weighted (tau/1e-5)^2 -- their tau^2 r is negligible in the step.
 // The sub-cycled exponential step is first order in its sub-step, so it is
 // run with sub-steps of frac and frac/2 and extrapolated (Richardson):
-// ln T_new = 2 ln T_(frac/2) - ln T_(frac), second order.  A pair whose
+// ln T_new = 2 ln T_(frac/2) - ln T_(frac), second order -- which still
+// leaves it ~1e-5 of T above the exact solution on average (up to 3e-4)
+// where cooling runs away (tau ~ 0.1-1: the cooling coefficient grows by
+// decades within the step), a one-sided error a network trained on it
+// inherits; hence the closed form by default.  A pair whose
 // cooling reaches the table's first temperature within the step (cooling
 // stops there, cooling.f90:71) is "completed": its target is the y that
 // lands exactly on that temperature, with weight 0 (the step hands such
@@ -293,19 +298,26 @@ __global__ void k_cool_pairs(Params p, long long N, uint64_t seed, double lnlo, 
   const double lam = cool_coef(p.cool, T);
   const double ce = lam * (n * n) / eth;
   const double dt = tau / ce;
-  const double p0 = w[4];
-  double u4 = eth;
-  cool_cell(p, w, u4, dt);
-  const double T1 = w[4] * p.mu0 * AMU / (w[0] * KB);
-  Params ph = p;
-  ph.cool_sub_frac = 0.5 * p.cool_sub_frac;
-  w[4] = p0;
-  u4 = eth;
-  cool_cell(ph, w, u4, dt);
-  const double T2 = w[4] * p.mu0 * AMU / (w[0] * KB);
-  double Tn = exp(2.0 * log(T2) - log(T1));
   const double Tmin = p.cool.T[0];
-  const bool completed = T2 < Tmin || Tn < Tmin;
+  double Tn;
+  bool completed;
+  if (p.cooling == COOL_EXACT) {
+    Tn = cool_exact_T(p.cool, T, lam, tau);
+    completed = !(Tn > Tmin);
+  } else {
+    const double p0 = w[4];
+    double u4 = eth;
+    cool_cell(p, w, u4, dt);
+    const double T1 = w[4] * p.mu0 * AMU / (w[0] * KB);
+    Params ph = p;
+    ph.cool_sub_frac = 0.5 * p.cool_sub_frac;
+    w[4] = p0;
+    u4 = eth;
+    cool_cell(ph, w, u4, dt);
+    const double T2 = w[4] * p.mu0 * AMU / (w[0] * KB);
+    Tn = exp(2.0 * log(T2) - log(T1));
+    completed = T2 < Tmin || Tn < Tmin;
+  }
   if (completed) Tn = Tmin;
   X[3 * i + 0] = (float)ln;
   X[3 * i + 1] = (float)lt;

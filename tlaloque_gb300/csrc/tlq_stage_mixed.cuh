@@ -527,11 +527,8 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
   for (int k = k0 - 1; k <= k1 && !aborted; ++k) {
     const bool first = k < k0;
     const long long c = L.at(i, j, k);
-    double uc[5];
     double ph[6];
     if (cell_ok && !first) {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
       if (p.gravity) {
         ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
         ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
@@ -556,10 +553,6 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
     for (int e = 0; e < 5; ++e) wc[e] = s.prm[k & 1].v[e][ly][lx];
     float dU[5];
     flux_divergence<1>(p, s, k, tx, ty, dtf, dtdx, dtdy, dtdz, wc, ph, dU);
-    // FP64 accumulation: UPP = U - dU (Godunov's centre value is U)
-    double up[5];
-#pragma unroll
-    for (int e = 0; e < 5; ++e) up[e] = uc[e] - f2d(dU[e]);
     // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U this
     // stage streams (= the old U of stage 2), in FP32 from the ring
     {
@@ -575,12 +568,41 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
         a.lapf[e * L.plane + c] = etaf * lap;
       }
     }
-    if (near_boundary_or_wind(p, i, j, k)) {
-      write_ghost_prims(p, L, a.uppf, gm1, i, j, k, up);  // borders(UPP, 2)
-      winds_cell(p, i, j, k, up);
+    // UPP = U - dU (Godunov's centre value is U).  UPP is kept in FP32, so
+    // it is formed in FP32 from the FP32 state of the ring, and its
+    // primitives as mixed_cell forms them, except where FP64 is needed: the
+    // pressure of a cell whose kinetic energy exceeds 0.99 of its total
+    // energy (FP32 would lose it to cancellation), and the cells whose UPP
+    // the boundaries or the winds also need (ghost images, wind overwrite),
+    // which take UPP = U - dU in FP64 from the state in HBM.
+    float w[5];
+    bool fp64 = near_boundary_or_wind(p, i, j, k);
+    if (!fp64) {
+      const float* A1 = cu(k);
+      const int o = ly * G::PX + lx;
+      float uf[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) uf[e] = __fsub_rn(A1[e * G::PB + o], dU[e]);
+      const float inv = 1.0f / uf[0];
+      w[0] = uf[0];
+      w[1] = uf[1] * inv;
+      w[2] = uf[2] * inv;
+      w[3] = uf[3] * inv;
+      const float ek = __fmul_rn(0.5f, __fmaf_rn(uf[3], w[3], __fmaf_rn(uf[2], w[2], __fmul_rn(uf[1], w[1]))));
+      fp64 = ek > __fmul_rn(0.99f, uf[4]);
+      w[4] = fmaxf(__fmul_rn(gm1, __fsub_rn(uf[4], ek)), 1e-20f);
     }
-    float cf[5], w[5];
-    mixed_cell(gm1, up, 1, cf, w);  // UPP's primitives, as stage 2 reads them
+    if (fp64) {
+      double up[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) up[e] = a.uold[e * L.plane + c] - f2d(dU[e]);
+      if (near_boundary_or_wind(p, i, j, k)) {
+        write_ghost_prims(p, L, a.uppf, gm1, i, j, k, up);  // borders(UPP, 2)
+        winds_cell(p, i, j, k, up);
+      }
+      float cf[5];
+      mixed_cell(gm1, up, 1, cf, w);
+    }
 #pragma unroll
     for (int e = 0; e < 5; ++e) a.uppf[e * L.plane + c] = w[e];
   }

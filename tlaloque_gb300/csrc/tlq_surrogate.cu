@@ -443,11 +443,12 @@ int sfail(tlq_ctx* c, int code, const std::string& m) {
     if (e_ != cudaSuccess) return sfail(ctx, TLQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-// Parameters of the exact integrator (the context's physics and table,
-// sub-cycled with the given sub-steps).
+// Parameters of the training pairs' integrator (the context's physics and
+// table): the exact integrator's closed form when sub_frac is 0, else the
+// sub-cycled integrator with the given sub-steps (extrapolated).
 Params exact_params(const tlq_ctx* ctx, double sub_frac, int max_sub) {
   Params p = ctx->P;
-  p.cooling = COOL_SUBCYCLE;
+  p.cooling = sub_frac > 0.0 ? COOL_SUBCYCLE : COOL_EXACT;
   p.cool_sub_frac = sub_frac;
   p.cool_max_sub = max_sub;
   return p;
@@ -484,13 +485,13 @@ void tlq_surrogate_opts_default(tlq_surrogate_opts* o) {
   o->seed = 12345ULL;
   const double box[6] = {-4.0, 4.0, 4.0, 8.5, -8.0, 1.0};
   for (int q = 0; q < 6; ++q) o->box[q] = box[q];
-  o->sub_frac = 2e-3;
+  o->sub_frac = 0.0;  // the exact integrator's closed form
   o->max_sub = 20000;
 }
 
 int tlq_cooling_pairs(tlq_ctx* ctx, long long n, unsigned long long seed, const double* box6, double sub_frac,
                       int max_sub, float* X, float* Y, double* raw) {
-  if (!ctx || n <= 0 || !box6 || !X || !Y || !(sub_frac > 0.0) || max_sub < 1) return TLQ_ERR_ARG;
+  if (!ctx || n <= 0 || !box6 || !X || !Y || !(sub_frac >= 0.0) || max_sub < 1) return TLQ_ERR_ARG;
   if (!ctx->dT) return sfail(ctx, TLQ_ERR_STATE, "cooling table not set");
   float *dX = nullptr, *dY = nullptr;
   double* dR = nullptr;

@@ -523,9 +523,11 @@ class Context:
         assert P.size == MLP_NPARAM and nm.size == 6 and bx.size == 6
         self._check(self.L.tlq_set_cooling_surrogate(self.h, _fp(P), _fp(nm), _dp(bx)), "set_cooling_surrogate")
 
-    def cooling_pairs(self, n: int, seed: int, box, sub_frac: float = 2e-3, max_sub: int = 20000):
+    def cooling_pairs(self, n: int, seed: int, box, sub_frac: float = 0.0, max_sub: int = 20000):
         """(X raw features [n,3], Y targets [n], raw (n, T, T_new, dt) [n,4])
-        from the exact integrator on the GPU."""
+        on the GPU: from the exact integrator's closed form (sub_frac 0) or
+        from the sub-cycled integrator with sub-steps of sub_frac and
+        sub_frac/2, extrapolated."""
         X = np.zeros((n, 3), dtype=np.float32)
         Y = np.zeros(n, dtype=np.float32)
         R = np.zeros((n, 4), dtype=np.float64)
