@@ -146,6 +146,7 @@ void fill_params(tlq_ctx* c) {
   p.f_cool_sub_frac = (float)p.cool_sub_frac;
   p.f_mlp_tol = (float)g.cool_mlp_tol;
   p.f_cooling_limit = (float)p.cooling_limit;
+  p.c_edge_p = (p.gamma - 1.0) * p.mu0 * AMU;  // c_edge_rho = T_0 KB: set with the cooling table
 }
 
 }  // namespace
@@ -555,6 +556,7 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int
   ctx->P.cool = CoolTable{ctx->dT,     ctx->dlogT, ctx->dC,      n,          ctx->dTf, ctx->dlogTf,
                           ctx->dCf,    ctx->dslope, ctx->dgcum, ctx->dslopef, ctx->dgcumf};
   ctx->cool_tmin = T[0];
+  ctx->P.c_edge_rho = T[0] * KB;
   if (!ctx->cool_counts) {
     CK(cudaMalloc(&ctx->cool_counts, 3 * sizeof(unsigned long long)));
     CK(cudaMemset(ctx->cool_counts, 0, 3 * sizeof(unsigned long long)));

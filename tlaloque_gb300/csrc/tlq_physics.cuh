@@ -90,6 +90,9 @@ struct Params {
   float f_inv_muamu;                   // 1/(mu0 AMU): n = rho f_inv_muamu
   float f_cool_sub_frac, f_cooling_limit;
   float f_mlp_tol;  // the surrogate's residual tolerance
+  // the cooling switch near the table's first temperature T_0, decided in
+  // FP64 without divisions: (gamma-1) mu0 AMU and T_0 KB (tlq_stage_mixed.cuh)
+  double c_edge_p, c_edge_rho;
 };
 
 // ---------------------------------------------------------------------------

@@ -116,13 +116,16 @@ __device__ __forceinline__ void mixed_cell(float gm1, const double* u, long long
   w[3] = cf[3] * inv;
   const float ek =
       __fmul_rn(0.5f, __fmaf_rn(cf[3], w[3], __fmaf_rn(cf[2], w[2], __fmul_rn(cf[1], w[1]))));
-  float p;
-  if (ek > __fmul_rn(0.99f, cf[4])) {
-    const double r = u[0], m1 = u[vs], m2 = u[2 * vs], m3 = u[3 * vs], E = u[4 * vs];
-    const double k2 = __fma_rn(m3, m3, __fma_rn(m2, m2, __dmul_rn(m1, m1)));
-    p = d2f(__dmul_rn((double)gm1, __dsub_rn(E, __ddiv_rn(__dmul_rn(0.5, k2), r))));
-  } else {
-    p = __fmul_rn(gm1, __fsub_rn(cf[4], ek));
+  const bool kin = ek > __fmul_rn(0.99f, cf[4]);
+  float p = __fmul_rn(gm1, __fsub_rn(cf[4], ek));
+  // a branch the whole warp skips unless one of its cells needs FP64 (the
+  // FP64 division would otherwise be evaluated for every cell)
+  if (__any_sync(__activemask(), kin)) {
+    if (kin) {
+      const double r = u[0], m1 = u[vs], m2 = u[2 * vs], m3 = u[3 * vs], E = u[4 * vs];
+      const double k2 = __fma_rn(m3, m3, __fma_rn(m2, m2, __dmul_rn(m1, m1)));
+      p = d2f(__dmul_rn((double)gm1, __dsub_rn(E, __ddiv_rn(__dmul_rn(0.5, k2), r))));
+    }
   }
   w[4] = fmaxf(p, 1e-20f);
 }
@@ -157,20 +160,28 @@ __device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
   return cool_coef_seg(t, temp, lo);
 }
 
-// Whether cooling applies (temp >= the table's first temperature,
+// Whether cooling applies (temp >= the table's first temperature T_0,
 // cooling.f90:71).  The switch is a jump in the source term; a cell whose
 // FP32 temperature falls within 1e-6 of the edge (e.g. a medium initialised
-// at exactly the table's lower edge) decides it from the FP64 state with the
-// plain step's arithmetic (uncontracted intrinsics), so both forms agree.
+// at the table's lower edge) decides it from the FP64 state, to FP64
+// accuracy, so both forms agree: with temp = p mu0 AMU / (rho KB) and
+// p = (gamma-1) (E - k2/(2 rho)), temp >= T_0 is
+// (gamma-1) mu0 AMU (E rho - k2/2) >= T_0 KB rho^2 for rho > 0 -- no FP64
+// division (each costs ~8 FMA slots of GB300's FP64 pipe), and the warp
+// takes the branch only when one of its cells is that close to the edge.
 __device__ __forceinline__ bool cools_at(const Params& p, float temp, const double* u) {
   const float Tmin = p.cool.Tf[0];
-  if (fabsf(__fsub_rn(temp, Tmin)) > 1e-6f * Tmin) return temp >= Tmin;
-  const double r = u[0];
-  const double k2 = __dadd_rn(__dadd_rn(__dmul_rn(u[1], u[1]), __dmul_rn(u[2], u[2])), __dmul_rn(u[3], u[3]));
-  double pr = __dmul_rn(__dsub_rn(p.gamma, 1.0), __dsub_rn(u[4], __ddiv_rn(__dmul_rn(0.5, k2), r)));
-  pr = pr > 1e-20 ? pr : 1e-20;
-  const double T = __ddiv_rn(__dmul_rn(__dmul_rn(pr, p.mu0), AMU), __dmul_rn(r, KB));
-  return T >= p.cool.T[0];
+  const bool near = !(fabsf(__fsub_rn(temp, Tmin)) > 1e-6f * Tmin);
+  bool yes = temp >= Tmin;
+  if (__any_sync(__activemask(), near)) {
+    if (near) {
+      const double r = u[0];
+      const double k2 = __fma_rn(u[3], u[3], __fma_rn(u[2], u[2], __dmul_rn(u[1], u[1])));
+      const double lhs = __dmul_rn(p.c_edge_p, __fma_rn(u[4], r, __dmul_rn(-0.5, k2)));
+      yes = lhs >= __dmul_rn(p.c_edge_rho, __dmul_rn(r, r));
+    }
+  }
+  return yes;
 }
 
 // The exact integrator (COOL_EXACT) in FP32: the same closed form as
@@ -208,15 +219,13 @@ __device__ __forceinline__ float cool_exact_dropf(const CoolTable& t, float temp
   return fmaxf(expm1f(__fadd_rn(lj, r)), __fsub_rn(t.Tf[0] / temp, 1.0f));
 }
 
-__device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv_muamu, float gm1, float* w,
-                                            double& u4, float dt, const double* u) {
+// The cooling of a cell that cools (cools_at), at temperature temp with
+// table coefficient aloss (found at table entry seg): w[4] and u4 updated.
+__device__ __forceinline__ void cool_cell_known(const Params& p, float cT, float inv_muamu, float gm1, float* w,
+                                                double& u4, float dt, float temp, float aloss, int seg) {
   const CoolTable& t = p.cool;
-  float temp = (w[4] / w[0]) * cT;
-  if (!cools_at(p, temp, u)) return;
   const float p0 = w[4];
   float ETH = w[4] / gm1;
-  int seg = 0;  // the table entry of the last coefficient
-  float aloss = cool_coef_seg(t, temp, seg);
   const float n = w[0] * inv_muamu;
   float ce = (aloss * n) * (n / ETH);
   int nsub = 1;
@@ -253,6 +262,15 @@ __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv
     if (floored) break;
   }
   u4 = u4 + f2d(__fsub_rn(w[4], p0) / gm1);
+}
+
+__device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv_muamu, float gm1, float* w,
+                                            double& u4, float dt, const double* u) {
+  const float temp = (w[4] / w[0]) * cT;
+  if (!cools_at(p, temp, u)) return;
+  int seg = 0;  // the table entry of the coefficient
+  const float aloss = cool_coef_seg(p.cool, temp, seg);
+  cool_cell_known(p, cT, inv_muamu, gm1, w, u4, dt, temp, aloss, seg);
 }
 
 // The face-ghost images of a stage-1 cell (borders(UPP, 2), boundaries.f90
@@ -592,7 +610,7 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
       fp64 = ek > __fmul_rn(0.99f, uf[4]);
       w[4] = fmaxf(__fmul_rn(gm1, __fsub_rn(uf[4], ek)), 1e-20f);
     }
-    if (fp64) {
+    if (__any_sync(__activemask(), fp64) && fp64) {
       double up[5];
 #pragma unroll
       for (int e = 0; e < 5; ++e) up[e] = a.uold[e * L.plane + c] - f2d(dU[e]);
@@ -708,11 +726,6 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
       for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
 #pragma unroll
       for (int e = 0; e < 5; ++e) lv[e] = a.lapf[e * L.plane + c];
-      if (p.gravity) {
-        ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
-        ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
-        ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
-      }
     }
     if (!first) pw.wait(s.bar, 4, k + 2, &s.abort);
     conserved(k + 1);
@@ -724,6 +737,14 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
     if (first) continue;
 
     if (cell_ok) {
+      // the potential's neighbours (L1/L2 hits: the block's planes) are
+      // loaded here, not before the faces, where 12 more live registers
+      // made the kernel spill
+      if (p.gravity) {
+        ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
+        ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
+        ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
+      }
       float wc[5];
 #pragma unroll
       for (int e = 0; e < 5; ++e) wc[e] = s.prm[k & 3].v[e][ty + 2][tx + 2];
@@ -760,12 +781,13 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
         if (cools_at(p, T, un)) {
           const float nd = w[0] * inv_muamu;
           const float eth = w[4] / gm1;
-          const float lam = cool_coef_f(p.cool, T);
+          int seg = 0;
+          const float lam = cool_coef_seg(p.cool, T, seg);
           const float tau = (lam * nd) * (nd / eth) * dtf;
           if (tau > p.f_cool_sub_frac) {
             queued = true;
           } else {
-            cool_cell_f(p, cT, inv_muamu, gm1, w, un[4], dtf, un);
+            cool_cell_known(p, cT, inv_muamu, gm1, w, un[4], dtf, T, lam, seg);
             ++nsingle;
           }
         }

@@ -143,9 +143,12 @@ def wind_bubble(n: int = 256, cooling: int = COOL_SUBCYCLE, T_wind: float = 1.0e
     rho = n_amb * mu * AMU
     # T = 1e4 K is the cooling table's first entry: cooling.f90:71 cools a
     # cell when temp >= cool_Tmin, so a medium at exactly 1e4 K is decided by
-    # the last bit of its pressure.  1e-9 above the edge gives the
-    # exact-arithmetic decision (cooled) robustly in every precision.
-    p = n_amb * KB * 1.0e4 * (1.0 + 1e-9)
+    # the last bit of its pressure.  1e-5 above the edge gives the
+    # exact-arithmetic decision (cooled) robustly in every precision, FP32
+    # included (its temperature carries ~1e-7 of rounding); the first step's
+    # cooling then takes the medium ~4e-4 below the edge, where FP32 decides
+    # too.
+    p = n_amb * KB * 1.0e4 * (1.0 + 1e-5)
     return cfg, conserved(cfg, rho, 0.0, 0.0, 0.0, p)
 
 
