@@ -9,6 +9,7 @@
 // gradient, the layer-1 and layer-4 weight gradients are FP32.
 #include "tlq_internal.h"
 #include "tlq_mlp.cuh"
+#include "tlq_umma.cuh"
 
 namespace tlq {
 namespace mlp {
@@ -243,6 +244,32 @@ __global__ void __launch_bounds__(TT) k_mlp_infer(const float* __restrict__ P, c
   }
 }
 
+// Batch inference on the tcgen05 path of the step's network pass
+// (tlq_umma.cuh): 128 samples per tile, one per thread.  A tile whose MMA
+// wait ran out writes NaN (the caller sees it), and the block stops.
+__global__ void __launch_bounds__(umma::ROWS) k_mlp_infer_umma(const float* __restrict__ P,
+                                                               const float* __restrict__ X, int n,
+                                                               float* __restrict__ Yout) {
+  __shared__ umma::Smem S;
+  const int ntiles = (n + umma::ROWS - 1) / umma::ROWS;
+  if ((int)blockIdx.x >= ntiles) return;
+  umma::load_weights_fp32(P, S);
+  umma::setup(S);
+  uint32_t phase = 0;
+  bool tc = true;
+  for (int tile = blockIdx.x; tile < ntiles && tc; tile += gridDim.x) {
+    const int r = tile * umma::ROWS + (int)threadIdx.x;
+    float x[3] = {0.f, 0.f, 0.f};
+    if (r < n)
+      for (int f = 0; f < 3; ++f) x[f] = X[3 * r + f];
+    float y = 0.f;
+    tc = umma::forward(S, x, y, phase);
+    if (r < n) Yout[r] = tc ? y : NAN;
+  }
+  if (!tc) umma::drain(S, phase);
+  umma::teardown(S);
+}
+
 // ---------------------------------------------------------------------------
 // Training pairs from the exact integrator.
 // ---------------------------------------------------------------------------
@@ -412,6 +439,15 @@ cudaError_t launch_pack_weights(const float* P, void* img, cudaStream_t s) {
 }
 
 cudaError_t launch_mlp_infer(const float* P, const float* X, int n, float* Y, cudaStream_t s) {
+  // the step's forward pass (tcgen05, TMEM accumulators)
+  const int tiles = (n + umma::ROWS - 1) / umma::ROWS;
+  const int blocks = std::max(1, std::min(tiles, 152 * 3));
+  mlp::k_mlp_infer_umma<<<blocks, umma::ROWS, 0, s>>>(P, X, n, Y);
+  return cudaGetLastError();
+}
+
+// The mma.sync forward pass (the training kernels' own), for comparison.
+cudaError_t launch_mlp_infer_sync(const float* P, const float* X, int n, float* Y, cudaStream_t s) {
   const int tiles = (n + mlp::TS - 1) / mlp::TS;
   const int blocks = std::max(1, std::min((tiles + mlp::TW - 1) / mlp::TW, 152 * 8));
   mlp::k_mlp_infer<<<blocks, mlp::TT, 0, s>>>(P, X, n, Y);

@@ -22,6 +22,7 @@
 #include "tlq_ctx.h"
 #include "tlq_mlp.cuh"
 #include "tlq_stage_mixed.cuh"
+#include "tlq_umma.cuh"
 
 namespace tlq {
 namespace {
@@ -235,7 +236,7 @@ __device__ void cool_sort_mesh(const CoolJob& j, double* red, unsigned nblocks, 
   cfl_contribute<CT>(f2d(m0), f2d(m1), f2d(m2), j.clk, red);
 }
 
-__device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red, unsigned nblocks, unsigned bid) {
+__device__ void cool_net_mesh(const CoolJob& j, umma::Smem& S, double* red, unsigned nblocks, unsigned bid) {
   const Params& p = j.p;
   const Layout& L = j.L;
   const Clock* clk = j.clk;
@@ -244,15 +245,16 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
   const long long n = (long long)*j.nqcount;
   if ((long long)bid * CT >= n) return;  // no network cell for this block: no weights, nothing to fold
   double* __restrict__ U = step_output(j.U0, j.U1, clk, j.it_base);
-  mlp::copy_weights<CT>(sa.img, W);
-  __syncthreads();
+  umma::load_weights(sa.img, S);
+  umma::setup(S);
   const CoolTable& tab = p.cool;
   const float gm1 = p.f_gamma - 1.0f, gf = p.f_gamma;
   const float dtf = d2f(clk->dt);
-  const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   float m0 = 0.f, m1 = 0.f, m2 = 0.f;
   unsigned long long used = 0, fell = 0;
-  // warp-uniform trip count: the network's tiles need all 32 lanes
+  uint32_t phase = 0;
+  bool tc = true;  // the tensor-core path is healthy (block-wide)
+  // block-uniform trip count: one 128-row MMA tile per iteration
   for (long long base = (long long)bid * CT; base < n; base += (long long)nblocks * CT) {
     const long long q = base + threadIdx.x;
     const bool valid = q < n;
@@ -268,38 +270,21 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
     CellCool c;
     cell_cool(p, sa, u, dtf, c);
     float y = 0.f;
-    if (__ballot_sync(0xffffffffu, valid)) {
-      // the warp's 32 cells as two m16 tiles (rows = lanes 0-15, 16-31)
-      float yt[2][2];
-#pragma unroll 1
-      for (int tsel = 0; tsel < 2; ++tsel) {
-        float xg[3], xg8[3];
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          xg[f] = __shfl_sync(0xffffffffu, c.feat[f], 16 * tsel + g);
-          xg8[f] = __shfl_sync(0xffffffffu, c.feat[f], 16 * tsel + g + 8);
-        }
-        mlp::forward_tile(W, xg, xg8, g, tig, yt[tsel]);
-      }
-      const int row = lane & 15, src = 4 * (row & 7);
-      const float a0 = __shfl_sync(0xffffffffu, yt[0][0], src), a1 = __shfl_sync(0xffffffffu, yt[0][1], src);
-      const float b0 = __shfl_sync(0xffffffffu, yt[1][0], src), b1 = __shfl_sync(0xffffffffu, yt[1][1], src);
-      y = (lane < 16) ? (row < 8 ? a0 : a1) : (row < 8 ? b0 : b1);
-    }
+    if (tc) tc = umma::forward(S, c.feat, y, phase);
     bool ok = false;
     if (valid) {
       const float T = c.T, tau = c.tau;
       // the exact integrator's change and the network's, T_new/T - 1 (the
       // network's r: ln(T_new/T) = -(tau + tau^2 r); clamped at the table's
-      // first temperature, where cooling stops)
-      // A cell whose cooling reaches the table's first temperature within
-      // the step (the exact change is the floor's, T_0/T - 1) takes the exact
-      // integrator: training leaves those pairs out, and the network's
-      // prediction, clamped at the floor, could only err on one side.
+      // first temperature, where cooling stops).  A cell whose cooling
+      // reaches that temperature within the step (the exact change is the
+      // floor's, T_0/T - 1) takes the exact integrator: training leaves those
+      // pairs out, and the network's prediction, clamped at the floor, could
+      // only err on one side.
       const float qfloor = __fsub_rn(tab.Tf[0] / T, 1.0f);
       const float qx = cool_exact_dropf(tab, T, c.lam, tau);
       const float qf = fmaxf(expm1f(-(1.0f + tau * y) * tau), qfloor);
-      ok = qx > qfloor && fabsf(qf - qx) <= p.f_mlp_tol;
+      ok = tc && qx > qfloor && fabsf(qf - qx) <= p.f_mlp_tol;
       if (ok) {
         const float dp = __fmul_rn(c.w[4], qf);
         c.w[4] = __fadd_rn(c.w[4], dp);
@@ -313,6 +298,13 @@ __device__ void cool_net_mesh(const CoolJob& j, mlp::SmemWeights& W, double* red
     used += ok ? 1 : 0;
     fell += (valid && !ok) ? 1 : 0;
   }
+  if (!tc) {
+    // an MMA wait ran out: the cells above took the exact integrator; the
+    // step reports the timeout
+    if (threadIdx.x == 0) atomicOr(&const_cast<Clock*>(clk)->status, ST_TIMEOUT);
+    umma::drain(S, phase);
+  }
+  umma::teardown(S);
   add_counts(sa, used, fell, 0);
   cfl_contribute<CT>(f2d(m0), f2d(m1), f2d(m2), j.clk, red);
 }
@@ -331,11 +323,11 @@ __global__ void __launch_bounds__(CT) k_cool_sort(const __grid_constant__ CoolJo
 
 __global__ void __launch_bounds__(CT, 3) k_cool_net(const __grid_constant__ CoolJob one,
                                                  const CoolJob* __restrict__ jobs, int njobs) {
-  __shared__ mlp::SmemWeights W;
+  __shared__ umma::Smem S;
   __shared__ double red[96];
   __shared__ SmemJob sj;
   const CoolJob& j = stage_job(sj, job_of_block(one, jobs, njobs, blockIdx.x));
-  cool_net_mesh(j, W, red, j.nblk, blockIdx.x - j.blk0);
+  cool_net_mesh(j, S, red, j.nblk, blockIdx.x - j.blk0);
 }
 
 __device__ void cool_dt_mesh(const CoolJob& j, double* red, int* flag, unsigned nblocks) {
