@@ -1,7 +1,7 @@
 """Benchmark of tlaloque's hydrodynamic step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tlq|reference]
-                    [--workload wind256|wind128|sedov128|sod|clumpy384|cloud128|cloud256|ensemble48]
+                    [--workload wind256|wind128|sedov128|sod|clumpy<N>|cloud128|cloud256|ensemble48]
 
 A "step" is one full iteration of the reference's main loop
 (source/mainHD.f90:74-99: CFL dt, two HLLC stages, ghost fill, winds, point
@@ -97,9 +97,10 @@ def make_workload(name: str):
     elif name == "sedov128":
         cfg, U0 = problems.sedov(128)
         desc = "3-D Sedov-Taylor blast 128^3, HLLC + van Leer, outflow"
-    elif name == "clumpy384":
-        cfg, U0 = problems.clumpy(384)
-        desc = ("clumpy radiative medium 384^3, periodic (8 pc)^3, lognormal density (k^-5/3), log T uniform "
+    elif name.startswith("clumpy") and name[6:].isdigit():
+        n = int(name[6:])
+        cfg, U0 = problems.clumpy(n)
+        desc = (f"clumpy radiative medium {n}^3, periodic (8 pc)^3, lognormal density (k^-5/3), log T uniform "
                 "1e3-1e8 K, rms Mach 2, HLLC + van Leer, sub-cycled tabulated cooling")
     elif name == "sod":
         cfg, U0 = problems.sod_tube()
@@ -386,6 +387,7 @@ def main():
     ap.add_argument("--clumpy-n", type=int, default=256, help="mesh of the surrogate-active record")
     ap.add_argument("--sur-steps", type=int, default=100, help="timed steps of the surrogate-active record")
     ap.add_argument("--no-surrogate-active", action="store_true")
+    ap.add_argument("--sur-tol", type=float, default=1e-5, help="residual tolerance of the surrogate-active record")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -487,7 +489,8 @@ def main():
         judge["ctx"].close()
         closed = measure(tlq.PREC_MIXED, nst, False, base=(ccfg, cU0), cooling=tlq.COOL_EXACT, **sub)
         closed["ctx"].close()
-        act = measure(tlq.PREC_MIXED, nst, False, net=net, base=(ccfg, cU0), cooling=tlq.COOL_MLP, **sub)
+        act = measure(tlq.PREC_MIXED, nst, False, net=net, base=(ccfg, cU0), cooling=tlq.COOL_MLP,
+                      cool_mlp_tol=args.sur_tol, **sub)
         act["ctx"].close()
 
         def acc(a):
@@ -500,6 +503,10 @@ def main():
                             "(sigma log10 n = 1, k^-5/3), log T uniform 1e3-1e8 K, rms Mach 2, the wind bubble's "
                             "cooling curve; HLLC + van Leer",
                 "mesh": [ccfg.nx, ccfg.ny, ccfg.nz], "warmup": args.warmup, "steps": nst,
+                "cool_mlp_tol": args.sur_tol,
+                "tol_note": "the residual tolerance of an accepted prediction, |T_pred - T_exact| / T; the north "
+                            "star's 1e-3 bounds each cell, but on this stiff medium the accepted cells' small "
+                            "shared bias sums to ~1e-6 per 100 steps there, so the record runs at a tighter one",
                 "value": act["value"], "unit": UNIT, "ms_per_step": act["ms"] / nst, "ms_stage1": act["k1"],
                 "ms_stage2": act["k2"], "ms_cool_passes": act["kc"],
                 "timed_cell_steps_network": nm, "timed_cell_steps_exact": nf, "timed_cell_steps_single_step": ns,
