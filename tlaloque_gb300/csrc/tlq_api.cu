@@ -212,6 +212,7 @@ int enqueue_step(tlq_ctx* ctx, int par, bool timed) {
   a.clk = ctx->clk;
   a.zlen = ctx->zlen;
   a.phi = ctx->cfg.self_gravity ? ctx->phit : ctx->phi;
+  a.phif = ctx->phif;
   a.lapf = ctx->lapf;
   // the mixed form keeps UPP as FP32 primitives in the same allocation
   a.uppf = reinterpret_cast<float*>(ctx->UPP);
@@ -416,8 +417,11 @@ int tlq_create(const tlq_config* cfg, tlq_ctx** out) {
     ctx->P.gravity = 1;
   }
   if (cfg->precision == TLQ_PREC_MIXED) {
-    if (cudaMalloc(&ctx->lapf, (size_t)L.plane * 5 * sizeof(float))) return bail(TLQ_ERR_NOMEM);
+    if (cudaMalloc(&ctx->lapf, (size_t)L.plane * 5 * sizeof(float)) ||
+        cudaMalloc(&ctx->phif, (size_t)L.plane * sizeof(float)))
+      return bail(TLQ_ERR_NOMEM);
     cudaMemset(ctx->lapf, 0, (size_t)L.plane * 5 * sizeof(float));
+    cudaMemset(ctx->phif, 0, (size_t)L.plane * sizeof(float));
   }
   if (cfg->cooling == TLQ_COOL_MLP) {
     const size_t ncell = (size_t)cfg->nx * cfg->ny * cfg->nz;
@@ -463,6 +467,7 @@ int tlq_destroy(tlq_ctx* ctx) {
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   cudaFree(ctx->U[0]); cudaFree(ctx->U[1]); cudaFree(ctx->UPP); cudaFree(ctx->Pc); cudaFree(ctx->phi);
   cudaFree(ctx->lapf);
+  cudaFree(ctx->phif);
   mg_free(ctx);
   cudaFree(ctx->mlp_params); cudaFree(ctx->mlp_image); cudaFree(ctx->cool_counts);
   cudaFree(ctx->mlp_cqueue); cudaFree(ctx->mlp_nqueue); cudaFree(ctx->mlp_qcount);
@@ -620,6 +625,9 @@ int tlq_set_point_masses(tlq_ctx* ctx, const double* xyzm, int n) {
     ctx->P.gravity = 1;
     CK(launch_point_potential_soa(ctx->P, ctx->L, ctx->dmasses, n, ctx->phi, ctx->stream));
   }
+  // the mixed stages read the potential in FP32 (self-gravity rewrites it
+  // with each solve)
+  if (ctx->phif) CK(launch_to_f32(ctx->phi, ctx->phif, ctx->L.plane, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   invalidate_graphs(ctx);
   return TLQ_OK;

@@ -166,6 +166,7 @@ void fill_desc(tlq_batch* b, int i) {
       a.clk = c->clk;
       a.zlen = b->zlen[i];
       a.phi = c->phi;
+      a.phif = c->phif;
       a.lapf = c->lapf;
       a.uold = c->U[par];
       a.out = (st == 1) ? c->UPP : c->U[par ^ 1];

@@ -22,6 +22,7 @@ struct tlq_ctx {
   double* UPP = nullptr;
   double* Pc = nullptr;   // carried pressure plane (cooling)
   double* phi = nullptr;  // point-mass potential plane
+  float* phif = nullptr;  // mixed form: the stages' potential (point masses + self-gravity) in FP32
   // self-gravity (tlq_gravity.cu): multigrid levels, control block, moment
   // partials, the self-gravity potential ((nx+2)^3) and the stages' total
   // potential plane PHIP + PHI (SoA plane layout, like phi)

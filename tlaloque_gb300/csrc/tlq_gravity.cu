@@ -42,6 +42,7 @@
 #include <cstring>
 #include <string>
 
+#include "tlq_convert.cuh"
 #include "tlq_ctx.h"
 
 namespace tlq {
@@ -345,7 +346,7 @@ __global__ void k_mg_cycle_end(MgCtl* c, int nparts) {
 // A solve that gave up (a bounded wait or the coarsest solve) marks the
 // step's status as timed out.
 __global__ void k_mg_end(const MgCtl* c, Clock* clk, int n, const double* E0, double* phig, const double* phip,
-                         double* phit, Layout L) {
+                         double* phit, float* phitf, Layout L) {
   if (!c->run) return;
   if (blockIdx.x == 0 && threadIdx.x == 0 && c->status) atomicOr(&clk->status, ST_TIMEOUT);
   const long long cells = (long long)(n + 2) * (n + 2) * (n + 2);
@@ -356,7 +357,9 @@ __global__ void k_mg_end(const MgCtl* c, Clock* clk, int n, const double* E0, do
     phig[q] = v;
     if (phit) {
       const long long o = L.at(i, j, k);
-      phit[o] = phip[o] + v;
+      const double pt = phip[o] + v;
+      phit[o] = pt;
+      if (phitf) phitf[o] = d2f(pt);  // the mixed form's stages read it in FP32
     }
   }
 }
@@ -1290,7 +1293,7 @@ cudaError_t enqueue_mg(tlq_ctx* ctx, Dens rho, const Clock* clk, double* phit, c
     for (int cyc = 0; cyc < MG_CYCLES; ++cyc) cycle(s);
   }
   k_mg_end<<<grid_for(m0 * m0 * m0, 256), 256, 0, s>>>(c, const_cast<Clock*>(clk), n, v.lv[0].E, ctx->phig, ctx->phi,
-                                                       phit, ctx->L);
+                                                       phit, phit ? ctx->phif : nullptr, ctx->L);
   return cudaGetLastError();
 }
 

@@ -58,6 +58,8 @@ cudaError_t launch_prims_soa_to_aos(const Params& p, const Aos& A, const Layout&
 cudaError_t launch_init_prims_dt(const Params& p, const Layout& L, const double* U, double* P, Clock* clk,
                                  int nblocks, cudaStream_t s);
 int init_blocks(const Params& p);
+// dst[q] = FP32 of src[q] (the mixed kernels' rounding), q < n.
+cudaError_t launch_to_f32(const double* src, float* dst, long long n, cudaStream_t s);
 cudaError_t launch_point_potential_soa(const Params& p, const Layout& L, const double* xyzm, int n, double* phi,
                                        cudaStream_t s);
 cudaError_t launch_conserved_sums(const Params& p, const Layout& L, const double* U, double* partials, int nblocks,

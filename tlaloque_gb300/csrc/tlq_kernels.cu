@@ -4,7 +4,10 @@
 //
 // Built with -fmad=false: no multiply-add is contracted, so every result is
 // bit-identical to the reference's FP64 arithmetic (transcendentals aside).
+#include <algorithm>
+
 #include "tlq_internal.h"
+#include "tlq_convert.cuh"
 
 namespace tlq {
 
@@ -279,6 +282,18 @@ __global__ void k_point_potential_ref(Params p, const double* xyzm, int n, doubl
     }
     phi[P.at(i, j, k)] = v;
   }
+}
+
+namespace {
+__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+    dst[q] = d2f(src[q]);
+}
+}  // namespace
+
+cudaError_t launch_to_f32(const double* src, float* dst, long long n, cudaStream_t s) {
+  k_to_f32<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, s>>>(src, dst, n);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_point_potential_soa(const Params& p, const Layout& L, const double* xyzm, int n, double* phi,

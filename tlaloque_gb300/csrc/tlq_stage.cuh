@@ -49,6 +49,7 @@ struct StageArgs {
   double* out;         // STAGE 1: UPP; STAGE 2: U of the next step
   double* pout;        // STAGE 2 with cooling: carried (cooled) interior pressure
   const double* phi;   // point-mass potential plane (null without gravity)
+  const float* phif;   // mixed form: the same potential rounded to FP32 (what its kernels read)
   Clock* clk;          // time, and the CFL reduction's ticket and maxima
   int zlen;            // planes per block
   int use_p;           // STAGE 1 with cooling: interior pressure from the P plane

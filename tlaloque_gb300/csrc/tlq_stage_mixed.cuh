@@ -406,7 +406,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
 // source, -dt S, when gravity is on): dU of Godunov (HLLC.f90:37-40).
 template <int STAGE, class Smem>
 __device__ __forceinline__ void flux_divergence(const Params& p, const Smem& s, int k, int tx, int ty, float dtf,
-                                                float dtdx, float dtdy, float dtdz, const float* wc, const double* ph,
+                                                float dtdx, float dtdy, float dtdz, const float* wc, const float* ph,
                                                 float* dU) {
   const int cur = (k + 1) & 1, prv = k & 1;
 #pragma unroll
@@ -415,9 +415,9 @@ __device__ __forceinline__ void flux_divergence(const Params& p, const Smem& s, 
             dtdz * (s.fz[cur][e][ty][tx] - s.fz[prv][e][ty][tx]);
   if (p.gravity) {
     // S_Solver (sources.f90:885-893) from the cell's primitives wc
-    const float fg1 = (d2f(ph[0]) - d2f(ph[1])) * p.f_hdx;
-    const float fg2 = (d2f(ph[2]) - d2f(ph[3])) * p.f_hdy;
-    const float fg3 = (d2f(ph[4]) - d2f(ph[5])) * p.f_hdz;
+    const float fg1 = (ph[0] - ph[1]) * p.f_hdx;
+    const float fg2 = (ph[2] - ph[3]) * p.f_hdy;
+    const float fg3 = (ph[4] - ph[5]) * p.f_hdz;
     float sv[5];
     sv[0] = 0.0f;
     sv[1] = -wc[0] * fg1;
@@ -545,12 +545,12 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
   for (int k = k0 - 1; k <= k1 && !aborted; ++k) {
     const bool first = k < k0;
     const long long c = L.at(i, j, k);
-    double ph[6];
+    float ph[6];
     if (cell_ok && !first) {
       if (p.gravity) {
-        ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
-        ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
-        ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
+        ph[0] = a.phif[c + 1]; ph[1] = a.phif[c - 1];
+        ph[2] = a.phif[c + L.px]; ph[3] = a.phif[c - L.px];
+        ph[4] = a.phif[c + pxy]; ph[5] = a.phif[c - pxy];
       }
     }
     if (!first) {
@@ -717,7 +717,7 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
     const long long c = L.at(i, j, k);
     double uc[5];
     float lv[5];
-    double ph[6];
+    float ph[6];
     bool queued = false;  // with the surrogate: handed to the cooling passes
     if (!first) pw.wait(s.bar, 4, k + 2, &s.abort);
     conserved(k + 1);
@@ -738,9 +738,9 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
 #pragma unroll
       for (int e = 0; e < 5; ++e) lv[e] = a.lapf[e * L.plane + c];
       if (p.gravity) {
-        ph[0] = a.phi[c + 1]; ph[1] = a.phi[c - 1];
-        ph[2] = a.phi[c + L.px]; ph[3] = a.phi[c - L.px];
-        ph[4] = a.phi[c + pxy]; ph[5] = a.phi[c - pxy];
+        ph[0] = a.phif[c + 1]; ph[1] = a.phif[c - 1];
+        ph[2] = a.phif[c + L.px]; ph[3] = a.phif[c - L.px];
+        ph[4] = a.phif[c + pxy]; ph[5] = a.phif[c - pxy];
       }
       float wc[5];
 #pragma unroll
