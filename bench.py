@@ -388,6 +388,7 @@ def main():
     ap.add_argument("--sur-steps", type=int, default=100, help="timed steps of the surrogate-active record")
     ap.add_argument("--no-surrogate-active", action="store_true")
     ap.add_argument("--sur-tol", type=float, default=1e-5, help="residual tolerance of the surrogate-active record")
+    ap.add_argument("--mlp-tol", type=float, default=1e-3, help="residual tolerance of the workload's surrogate form")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -553,7 +554,8 @@ def main():
             net = tctx.get_cooling_surrogate()
         f64x = measure(tlq.PREC_FP64, args.steps, False, cooling=tlq.COOL_EXACT, **sub)
         f64x["ctx"].close()
-        sur = measure(tlq.PREC_MIXED, args.steps, True, net=net, cooling=tlq.COOL_MLP, **sub)
+        sur = measure(tlq.PREC_MIXED, args.steps, True, net=net, cooling=tlq.COOL_MLP, cool_mlp_tol=args.mlp_tol,
+                      **sub)
         nm, nf, ns = sur["cool"]
         forms["fp64_exact_cooling"] = form(f64x)
         forms["mixed_surrogate"] = form(sur)
@@ -561,6 +563,7 @@ def main():
         forms["mixed_surrogate_vs_fp64_exact_cooling"] = accuracy(sur, f64x)
         surrogate = {"train": {k: rep[k] for k in ("ms_generate", "ms_train", "steps", "val_accept", "val_p99_rel_T",
                                                     "val_rmse_y")},
+                     "cool_mlp_tol": args.mlp_tol,
                      "timed_cell_steps_network": nm, "timed_cell_steps_fallback": nf,
                      "timed_cell_steps_single_step": ns,
                      "fallback_rate": nf / max(1, nm + nf),
