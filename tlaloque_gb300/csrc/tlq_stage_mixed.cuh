@@ -72,18 +72,9 @@ struct MixedSmem1 {
 // plane k read k-1..k+2; plane k+3 is requested into k-1's slot once those
 // faces are done); the conserved values HLLC takes at cell centres, formed
 // from them on the faces' cross-shaped region, in a 2-plane ring (k, k+1).
-#ifndef TLQ_S2_SLOPES
-#define TLQ_S2_SLOPES 1
-#endif
 struct MixedSmem2 {
   PlaneF<2> prm[4];
-#if TLQ_S2_SLOPES
-  float sx[5][MTY][MTX + 2];  // limited x slopes of plane k: cells i0-1 .. i0+MTX on the tile's rows
-  float sy[5][MTY + 2][MTX];  // limited y slopes of plane k: rows j0-1 .. j0+MTY on the tile's columns
-  float sz[2][5][MTY][MTX];   // limited z slopes of the tile's cells, planes k and k+1 (by parity)
-#else
   PlaneF<2> cu[2];
-#endif
   float fx[5][MTY][MTX + 1];
   float fy[5][MTY + 1][MTX];
   float fz[2][5][MTY][MTX];
@@ -639,138 +630,6 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
   }
 }
 
-#if TLQ_S2_SLOPES
-// The conserved values HLLC takes at a cell centre, from its primitives.
-__device__ __forceinline__ void prim_to_cons(const float* w, float igm1, float* u) {
-  const float k2 = __fmaf_rn(w[3], w[3], __fmaf_rn(w[2], w[2], __fmul_rn(w[1], w[1])));
-  u[0] = w[0];
-  u[1] = __fmul_rn(w[0], w[1]);
-  u[2] = __fmul_rn(w[0], w[2]);
-  u[3] = __fmul_rn(w[0], w[3]);
-  u[4] = __fmaf_rn(w[4], igm1, __fmul_rn(__fmul_rn(0.5f, w[0]), k2));
-}
-
-// Stage 2's limited slopes (limiter/average, HLLC.f90:560-638): a face's
-// left state is its left cell's primitives plus half that cell's slope, its
-// right state the right cell's minus half of its slope
-// (pL = p_i + phi_i/2, pR = p_{i+1} - phi_{i+1}/2, with phi_i =
-// average(p_i - p_{i-1}, p_{i+1} - p_i)), so each cell's slope along a
-// direction serves the two faces beside it and is evaluated once.  xy: the
-// x and y slopes of plane k on the cells beside the tile's faces; always:
-// the z slopes of plane zq on the tile's cells.
-template <int LIM>
-__device__ __forceinline__ void stage2_slopes(const Params& p, MixedSmem2& s, const float* Wk, const float* Wzm,
-                                              const float* Wz, const float* Wzp, int zq, bool xy) {
-  using G = MGeo<2>;
-  constexpr int NSX = (MTX + 2) * MTY, NSY = MTX * (MTY + 2), NSZ = MTX * MTY;
-  const int lim = LIM >= 0 ? LIM : p.limiter;
-  for (int t = (xy ? 0 : NSX + NSY) + (int)threadIdx.x; t < NSX + NSY + NSZ; t += MNT) {
-    if (t < NSX) {
-      const int cx = t % (MTX + 2), cy = t / (MTX + 2);  // cell (1 + cx, 2 + cy) of the box
-      const float* w = Wk + (2 + cy) * G::PX + 1 + cx;
-#pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        const float* we = w + e * G::PB;
-        s.sx[e][cy][cx] = average(we[0] - we[-1], we[1] - we[0], lim);
-      }
-    } else if (t < NSX + NSY) {
-      const int u = t - NSX, cx = u % MTX, cy = u / MTX;  // cell (2 + cx, 1 + cy)
-      const float* w = Wk + (1 + cy) * G::PX + 2 + cx;
-#pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        const float* we = w + e * G::PB;
-        s.sy[e][cy][cx] = average(we[0] - we[-G::PX], we[G::PX] - we[0], lim);
-      }
-    } else {
-      const int u = t - NSX - NSY, cx = u % MTX, cy = u / MTX;  // cell (2 + cx, 2 + cy)
-      const int o = (2 + cy) * G::PX + 2 + cx;
-#pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        const int oe = e * G::PB + o;
-        s.sz[zq & 1][e][cy][cx] = average(Wz[oe] - Wzm[oe], Wzp[oe] - Wz[oe], lim);
-      }
-    }
-  }
-}
-
-// Stage 2's faces of plane k from the primitives and the slopes, as one flat
-// task list (as mixed_faces).
-template <int LIM, int SOLV>
-__device__ __forceinline__ void stage2_faces(const Params& p, MixedSmem2& s, int i0, int j0, int k, bool xy, float gf,
-                                             float g1f, float igm1, const float* Wk, const float* Wk1) {
-  using G = MGeo<2>;
-  constexpr int NXF = (MTX + 1) * MTY, NYF = MTX * (MTY + 1), NZF = MTX * MTY;
-  constexpr int SXV = MTY * (MTX + 2), SYV = (MTY + 2) * MTX, SZV = MTY * MTX;  // variable strides
-  for (int t = (xy ? 0 : NXF + NYF) + (int)threadIdx.x; t < NXF + NYF + NZF; t += MNT) {
-    int d, fxl, fyl, sv;
-    const float *pl, *pr, *sl, *sr;
-    bool valid;
-    if (t < NXF) {
-      d = 1;
-      fxl = t % (MTX + 1);
-      fyl = t / (MTX + 1);
-      pl = Wk + (fyl + 2) * G::PX + fxl + 1;  // cell i0 - 1 + fxl
-      pr = pl + 1;
-      sl = &s.sx[0][fyl][fxl];
-      sr = sl + 1;
-      sv = SXV;
-      valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
-    } else if (t < NXF + NYF) {
-      d = 2;
-      const int u = t - NXF;
-      fxl = u % MTX;
-      fyl = u / MTX;
-      pl = Wk + (fyl + 1) * G::PX + fxl + 2;  // cell j0 - 1 + fyl
-      pr = pl + G::PX;
-      sl = &s.sy[0][fyl][fxl];
-      sr = sl + MTX;
-      sv = SYV;
-      valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
-    } else {
-      d = 3;
-      const int u = t - NXF - NYF;
-      fxl = u % MTX;
-      fyl = u / MTX;
-      const int o = (fyl + 2) * G::PX + fxl + 2;
-      pl = Wk + o;
-      pr = Wk1 + o;
-      sl = &s.sz[k & 1][0][fyl][fxl];
-      sr = &s.sz[(k + 1) & 1][0][fyl][fxl];
-      sv = SZV;
-      valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
-    }
-    if (!valid) continue;
-    float wl[5], wr[5], UL[5], UR[5], ff[5];
-#pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      wl[e] = pl[e * G::PB];
-      wr[e] = pr[e * G::PB];
-    }
-    prim_to_cons(wl, igm1, UL);
-    prim_to_cons(wr, igm1, UR);
-#pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      wl[e] = wl[e] + 0.5f * sl[e * sv];
-      wr[e] = wr[e] - 0.5f * sr[e * sv];
-    }
-    if (!riemann(SOLV >= 0 ? SOLV : p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) ff[e] = NAN;
-    }
-    if (d == 1) {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
-    } else if (d == 2) {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
-    } else {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
-    }
-  }
-}
-#endif
-
 // One tile of stage 2: streams UPP's FP32 primitives with a 2-cell halo;
 // writes U of the next step (FP64) and its face-ghost images, cools, and
 // reduces the signal speeds for the next dt.  nblk / bid: the mesh's tiles
@@ -812,7 +671,6 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
   PlaneWaits pw;
   pw.waited = k0 - 3;
   auto prm = [&](int q) { return &s.prm[q & 3].v[0][0][0]; };
-#if !TLQ_S2_SLOPES
   auto cu = [&](int q) { return &s.cu[q & 1].v[0][0][0]; };
   // conserved values of plane q (landed) on the cells beside its faces
   auto conserved = [&](int q) {
@@ -839,17 +697,12 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
       C[4 * G::PB + o] = __fmaf_rn(pr, igm1, __fmul_rn(__fmul_rn(0.5f, r), k2));
     }
   };
-#endif
 
   // prologue: planes k0-2 .. k0+1 (the first z face, k0 - 1/2, reads them)
   if (tid == 0)
     for (int q = k0 - 2; q <= k0 + 1; ++q) issue(q);
   for (int q = k0 - 2; q <= k0 + 1; ++q) pw.wait(s.bar, 4, q, &s.abort);
-#if TLQ_S2_SLOPES
-  stage2_slopes<LIM>(p, s, prm(k0 - 1), prm(k0 - 2), prm(k0 - 1), prm(k0), k0 - 1, false);  // z slopes of k0 - 1
-#else
   conserved(k0 - 1);
-#endif
 
   const int tx = tid % MTX, ty = tid / MTX;
   const int i = i0 + tx, j = j0 + ty;
@@ -867,19 +720,10 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
     float ph[6];
     bool queued = false;  // with the surrogate: handed to the cooling passes
     if (!first) pw.wait(s.bar, 4, k + 2, &s.abort);
-#if TLQ_S2_SLOPES
-    // x, y slopes of plane k (not needed below the chunk) and z slopes of k+1
-    stage2_slopes<LIM>(p, s, prm(k), prm(k), prm(k + 1), prm(k + 2), k + 1, !first);
-#else
     conserved(k + 1);
-#endif
     __syncthreads();
     if (s.abort) { aborted = true; break; }
-#if TLQ_S2_SLOPES
-    stage2_faces<LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, igm1, prm(k), prm(k + 1));
-#else
     mixed_faces<2, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, prm, cu);
-#endif
     __syncthreads();
     if (tid == 0 && k + 3 <= last) issue(k + 3);  // into plane k-1's slot: its faces are done
     if (first) continue;
