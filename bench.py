@@ -140,13 +140,19 @@ def bytes_per_zone(cfg, mixed: bool = False) -> dict:
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled during the timed region.
+    start() returns once the first sample has arrived (nvidia-smi takes a
+    few hundred ms to start), so the sampler is already running when timing
+    begins; begin()/end() bracket the timed region on the host clock and
+    stop() summarises the samples that arrived inside it."""
 
     def __init__(self, index: int):
         self.index = index
         self.samples = []
         self.proc = None
         self.thread = None
+        self.first = threading.Event()
+        self.t0 = self.t1 = None
 
     def start(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -154,20 +160,31 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
-            return
+            return self
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        self.first.wait(timeout=5.0)
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.samples.append(parts)
+                self.samples.append((time.monotonic(), parts))
+                self.first.set()
+
+    def begin(self):
+        self.t0 = time.monotonic()
+
+    def end(self):
+        self.t1 = time.monotonic()
 
     def stop(self):
+        if self.t1 is None:
+            self.end()
         if self.proc:
             self.proc.terminate()
             try:
@@ -176,14 +193,23 @@ class ClockSampler:
                 self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        if not self.samples:
+        t0 = self.t0 if self.t0 is not None else float("-inf")
+        inside = [s for t, s in self.samples if t0 <= t <= self.t1]
+        where = "timed region"
+        if not inside and self.samples:
+            # the region was shorter than the sampling interval: the sample closest to it
+            mid = 0.5 * (t0 + self.t1) if self.t0 is not None else self.t1
+            inside = [min(self.samples, key=lambda ts: abs(ts[0] - mid))[1]]
+            where = "nearest sample to the timed region (shorter than the sampling interval)"
+        if not inside:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        sm = [float(s[1]) for s in inside if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in inside if s[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[q] for s in self.samples for q in range(4) if s[5 + q].lower().startswith("active")})
+        reasons = sorted({names[q] for s in inside for q in range(4) if s[5 + q].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(inside), "sampled": where,
+                "region_s": round(self.t1 - t0, 4) if self.t0 is not None else None}
 
 
 # ---------------------------------------------------------------------------
@@ -284,9 +310,11 @@ def run_ensemble(args, world, rank, dist):
     b.synchronize()
     barrier(dist)
     b.enable_timing(True)
-    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    sampler.start()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))).start()
+    sampler.begin()
     b.run(args.steps)
+    b.synchronize()
+    sampler.end()
     clocks = sampler.stop()
     st = b.stats()
     ms = allmax(dist, st.ms_per_step * args.steps)
@@ -432,18 +460,20 @@ def main():
         ctx.advance(args.warmup)    # warm-up (builds the CUDA graphs)
         ctx.synchronize()
         st0 = ctx.stats()
-        sampler = ClockSampler(local) if sample_clocks else None
-        if sampler:
-            sampler.start()
+        sampler = ClockSampler(local).start() if sample_clocks else None
         ctx.enable_timing(True)
         barrier(dist)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if sampler:
+            sampler.begin()
         with torch.cuda.stream(stream):
             e0.record(stream)
             ctx.advance(steps)
             e1.record(stream)
         torch.cuda.synchronize()
+        if sampler:
+            sampler.end()
         barrier(dist)
         ms = e0.elapsed_time(e1)
         clocks = sampler.stop() if sampler else None

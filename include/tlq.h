@@ -170,7 +170,10 @@ typedef struct tlq_stats {
   long long timed;      /* number of timed steps behind the averages */
   double bytes_state;   /* device bytes held for the mesh state */
   long long cool_mlp;      /* TLQ_COOL_MLP: cell-steps cooled by the network (since upload) */
-  long long cool_fallback; /* TLQ_COOL_MLP: cell-steps handed to the exact integrator */
+  long long cool_fallback; /* TLQ_COOL_MLP: cell-steps with tau above cool_sub_frac cooled by the exact
+                              integrator's closed form instead of the network: outside its box, failing
+                              the residual check, or taken to the table's first temperature within the
+                              step (stage 2 does those of the table's first segment itself) */
   double ms_cool;          /* TLQ_COOL_MLP: average device time of the timed cooling passes */
   long long cool_single;   /* TLQ_COOL_MLP: cell-steps with tau <= cool_sub_frac, cooled by the exact
                               integrator's single exponential step (the network has nothing to gain;

@@ -129,15 +129,18 @@ __device__ __forceinline__ R average(R a, R b, int opt) {
       return R(0.5) * (a + b);
     case LIM_VANLEER:
       if constexpr (sizeof(R) == 4) {
-        // FP32 (mixed form): the same limiter without products of two
-        // differences, which underflow FP32 for cgs-scale densities
-        // (|drho| ~ 1e-25 g/cm^3 squared is below FLT_MIN):
-        // a b (a+b)/(a^2+b^2) = m r (1+r)/(1+r^2), m the larger, r = ratio <= 1.
-        if (!((a > R(0) && b > R(0)) || (a < R(0) && b < R(0)))) return R(0.0);
-        const bool ab = fabs(a) >= fabs(b);
-        const R m = ab ? a : b;
-        const R r = ab ? b / a : a / b;
-        return m * r * (R(1) + r) / (R(1) + r * r);
+        // FP32 (mixed form): products of two differences underflow FP32
+        // for cgs-scale densities (|drho| ~ 1e-25 g/cm^3 squared is below
+        // FLT_MIN), so a and b are first scaled by the power of two 2^-E
+        // that brings the larger magnitude to [1, 2) (E from its exponent
+        // bits; both scalings exact).  The limiter is homogeneous of degree
+        // 1: the scaled result times 2^E.  The scaled denominator lies in
+        // [1, 8], within the fast division's range.
+        const unsigned eb = __float_as_uint(fmaxf(fabsf(a), fabsf(b))) & 0x7f800000u;
+        const float s = __uint_as_float(0x7f000000u - eb);
+        const float x = a * s, y = b * s, xy = x * y;
+        if (!(xy > 0.0f)) return R(0.0);
+        return __fdividef(xy * (x + y), fmaf(x, x, y * y)) * __uint_as_float(eb);
       } else {
         if (a * b <= R(0.0)) return R(0.0);
         return a * b * (a + b) / (a * a + b * b);

@@ -219,6 +219,21 @@ __device__ __forceinline__ float cool_exact_dropf(const CoolTable& t, float temp
   return fmaxf(expm1f(__fadd_rn(lj, r)), __fsub_rn(t.Tf[0] / temp, 1.0f));
 }
 
+// Whether cool_exact_dropf takes a cell of the table's first segment
+// (the search's first node above temp is node 1) to the table's first
+// temperature: tau beyond the segment's own cooling time, with nothing of
+// the table below it (G(T_0) = 0).  The same FP32 operations as that
+// function's test, so a cell this accepts gets the bits it would give.
+__device__ __forceinline__ bool cool_floors_first(const CoolTable& t, float temp, float lam, float tau) {
+  const float a = __fsub_rn(1.0f, t.slopef[0]);
+  const float lxlo = logf(t.Tf[0] / temp);
+  const bool flat = fabsf(a) < 1e-6f;
+  const float tau_i = flat ? -lxlo : -expm1f(__fmul_rn(a, lxlo)) / a;
+  if (tau <= tau_i) return false;
+  const float G = __fsub_rn(t.gcumf[0], __fmul_rn(__fsub_rn(tau, tau_i), temp) / lam);
+  return !(G > 0.0f);
+}
+
 // The cooling of a cell that cools (cools_at), at temperature temp with
 // table coefficient aloss (found at table entry seg): w[4] and u4 updated.
 __device__ __forceinline__ void cool_cell_known(const Params& p, float cT, float inv_muamu, float gm1, float* w,
@@ -709,6 +724,7 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
   const bool cell_ok = (ty < MTY) && (i <= p.nx) && (j <= p.ny);
   float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
   unsigned nsingle = 0;  // with the surrogate: cells cooled in a single step
+  unsigned nfloor = 0;   // ... and first-segment cells taken to the floor
   const float cT = p.f_cT;
   const float inv_muamu = p.f_inv_muamu;
   bool aborted = false;
@@ -773,7 +789,12 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
         // A cell whose tau (Lambda n^2 dt / E_th, formed as the cooling
         // passes form it) is at most the single-step limit takes the exact
         // integrator's single exponential step here (the passes would do the
-        // same); the passes cool the others and take their signal speeds.
+        // same); so does a cell of the table's first segment that the exact
+        // integrator takes to the table's first temperature within the step
+        // (a medium sitting at that floor): the network is not asked for
+        // those (the passes would hand them to the exact integrator, with
+        // these bits).  The passes cool the others and take their signal
+        // speeds.
         const float T = (w[4] / w[0]) * cT;
         if (cools_at(p, T, un)) {
           const float nd = w[0] * inv_muamu;
@@ -782,7 +803,15 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
           const float lam = cool_coef_seg(p.cool, T, seg);
           const float tau = (lam * nd) * (nd / eth) * dtf;
           if (tau > p.f_cool_sub_frac) {
-            queued = true;
+            if (seg == 1 && cool_floors_first(p.cool, T, lam, tau)) {
+              // cool_cell_known's exact branch with cool_exact_dropf's floor
+              const float dp = __fmul_rn(w[4], __fsub_rn(p.cool.Tf[0] / T, 1.0f));
+              w[4] = __fadd_rn(w[4], dp);
+              un[4] = un[4] + f2d(dp / gm1);
+              ++nfloor;
+            } else {
+              queued = true;
+            }
           } else {
             cool_cell_known(p, cT, inv_muamu, gm1, w, un[4], dtf, T, lam, seg);
             ++nsingle;
@@ -831,10 +860,14 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
     d0 = d1 = d2 = NAN;
   }
   if (p.cooling == COOL_MLP && a.cool_counts) {
-    unsigned v = nsingle;
+    unsigned v = nsingle, f = nfloor;
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    for (int off = 16; off > 0; off >>= 1) {
+      v += __shfl_xor_sync(0xffffffffu, v, off);
+      f += __shfl_xor_sync(0xffffffffu, f, off);
+    }
     if ((tid & 31) == 0 && v) atomicAdd(&a.cool_counts[2], (unsigned long long)v);
+    if ((tid & 31) == 0 && f) atomicAdd(&a.cool_counts[1], (unsigned long long)f);  // the exact integrator's
   }
   if (p.cooling != COOL_MLP) {
     cfl_reduce_finalize_n<MNT>(d0, d1, d2, clk, p, true, s.red, &s.flag, nblk);
