@@ -18,7 +18,6 @@
 
 namespace tlq {
 
-
 // Geometry of the planes a stage stages in shared memory (x fastest, tile
 // cell (tx, ty) at (OY + ty, 2 + tx)).  Stage 1 (first-order fluxes of U and
 // the viscosity Laplacian of U) needs a 1-cell halo; its box is 2 cells wide
@@ -70,11 +69,14 @@ struct MixedSmem1 {
 };
 // Stage 2: UPP's FP32 primitives land by TMA in a 4-plane ring (the faces of
 // plane k read k-1..k+2; plane k+3 is requested into k-1's slot once those
-// faces are done); the conserved values HLLC takes at cell centres, formed
-// from them on the faces' cross-shaped region, in a 2-plane ring (k, k+1).
+// faces are done).  Each thread's cell operands of the plane (the old U, the
+// viscosity term, the potential's six neighbours) are copied from HBM into
+// its own slots before the face phase and read after it.
 struct MixedSmem2 {
   PlaneF<2> prm[4];
-  PlaneF<2> cu[2];
+  double uop[5][MNT];
+  float lvp[5][MNT];
+  float php[6][MNT];
   float fx[5][MTY][MTX + 1];
   float fy[5][MTY + 1][MTX];
   float fz[2][5][MTY][MTX];
@@ -316,22 +318,42 @@ __device__ __forceinline__ void write_ghost_prims(const Params& p, const Layout&
   }
 }
 
+// The conserved values of a cell from its FP32 primitives: what HLLC takes
+// at the cell centres beside a stage-2 face (UPP is stored as primitives).
+__device__ __forceinline__ void prim_cons(const float* w, float igm1, float* u) {
+  const float k2 = __fmaf_rn(w[3], w[3], __fmaf_rn(w[2], w[2], __fmul_rn(w[1], w[1])));
+  u[0] = w[0];
+  u[1] = __fmul_rn(w[0], w[1]);
+  u[2] = __fmul_rn(w[0], w[2]);
+  u[3] = __fmul_rn(w[0], w[3]);
+  u[4] = __fmaf_rn(w[4], igm1, __fmul_rn(__fmul_rn(0.5f, w[0]), k2));
+}
+
 // One face flux, direction d (1 x, 2 y, 3 z), from the primitives of the
-// four cells along d (w0..w3; stage 1 reads only w1, w2) and the conserved
-// values of the two cells beside the face, each `VS` floats between
-// variables.  Every face of both stages and of the batched kernels goes
-// through this one copy of the code.
+// four cells along d (w0..w3; stage 1 reads only w1, w2), each `VS` floats
+// between variables, and the conserved values of the two cells beside the
+// face: stage 1 reads them (uL, uR: the FP32 image of U), stage 2 forms them
+// from w1, w2 (igm1 = 1/(gamma-1)).  Every face of both stages and of the
+// batched kernels goes through this one copy of the code.
 template <int STAGE, int LIM, int SOLV, int VS>
-__device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, int d, const float* w0,
-                                          const float* w1, const float* w2, const float* w3, const float* uL,
-                                          const float* uR, float* ff) {
+__device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, float igm1, int d,
+                                          const float* w0, const float* w1, const float* w2, const float* w3,
+                                          const float* uL, const float* uR, float* ff) {
   float wll[5], wl[5], wr[5], wrr[5], UL[5], UR[5];
 #pragma unroll
   for (int e = 0; e < 5; ++e) {
     wl[e] = w1[e * VS];
     wr[e] = w2[e * VS];
-    UL[e] = uL[e * VS];
-    UR[e] = uR[e * VS];
+  }
+  if (STAGE == 1) {
+#pragma unroll
+    for (int e = 0; e < 5; ++e) {
+      UL[e] = uL[e * VS];
+      UR[e] = uR[e * VS];
+    }
+  } else {
+    prim_cons(wl, igm1, UL);
+    prim_cons(wr, igm1, UR);
   }
   if (STAGE == 2) {
 #pragma unroll
@@ -350,16 +372,17 @@ __device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, 
 // All x, y and z faces of plane k of a tile as one flat task list (x faces
 // (MTX+1) x MTY, y faces MTX x (MTY+1), z faces MTX x MTY: no face twice);
 // xy false: only the z faces (the plane below a z-chunk).  prm(q) / cu(q):
-// the planes of primitives / conserved values of plane q.
+// the planes of primitives / conserved values of plane q (stage 1; stage 2
+// forms the conserved values from the primitives).
 template <int STAGE, int LIM, int SOLV, class Smem, class PrmOf, class CuOf>
 __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, int j0, int k, bool xy, float gf,
-                                            float g1f, PrmOf prm, CuOf cu) {
+                                            float g1f, float igm1, PrmOf prm, CuOf cu) {
   using G = MGeo<STAGE>;
   constexpr int OY = G::OY, PX = G::PX, VS = G::PB;
   constexpr int NXF = (MTX + 1) * MTY, NYF = MTX * (MTY + 1), NZF = MTX * MTY;
   const int tbeg = xy ? 0 : NXF + NYF;
   const float* pk = prm(k);
-  const float* ck = cu(k);
+  const float* ck = (STAGE == 1) ? cu(k) : nullptr;
   for (int t = tbeg + (int)threadIdx.x; t < NXF + NYF + NZF; t += MNT) {
     int d, fxl, fyl;
     const float *w0, *w1, *w2, *w3, *uL, *uR;
@@ -372,8 +395,8 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w0 = w1 - 1;
       w2 = w1 + 1;
       w3 = w1 + 2;
-      uL = ck + (fyl + OY) * PX + fxl + 1;
-      uR = uL + 1;
+      uL = (STAGE == 1) ? ck + (fyl + OY) * PX + fxl + 1 : nullptr;
+      uR = (STAGE == 1) ? uL + 1 : nullptr;
       valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
     } else if (t < NXF + NYF) {
       d = 2;
@@ -384,8 +407,8 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w0 = w1 - PX;
       w2 = w1 + PX;
       w3 = w1 + 2 * PX;
-      uL = ck + (fyl - 1 + OY) * PX + fxl + 2;
-      uR = uL + PX;
+      uL = (STAGE == 1) ? ck + (fyl - 1 + OY) * PX + fxl + 2 : nullptr;
+      uR = (STAGE == 1) ? uL + PX : nullptr;
       valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
     } else {
       d = 3;
@@ -397,13 +420,13 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w1 = pk + o;
       w2 = prm(k + 1) + o;
       w3 = prm(k + 2) + o;
-      uL = ck + o;
-      uR = cu(k + 1) + o;
+      uL = (STAGE == 1) ? ck + o : nullptr;
+      uR = (STAGE == 1) ? cu(k + 1) + o : nullptr;
       valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
     }
     if (!valid) continue;
     float ff[5];
-    face_flux<STAGE, LIM, SOLV, VS>(p, gf, g1f, d, w0, w1, w2, w3, uL, uR, ff);
+    face_flux<STAGE, LIM, SOLV, VS>(p, gf, g1f, igm1, d, w0, w1, w2, w3, uL, uR, ff);
     if (d == 1) {
 #pragma unroll
       for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
@@ -576,7 +599,7 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
       if (s.abort) { aborted = true; break; }
       if (tid == 0 && k + 2 <= last) issue(k + 2);
     }
-    mixed_faces<1, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, prm, cu);
+    mixed_faces<1, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, 0.0f, prm, cu);
     __syncthreads();
     if (first || !cell_ok) continue;
 
@@ -686,38 +709,12 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
   PlaneWaits pw;
   pw.waited = k0 - 3;
   auto prm = [&](int q) { return &s.prm[q & 3].v[0][0][0]; };
-  auto cu = [&](int q) { return &s.cu[q & 1].v[0][0][0]; };
-  // conserved values of plane q (landed) on the cells beside its faces
-  auto conserved = [&](int q) {
-    const float* W = prm(q);
-    float* C = &s.cu[q & 1].v[0][0][0];
-    constexpr int NROW = (MTX + 2) * MTY, NCOL = 2 * MTX;
-    for (int t = tid; t < NROW + NCOL; t += MNT) {
-      int lx, ly;
-      if (t < NROW) {
-        lx = 1 + t % (MTX + 2);
-        ly = 2 + t / (MTX + 2);
-      } else {
-        const int u = t - NROW;
-        lx = 2 + u % MTX;
-        ly = (u < MTX) ? 1 : MTY + 2;
-      }
-      const int o = ly * G::PX + lx;
-      const float r = W[o], vx = W[G::PB + o], vy = W[2 * G::PB + o], vz = W[3 * G::PB + o], pr = W[4 * G::PB + o];
-      const float k2 = __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx)));
-      C[o] = r;
-      C[G::PB + o] = __fmul_rn(r, vx);
-      C[2 * G::PB + o] = __fmul_rn(r, vy);
-      C[3 * G::PB + o] = __fmul_rn(r, vz);
-      C[4 * G::PB + o] = __fmaf_rn(pr, igm1, __fmul_rn(__fmul_rn(0.5f, r), k2));
-    }
-  };
+  auto nocu = [](int) -> const float* { return nullptr; };
 
   // prologue: planes k0-2 .. k0+1 (the first z face, k0 - 1/2, reads them)
   if (tid == 0)
     for (int q = k0 - 2; q <= k0 + 1; ++q) issue(q);
   for (int q = k0 - 2; q <= k0 + 1; ++q) pw.wait(s.bar, 4, q, &s.abort);
-  conserved(k0 - 1);
 
   const int tx = tid % MTX, ty = tid / MTX;
   const int i = i0 + tx, j = j0 + ty;
@@ -735,28 +732,39 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
     float lv[5];
     float ph[6];
     bool queued = false;  // with the surrogate: handed to the cooling passes
+    if (!first && cell_ok) {
+      // the cell's operands in HBM, landing while the faces are evaluated
+#pragma unroll
+      for (int e = 0; e < 5; ++e) cp_async8(&s.uop[e][tid], &a.uold[e * L.plane + c]);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) cp_async4(&s.lvp[e][tid], &a.lapf[e * L.plane + c]);
+      if (p.gravity) {
+        cp_async4(&s.php[0][tid], &a.phif[c + 1]);
+        cp_async4(&s.php[1][tid], &a.phif[c - 1]);
+        cp_async4(&s.php[2][tid], &a.phif[c + L.px]);
+        cp_async4(&s.php[3][tid], &a.phif[c - L.px]);
+        cp_async4(&s.php[4][tid], &a.phif[c + pxy]);
+        cp_async4(&s.php[5][tid], &a.phif[c - pxy]);
+      }
+      cp_async_commit();
+    }
     if (!first) pw.wait(s.bar, 4, k + 2, &s.abort);
-    conserved(k + 1);
     __syncthreads();
     if (s.abort) { aborted = true; break; }
-    mixed_faces<2, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, prm, cu);
+    mixed_faces<2, LIM, SOLV>(p, s, i0, j0, k, !first, gf, g1f, igm1, prm, nocu);
     __syncthreads();
     if (tid == 0 && k + 3 <= last) issue(k + 3);  // into plane k-1's slot: its faces are done
     if (first) continue;
 
     if (cell_ok) {
-      // The cell's global operands are loaded here, after the face phase:
-      // held across it (27 more live registers) they made the kernel spill,
-      // and with 5 blocks per SM other warps cover their latency (measured
-      // 1.93 -> 1.81 ms per launch at 256^3).
+      cp_async_wait_all();  // this thread's own copies: no barrier
 #pragma unroll
-      for (int e = 0; e < 5; ++e) uc[e] = a.uold[e * L.plane + c];
+      for (int e = 0; e < 5; ++e) uc[e] = s.uop[e][tid];
 #pragma unroll
-      for (int e = 0; e < 5; ++e) lv[e] = a.lapf[e * L.plane + c];
+      for (int e = 0; e < 5; ++e) lv[e] = s.lvp[e][tid];
       if (p.gravity) {
-        ph[0] = a.phif[c + 1]; ph[1] = a.phif[c - 1];
-        ph[2] = a.phif[c + L.px]; ph[3] = a.phif[c - L.px];
-        ph[4] = a.phif[c + pxy]; ph[5] = a.phif[c - pxy];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) ph[q] = s.php[q][tid];
       }
       float wc[5];
 #pragma unroll
@@ -851,6 +859,7 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
     }
   }
 
+  cp_async_wait_all();  // (a tile that gave up leaves no copy of its own in flight)
   double d0 = f2d(m0), d1 = f2d(m1), d2 = f2d(m2);
   if (aborted) {
     if (tid == 0) {
