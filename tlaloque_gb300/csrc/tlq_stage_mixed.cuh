@@ -369,20 +369,67 @@ __device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, 
   }
 }
 
-// All x, y and z faces of plane k of a tile as one flat task list (x faces
-// (MTX+1) x MTY, y faces MTX x (MTY+1), z faces MTX x MTY: no face twice);
-// xy false: only the z faces (the plane below a z-chunk).  prm(q) / cu(q):
-// the planes of primitives / conserved values of plane q (stage 1; stage 2
-// forms the conserved values from the primitives).
+// All x, y and z faces of plane k of a tile (x faces (MTX+1) x MTY, y faces
+// MTX x (MTY+1), z faces MTX x MTY: no face twice); xy false: only the z
+// faces (the plane below a z-chunk).  prm(q) / cu(q): the planes of
+// primitives / conserved values of plane q (stage 1; stage 2 forms the
+// conserved values from the primitives).
+//   Stage 1 (first-order faces, little code per face) evaluates them in
+// three rounds of one direction each, the direction known at compile time:
+// each thread the left x face, the lower y face and the upper z face of one
+// cell, and the tile's right x edge (warp 0) and upper y edge (warp 1) as
+// second faces of their rounds.  Stage 2's faces (limiter and HLLC) are one
+// flat task list through one copy of the code (the rounds' three copies
+// measured slower there).
 template <int STAGE, int LIM, int SOLV, class Smem, class PrmOf, class CuOf>
 __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, int j0, int k, bool xy, float gf,
                                             float g1f, float igm1, PrmOf prm, CuOf cu) {
   using G = MGeo<STAGE>;
   constexpr int OY = G::OY, PX = G::PX, VS = G::PB;
   constexpr int NXF = (MTX + 1) * MTY, NYF = MTX * (MTY + 1), NZF = MTX * MTY;
-  const int tbeg = xy ? 0 : NXF + NYF;
   const float* pk = prm(k);
   const float* ck = (STAGE == 1) ? cu(k) : nullptr;
+  if constexpr (STAGE == 1) {
+    constexpr int NC = MTX * MTY;
+    const int tid = threadIdx.x;
+    if (xy) {
+      for (int t = tid; t < NXF; t += MNT) {  // t >= NC: the right edge, x = MTX
+        const int fxl = (t < NC) ? t % MTX : MTX, fyl = (t < NC) ? t / MTX : t - NC;
+        const int o = (fyl + OY) * PX + fxl + 1;  // cell i0 - 1 + fxl
+        if ((i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny)) {
+          float ff[5];
+          face_flux<1, LIM, SOLV, VS>(p, gf, g1f, igm1, 1, nullptr, pk + o, pk + o + 1, nullptr, ck + o, ck + o + 1,
+                                      ff);
+#pragma unroll
+          for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
+        }
+      }
+      for (int t = (tid + MNT - 32) % MNT; t < NYF; t += MNT) {  // t >= NC: the upper edge, y = MTY
+        const int fxl = (t < NC) ? t % MTX : t - NC, fyl = (t < NC) ? t / MTX : MTY;
+        const int o = (fyl - 1 + OY) * PX + fxl + 2;  // cell j0 - 1 + fyl
+        if ((i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny)) {
+          float ff[5];
+          face_flux<1, LIM, SOLV, VS>(p, gf, g1f, igm1, 2, nullptr, pk + o, pk + o + PX, nullptr, ck + o,
+                                      ck + o + PX, ff);
+#pragma unroll
+          for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
+        }
+      }
+    }
+    {
+      const int fxl = tid % MTX, fyl = tid / MTX;
+      const int o = (fyl + OY) * PX + fxl + 2;
+      if (tid < NZF && (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny)) {
+        float ff[5];
+        face_flux<1, LIM, SOLV, VS>(p, gf, g1f, igm1, 3, nullptr, pk + o, prm(k + 1) + o, nullptr, ck + o,
+                                    cu(k + 1) + o, ff);
+#pragma unroll
+        for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
+      }
+    }
+    return;
+  }
+  const int tbeg = xy ? 0 : NXF + NYF;
   for (int t = tbeg + (int)threadIdx.x; t < NXF + NYF + NZF; t += MNT) {
     int d, fxl, fyl;
     const float *w0, *w1, *w2, *w3, *uL, *uR;
@@ -395,8 +442,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w0 = w1 - 1;
       w2 = w1 + 1;
       w3 = w1 + 2;
-      uL = (STAGE == 1) ? ck + (fyl + OY) * PX + fxl + 1 : nullptr;
-      uR = (STAGE == 1) ? uL + 1 : nullptr;
+      uL = uR = nullptr;
       valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
     } else if (t < NXF + NYF) {
       d = 2;
@@ -407,8 +453,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w0 = w1 - PX;
       w2 = w1 + PX;
       w3 = w1 + 2 * PX;
-      uL = (STAGE == 1) ? ck + (fyl - 1 + OY) * PX + fxl + 2 : nullptr;
-      uR = (STAGE == 1) ? uL + PX : nullptr;
+      uL = uR = nullptr;
       valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
     } else {
       d = 3;
@@ -420,8 +465,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w1 = pk + o;
       w2 = prm(k + 1) + o;
       w3 = prm(k + 2) + o;
-      uL = (STAGE == 1) ? ck + o : nullptr;
-      uR = (STAGE == 1) ? cu(k + 1) + o : nullptr;
+      uL = uR = nullptr;
       valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
     }
     if (!valid) continue;
