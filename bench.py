@@ -100,8 +100,9 @@ def make_workload(name: str):
     elif name.startswith("clumpy") and name[6:].isdigit():
         n = int(name[6:])
         cfg, U0 = problems.clumpy(n)
-        desc = (f"clumpy radiative medium {n}^3, periodic (8 pc)^3, lognormal density (k^-5/3), log T uniform "
-                "1e3-1e8 K, rms Mach 2, HLLC + van Leer, sub-cycled tabulated cooling")
+        desc = (f"clumpy radiative medium {n}^3, periodic (8 pc)^3, lognormal density (sigma ln n = 1, mean "
+                "1 cm^-3, k^-5/3), log T uniform 1e3-1e8 K, rms Mach 2, HLLC + van Leer, sub-cycled tabulated "
+                "cooling")
     elif name == "sod":
         cfg, U0 = problems.sod_tube()
         desc = "Sod shock tube 256x4x4, HLL, gamma 1.4, outflow"
@@ -415,7 +416,7 @@ def main():
     ap.add_argument("--clumpy-n", type=int, default=256, help="mesh of the surrogate-active record")
     ap.add_argument("--sur-steps", type=int, default=100, help="timed steps of the surrogate-active record")
     ap.add_argument("--no-surrogate-active", action="store_true")
-    ap.add_argument("--sur-tol", type=float, default=1e-5, help="residual tolerance of the surrogate-active record")
+    ap.add_argument("--sur-tol", type=float, default=1e-3, help="residual tolerance of the surrogate-active record")
     ap.add_argument("--mlp-tol", type=float, default=1e-3, help="residual tolerance of the workload's surrogate form")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -531,13 +532,12 @@ def main():
                     "energy_drift_rel_per_100_steps": abs(a["E"] - judge["E"]) / abs(judge["E"]) * (100.0 / n_all)}
         nm, nf, ns = act["cool"]
         return {"workload": f"clumpy radiative medium {args.clumpy_n}^3, periodic (8 pc)^3, lognormal density "
-                            "(sigma log10 n = 1, k^-5/3), log T uniform 1e3-1e8 K, rms Mach 2, the wind bubble's "
+                            "(sigma ln n = 1, mean 1 cm^-3, k^-5/3), log T uniform 1e3-1e8 K, rms Mach 2, the wind bubble's "
                             "cooling curve; HLLC + van Leer",
                 "mesh": [ccfg.nx, ccfg.ny, ccfg.nz], "warmup": args.warmup, "steps": nst,
                 "cool_mlp_tol": args.sur_tol,
-                "tol_note": "the residual tolerance of an accepted prediction, |T_pred - T_exact| / T; the north "
-                            "star's 1e-3 bounds each cell, but on this stiff medium the accepted cells' small "
-                            "shared bias sums to ~1e-6 per 100 steps there, so the record runs at a tighter one",
+                "tol_note": "the residual tolerance of an accepted prediction, |T_pred - T_exact| / T (the north "
+                            "star's a-posteriori check at 1e-3)",
                 "value": act["value"], "unit": UNIT, "ms_per_step": act["ms"] / nst, "ms_stage1": act["k1"],
                 "ms_stage2": act["k2"], "ms_cool_passes": act["kc"],
                 "timed_cell_steps_network": nm, "timed_cell_steps_exact": nf, "timed_cell_steps_single_step": ns,

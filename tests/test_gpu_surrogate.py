@@ -220,18 +220,18 @@ def test_wind_bubble_bars_with_surrogate(trained):
 
 def test_clumpy_100_steps_energy_bar(trained):
     """The stiffest case: a 64^3 clumpy medium (lognormal density, log T
-    uniform over 1e3-1e8 K, rms Mach 2; the coarse mesh's large dt puts ~16 %
-    of the cells in the network's domain every step), 100 steps of mixed +
-    surrogate against the plain FP64 step with the exact integrator.
+    uniform over 1e3-1e8 K, rms Mach 2; the coarse mesh's large dt puts
+    ~13 % of the cells in the network's domain every step), 100 steps of
+    mixed + surrogate against the plain FP64 step with the exact integrator.
 
-    Which term carries the drift: at the benchmark spec's residual tolerance
-    (1e-3 of T) every accepted cell is within 1e-3 of the exact integrator,
-    but the accepted cells' errors share the network's local bias, and
-    ~40 k of them a step sum to ~1e-5 of the total energy per 100 steps --
-    the network's share, well above the mixed form's own (the mixed step
-    with the exact integrator).  The bar (1 % L1 density, 1e-6 energy drift
-    per 100 steps) holds with the tolerance at 3e-7 of T, where the network
-    still cools a quarter or more of its cells."""
+    The bar (1 % L1 density, 1e-6 energy drift per 100 steps) holds at the
+    the benchmark spec's residual tolerance (1e-3 of T) with the network accepting
+    nearly every cell it is asked for.  Which term carries the drift: the
+    accepted cells' errors share the network's local bias and sum to ~1e-7
+    of the total energy per 100 steps, well above the mixed form's own share
+    (the mixed step with the exact integrator, ~1e-9); a tighter tolerance
+    (3e-7 of T) takes most of it away while the network still cools most of
+    its cells."""
     _, net = trained
     cfg, U0 = problems.clumpy(64, seed=5)
     nst = 100
@@ -244,14 +244,15 @@ def test_clumpy_100_steps_energy_bar(trained):
     for r in (mix, loose, tight):
         assert r["rc"] == tlq.OK and r["it"] == nst
     accept = lambda r: r["mlp"] / max(1, r["mlp"] + r["fb"])
-    err = rel_l1(interior(tight["W"])[0], interior(ref["W"])[0])
+    err = rel_l1(interior(loose["W"])[0], interior(ref["W"])[0])
     print(f"clumpy64 x {nst}: mixed form alone drift {drift(mix):.3e}; surrogate tol 1e-3 drift {drift(loose):.3e} "
-          f"(accept {accept(loose):.3f}, {loose['mlp'] / nst:.0f} network cells/step); tol 3e-7 drift "
-          f"{drift(tight):.3e} L1 rho {err:.3e} (accept {accept(tight):.3f}, {tight['mlp'] / nst:.0f}/step)")
-    assert drift(mix) <= 1e-6                    # the mixed form's own share
-    assert drift(loose) > drift(mix)             # at 1e-3 the network's accepted errors dominate
-    assert err <= 1e-2 and drift(tight) <= 1e-6  # the bar, at the tight tolerance
-    assert accept(tight) >= 0.25 and tight["mlp"] / nst > 5000
+          f"L1 rho {err:.3e} (accept {accept(loose):.3f}, {loose['mlp'] / nst:.0f} network cells/step); tol 3e-7 "
+          f"drift {drift(tight):.3e} (accept {accept(tight):.3f}, {tight['mlp'] / nst:.0f}/step)")
+    assert drift(mix) <= 1e-8                    # the mixed form's own share
+    assert err <= 1e-2 and drift(loose) <= 1e-6  # the bar, at the benchmark spec's tolerance
+    assert accept(loose) >= 0.9 and loose["mlp"] / nst > 20000
+    assert drift(mix) < drift(loose)             # the network's accepted errors carry the drift
+    assert drift(tight) < 0.5 * drift(loose) and accept(tight) >= 0.5
 
 
 def test_surrogate_gain_over_sub_cycling(trained):
@@ -259,10 +260,10 @@ def test_surrogate_gain_over_sub_cycling(trained):
     on, on a clumpy medium where cooling is stiff: the step's cooling against
     the judge (FP64 step, exact integrator).  The surrogate is more accurate
     than the sub-cycled integrator at a coarse setting (16 sub-steps of at
-    most 0.1 tau) and faster than the sub-cycled integrator run fine enough
-    to be close to exact (2e-3 tau, up to 20000 sub-steps).  The exact
-    integrator's closed form, which the surrogate checks every prediction
-    against, is printed beside them."""
+    most 0.1 tau), and both faster and more accurate than the sub-cycled
+    integrator run fine enough to be close to exact (2e-3 tau, up to 20000
+    sub-steps).  The exact integrator's closed form, which the surrogate
+    checks every prediction against, is printed beside them."""
     _, net = trained
     cfg, U0 = problems.clumpy(48, seed=1)
     n = 3
@@ -282,7 +283,7 @@ def test_surrogate_gain_over_sub_cycling(trained):
           f"ms/step coarse {coarse['ms']:.3f} fine {fine['ms']:.3f} mlp {mlp['ms']:.3f} closed form "
           f"{closed['ms']:.3f}; fallback {frac_fb:.4f}")
     assert e_mlp < 0.5 * e_coarse
-    assert mlp["ms"] < 0.5 * fine["ms"]
+    assert mlp["ms"] < fine["ms"] and e_mlp < e_fine
     # a tighter residual tolerance: fewer accepted cells, closer to the exact integrator
     tight = run(mixed_cfg(cfg, tlq.COOL_MLP, cool_mlp_tol=1e-5, **SUB), U0, n, net=net)
     e_tight = rel_l1(eth(tight), eth(exact))

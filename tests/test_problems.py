@@ -110,8 +110,8 @@ def test_clumpy_medium_distributions():
     assert all(b == tlq.BC_PERIODIC for b in cfg.bc)
     rho, vx, vy, vz, p = prims(cfg, U)
     nd = interior(rho) / (1.3 * P.AMU)
-    lgn = np.log10(nd)
-    assert abs(lgn.mean()) < 1e-9 and abs(lgn.std() - 1.0) < 1e-9  # lognormal density, sigma(log10 n) = 1
+    # lognormal density: sigma(ln n) = 1, mean 1 cm^-3
+    assert abs(np.log(nd).std() - 1.0) < 1e-9 and abs(nd.mean() - 1.0) < 1e-9
     T = interior(p) * 1.3 * P.AMU / (interior(rho) * P.KB)
     assert T.min() >= 1e3 * (1 - 1e-9) and T.max() <= 1e8 * (1 + 1e-9)
     cs4 = np.sqrt(cfg.gamma * P.KB * 1.0e4 / (1.3 * P.AMU))

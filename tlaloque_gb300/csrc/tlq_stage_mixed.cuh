@@ -236,6 +236,18 @@ __device__ __forceinline__ bool cool_floors_first(const CoolTable& t, float temp
   return !(G > 0.0f);
 }
 
+// exp(x) - 1 of a cooling factor's exponent (x <= 0): the Taylor series to
+// x^5 for |x| < 1/64 (truncation below x^6/720, under 2e-12 of the result),
+// expm1f beyond.  Horner steps as explicit FMAs (no contraction choice).
+__device__ __forceinline__ float expm1_cool(float x) {
+  if (!(fabsf(x) < 0.015625f)) return expm1f(x);
+  float r = __fmaf_rn(x, 1.0f / 120.0f, 1.0f / 24.0f);
+  r = __fmaf_rn(x, r, 1.0f / 6.0f);
+  r = __fmaf_rn(x, r, 0.5f);
+  r = __fmaf_rn(x, r, 1.0f);
+  return __fmul_rn(x, r);
+}
+
 // The cooling of a cell that cools (cools_at), at temperature temp with
 // table coefficient aloss (found at table entry seg): w[4] and u4 updated.
 __device__ __forceinline__ void cool_cell_known(const Params& p, float cT, float inv_muamu, float gm1, float* w,
@@ -258,8 +270,13 @@ __device__ __forceinline__ void cool_cell_known(const Params& p, float cT, float
     nsub = (q > (float)p.cool_max_sub) ? p.cool_max_sub : (int)q;
     if (nsub < 1) nsub = 1;
   }
+  // Each sub-step's factor f = exp(-ce h) is carried as f - 1 (expm1_cool),
+  // and the pressure's relative change over the sub-steps as q = p/p0 - 1:
+  // with ce h ~ 1e-3, f itself keeps only the top few digits of f - 1 in
+  // FP32 (and p - p0 those of the change), which biased the energy removed
+  // by ~1e-3 of itself.
   const float h = dt / (float)nsub;
-  const float fmin = 1.0f - p.f_cooling_limit;
+  float q = 0.0f;
   for (int s = 0; s < nsub; ++s) {
     if (s > 0) {
       temp = (w[4] / w[0]) * cT;
@@ -268,17 +285,18 @@ __device__ __forceinline__ void cool_cell_known(const Params& p, float cT, float
       aloss = cool_coef_seg(t, temp, seg);
       ce = (aloss * n) * (n / ETH);
     }
-    float f = __expf(-ce * h);
-    if (f < fmin) f = fmin;
+    float fq = expm1_cool(-ce * h);
+    if (fq < -p.f_cooling_limit) fq = -p.f_cooling_limit;  // f < 1 - cooling_limit
     bool floored = false;
-    if (temp * f < (float)T_FLOOR) {
-      f = (float)T_FLOOR / temp;
+    if (__fmaf_rn(temp, fq, temp) < (float)T_FLOOR) {
+      fq = __fsub_rn((float)T_FLOOR / temp, 1.0f);
       floored = true;
     }
-    w[4] = w[4] * f;
+    q = __fadd_rn(q, __fmaf_rn(q, fq, fq));  // (1 + q)(1 + fq) - 1
+    w[4] = __fmaf_rn(p0, q, p0);
     if (floored) break;
   }
-  u4 = u4 + f2d(__fsub_rn(w[4], p0) / gm1);
+  u4 = u4 + f2d(__fmul_rn(p0, q) / gm1);
 }
 
 __device__ __forceinline__ void cool_cell_f(const Params& p, float cT, float inv_muamu, float gm1, float* w,

@@ -216,12 +216,13 @@ def gaussian_field(n: int, seed: int, slope: float = -5.0 / 3.0) -> np.ndarray:
 
 
 def clumpy(n: int = 384, seed: int = 0, cooling: int = COOL_SUBCYCLE, box_pc: float = 8.0, mach: float = 2.0,
-           sigma_log10_n: float = 1.0, cool_max_sub: int = 16, cool_sub_frac: float = 0.1):
-    """Clumpy radiative medium: n^3 periodic (8 pc)^3 box; log10 n Gaussian
-    (mean 0, std 1, k^-5/3 spectrum: a lognormal density); log10 T uniform in
-    [3, 8] (a k^-5/3 Gaussian field through its normal CDF); velocities k^-5/3
-    fields with rms Mach 2 relative to the 1e4 K sound speed; mu 1.3, gamma
-    5/3, HLLC, CFL 0.4; synthetic cooling curve."""
+           sigma_ln_n: float = 1.0, cool_max_sub: int = 16, cool_sub_frac: float = 0.1):
+    """Clumpy radiative medium: n^3 periodic (8 pc)^3 box; a lognormal
+    density, ln n Gaussian with standard deviation sigma_ln_n (k^-5/3
+    spectrum), scaled to a mean of 1 cm^-3; log10 T uniform in [3, 8] (a
+    k^-5/3 Gaussian field through its normal CDF); velocities k^-5/3 fields
+    with rms Mach 2 relative to the 1e4 K sound speed; mu 1.3, gamma 5/3,
+    HLLC, CFL 0.4; synthetic cooling curve."""
     from scipy.special import ndtr
 
     L = box_pc * PC
@@ -231,15 +232,15 @@ def clumpy(n: int = 384, seed: int = 0, cooling: int = COOL_SUBCYCLE, box_pc: fl
                  cfl=0.4, eta=0.5e-2, mu0=mu, limiter=LIMITER_VANLEER, solver=SOLVER_HLLC, bc=(BC_PERIODIC,) * 6,
                  cooling=cooling, cool_max_sub=cool_max_sub, cool_sub_frac=cool_sub_frac, cool_T=T_cool,
                  cool_logL=logL)
-    lgn = sigma_log10_n * gaussian_field(n, seed)
+    nd = np.exp(sigma_ln_n * gaussian_field(n, seed))
+    nd /= nd.mean()
     lgT = 3.0 + 5.0 * ndtr(gaussian_field(n, seed + 1))
     cs4 = np.sqrt(cfg.gamma * KB * 1.0e4 / (mu * AMU))
     vel = [gaussian_field(n, seed + 2 + q) for q in range(3)]
     scale = mach * cs4 / np.sqrt(np.mean(vel[0] ** 2 + vel[1] ** 2 + vel[2] ** 2))
-    nd = 10.0 ** lgn
     rho_i = nd * mu * AMU
     p_i = nd * KB * 10.0 ** lgT
-    del lgn, lgT, nd
+    del lgT, nd
     # interior fields; ghosts by periodic wrap (borders() refreshes them)
     wrap = lambda a: np.pad(a, 2, mode="wrap")
     return cfg, conserved(cfg, wrap(rho_i), *(wrap(scale * v) for v in vel), wrap(p_i))
