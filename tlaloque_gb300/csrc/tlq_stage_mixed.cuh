@@ -52,12 +52,13 @@ struct MixedBlocks {
 
 // Stage 1: U arrives in FP64 (one TMA landing slot; the next plane is
 // requested as soon as this one is converted, a whole plane's work ahead of
-// its use), converted per plane to FP32 conserved values (3-plane ring: the
-// Laplacian of plane k reads k-1..k+1) and primitives (2-plane ring: the
-// faces of plane k read k and k+1).
+// its use), converted per plane to FP32 conserved values (4-plane ring: the
+// Laplacian of plane k reads k-1..k+1, and plane k+2's conversion may run
+// beside it) and primitives (2-plane ring: the faces of plane k read k and
+// k+1).
 struct MixedSmem1 {
   double raw[5 * MGeo<1>::PB];
-  PlaneF<1> cu[3];
+  PlaneF<1> cu[4];
   PlaneF<1> prm[2];
   float fx[5][MTY][MTX + 1];
   float fy[5][MTY + 1][MTX];
@@ -100,7 +101,6 @@ struct MixedSmemSel<2> {
 template <int S>
 using MixedSmem = typename MixedSmemSel<S>::type;
 
-__device__ __forceinline__ int cu_slot(int q) { return (q + 12) % 3; }
 
 // One cell: FP64 conserved (stride vs) -> FP32 conserved and primitives.
 // The pressure of a cell whose kinetic energy exceeds 0.99 of its total
@@ -598,7 +598,7 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
   // U of plane q (landed) -> FP32 conserved and primitives on the cells its
   // faces and Laplacian read
   auto convert = [&](int q) {
-    float* C = &s.cu[cu_slot(q)].v[0][0][0];
+    float* C = &s.cu[q & 3].v[0][0][0];
     float* W = &s.prm[q & 1].v[0][0][0];
     constexpr int NROW = (MTX + 2) * MTY, NCOL = 2 * MTX;
     for (int t = tid; t < NROW + NCOL; t += MNT) {
@@ -622,7 +622,7 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
     }
   };
   auto prm = [&](int q) { return &s.prm[q & 1].v[0][0][0]; };
-  auto cu = [&](int q) { return &s.cu[cu_slot(q)].v[0][0][0]; };
+  auto cu = [&](int q) { return &s.cu[q & 3].v[0][0][0]; };
 
   // prologue: planes k0-1 and k0
   bool aborted = false;
@@ -654,8 +654,10 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
       }
     }
     if (!first) {
+      // no barrier before the conversion: the previous plane's cell phase,
+      // which other warps may still be running, reads the conserved slots
+      // of planes k-2..k and no primitive slot
       pw.wait(s.bar, 1, k + 1, &s.abort);
-      __syncthreads();  // the previous plane's epilogue read the ring slots this conversion overwrites
       convert(k + 1);
       __syncthreads();
       if (s.abort) { aborted = true; break; }
@@ -666,9 +668,17 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
     if (first || !cell_ok) continue;
 
     const int lx = tx + 2, ly = ty + 1;
-    float wc[5];
-#pragma unroll
-    for (int e = 0; e < 5; ++e) wc[e] = s.prm[k & 1].v[e][ly][lx];
+    float wc[5];  // the cell's velocity and density for the gravity source, as mixed_cell forms them
+    if (p.gravity) {
+      const float* A1 = cu(k);
+      const int o = ly * G::PX + lx;
+      wc[0] = A1[o];
+      const float inv = 1.0f / wc[0];
+      wc[1] = A1[G::PB + o] * inv;
+      wc[2] = A1[2 * G::PB + o] * inv;
+      wc[3] = A1[3 * G::PB + o] * inv;
+      wc[4] = 0.0f;
+    }
     float dU[5];
     flux_divergence<1>(p, s, k, tx, ty, dtf, dtdx, dtdy, dtdz, wc, ph, dU);
     // step's viscosity, eta * (sum of the 6 neighbours - 6 U), of the U this
