@@ -558,8 +558,20 @@ int tlq_set_cooling_table(tlq_ctx* ctx, const double* T, const double* logL, int
   CK(cudaMemcpy(ctx->dgcum, gc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->dslopef, slf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->dgcumf, gcf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  // nodes uniform in log10 T (each within a third of a step of the line
+  // through the first and last): the FP32 searches guess the segment
+  float lt0 = 0.0f, dl_inv = 0.0f;
+  if (n >= 3) {
+    const double l0 = std::log10((double)fT[0]), dl = (std::log10((double)fT[n - 1]) - l0) / (double)(n - 1);
+    bool uniform = dl > 0.0;
+    for (int q = 0; q < n && uniform; ++q) uniform = std::fabs(std::log10((double)fT[q]) - (l0 + dl * q)) <= dl / 3.0;
+    if (uniform) {
+      lt0 = (float)l0;
+      dl_inv = (float)(1.0 / dl);
+    }
+  }
   ctx->P.cool = CoolTable{ctx->dT,     ctx->dlogT, ctx->dC,      n,          ctx->dTf, ctx->dlogTf,
-                          ctx->dCf,    ctx->dslope, ctx->dgcum, ctx->dslopef, ctx->dgcumf};
+                          ctx->dCf,    ctx->dslope, ctx->dgcum, ctx->dslopef, ctx->dgcumf, lt0, dl_inv};
   ctx->cool_tmin = T[0];
   ctx->P.c_edge_rho = T[0] * KB;
   if (!ctx->cool_counts) {

@@ -64,6 +64,10 @@ struct CoolTable {
   const double* gcum;
   const float* slopef;
   const float* gcumf;
+  // a table whose nodes are uniform in log10 T (within a third of a step):
+  // log10 T_0 and 1/step, from which the FP32 searches guess a cell's
+  // segment; dl_inv = 0 for any other table
+  float lt0, dl_inv;
 };
 
 // Static description of the mesh and the physics switches, passed by value.

@@ -141,9 +141,20 @@ __device__ __forceinline__ void mixed_cell(float gm1, const double* u, long long
 // cell's temperature moves little between sub-steps, and when the guess is
 // still the first entry above temp (the entry below it is not) the search is
 // skipped and the result is the same.
-__device__ __forceinline__ float cool_coef_seg(const CoolTable& t, float temp, int& lo) {
-  const bool same = lo >= 1 && lo <= t.n && !(t.Tf[lo - 1] > temp) && (lo == t.n || t.Tf[lo] > temp);
-  if (!same) {
+// The first table node above temp (1..n-1; n above the table), as find_coef
+// picks it: on a table uniform in log10 T (t.dl_inv > 0) from a guess at the
+// segment from lt = log10 T, moved to the node that satisfies the search's
+// condition (the guess decides only how many loads that takes: one or two
+// instead of a binary search's chain of eight dependent ones); otherwise a
+// binary search.
+__device__ __forceinline__ int first_above_f(const CoolTable& t, float temp, float lt) {
+  int lo;
+  if (t.dl_inv > 0.0f) {
+    const float x = fminf(fmaxf(__fmul_rn(__fsub_rn(lt, t.lt0), t.dl_inv), 0.0f), (float)(t.n - 1));
+    lo = 1 + (int)x;
+    while (lo > 1 && t.Tf[lo - 1] > temp) --lo;
+    while (lo < t.n && !(t.Tf[lo] > temp)) ++lo;
+  } else {
     lo = 1;
     int hi = t.n;
     while (lo < hi) {
@@ -151,10 +162,17 @@ __device__ __forceinline__ float cool_coef_seg(const CoolTable& t, float temp, i
       if (t.Tf[mid] > temp) hi = mid; else lo = mid + 1;
     }
   }
+  return lo;
+}
+
+__device__ __forceinline__ float cool_coef_seg(const CoolTable& t, float temp, int& lo) {
+  const float lt = log10f(temp);
+  const bool same = lo >= 1 && lo <= t.n && !(t.Tf[lo - 1] > temp) && (lo == t.n || t.Tf[lo] > temp);
+  if (!same) lo = first_above_f(t, temp, lt);
   if (lo >= t.n) return exp10f(t.Cf[t.n - 1]);
   const float T0 = t.logTf[lo - 1], C0 = t.Cf[lo - 1];
   const float T1 = t.logTf[lo], C1 = t.Cf[lo];
-  return exp10f(__fmaf_rn((C1 - C0) / (T1 - T0), __fsub_rn(log10f(temp), T0), C0));
+  return exp10f(__fmaf_rn((C1 - C0) / (T1 - T0), __fsub_rn(lt, T0), C0));
 }
 
 __device__ __forceinline__ float cool_coef_f(const CoolTable& t, float temp) {
@@ -195,11 +213,8 @@ __device__ __forceinline__ bool cools_at(const Params& p, float temp, const doub
 // meet products use explicit-rounding intrinsics (one contraction choice in
 // every kernel that inlines this).
 __device__ __forceinline__ float cool_exact_dropf(const CoolTable& t, float temp, float lam, float tau) {
-  int lo = 1, hi = t.n;  // first node above temp (n: none), as find_coef
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (t.Tf[mid] > temp) hi = mid; else lo = mid + 1;
-  }
+  int lo = first_above_f(t, temp, log10f(temp));  // first node above temp (n: none), as find_coef
+  int hi;
   const int i = lo - 1;
   const float a = __fsub_rn(1.0f, t.slopef[i]);
   const float lxlo = logf(t.Tf[i] / temp);  // <= 0
