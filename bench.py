@@ -17,7 +17,12 @@ zone-updates/s = interior cells x steps / time.
              relative L1 density error and total-energy drift against FP64
              after W+K steps (the surrogate against FP64 with the exact
              integrator it falls back to); `surrogate` its training and
-             fallback rate (the network is trained on the GPU first);
+             fallback rate (the network is trained on the GPU first), and
+             `surrogate.active` the same forms on the clumpy medium, where
+             the network cools a quarter of a million cells a step;
+* ensemble   (wind256) the 48-member ensemble in the batched persistent
+             form for --ens-steps steps, against its members one after
+             another (same form; plain FP64 with the exact integrator);
 * e2e        the same metric end to end through the C ABI with host
              buffers: per step tlq_upload (pinned host -> device + layout
              conversion + calc_prims/dt), tlq_step, tlq_download;
@@ -280,23 +285,18 @@ def ensemble_members(n: int = 48, seed: int = 2024):
     return out
 
 
-def run_ensemble(args, world, rank, dist):
-    """48 independent wind bubbles advanced by the batched persistent step
+def ensemble_record(steps, warmup, net, world, dist):
+    """The ensemble's 48 wind bubbles advanced by the batched persistent step
     (one launch per stage over all members' tiles, graph-replayed step,
-    z-chunks from the autotuner), against the same members stepped one
-    context after another."""
+    z-chunks from the autotuner) for `steps` timed steps after `warmup`,
+    against the same members stepped one context after another, in the same
+    form and in plain FP64 with the exact cooling integrator.  net: the
+    cooling surrogate's weights (the members share the table and physics)."""
     import tempfile
 
-    import torch
-    from tlaloque_gb300 import build as tbuild
     from tlaloque_gb300 import tlq
-    tbuild.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     members = ensemble_members()
     cells = sum(c.cells for c, _ in members)
-    with tlq.Context(members[0][0]) as tctx:  # one network: the members share the cooling table and physics
-        rep = tctx.train_cooling_surrogate(nsamples=args.train_samples, epochs=args.train_epochs)
-        net = tctx.get_cooling_surrogate()
     b = tlq.Batch([c for c, _ in members])
     for m, (cfg, U0) in zip(b.members, members):
         m.set_cooling_surrogate(*net)
@@ -307,68 +307,79 @@ def run_ensemble(args, world, rank, dist):
     t0 = time.perf_counter()
     chosen = b.autotune(cache, steps=3)
     tune_s = time.perf_counter() - t0
-    b.run(args.warmup)
+    b.run(warmup)
     b.synchronize()
     barrier(dist)
     b.enable_timing(True)
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))).start()
     sampler.begin()
-    b.run(args.steps)
+    b.run(steps)
     b.synchronize()
     sampler.end()
     clocks = sampler.stop()
     st = b.stats()
-    ms = allmax(dist, st.ms_per_step * args.steps)
+    ms = allmax(dist, st.ms_per_step * steps)
     status = b.status()
     b.close()
-    # the same members one context after another (per-member graphs)
-    seq_ms = 0.0
-    for cfg, U0 in members:
-        with tlq.Context(cfg) as ctx:
-            ctx.set_cooling_surrogate(*net)
-            U1 = U0.copy(order="F")
-            ctx.borders(U1, 1)
-            ctx.upload(U1)
-            ctx.advance(args.warmup)
-            ctx.enable_timing(True)
-            ctx.advance(args.steps)
-            s = ctx.stats()
-            seq_ms += (s.ms_stage1 + s.ms_stage2 + s.ms_cool) * args.steps
-    # and in the plain FP64 form with the exact integrator (what the reference
-    # computes), one context after another
-    seq64_ms = 0.0
-    for cfg, U0 in members:
-        cfg64 = tlq.Config(**{**cfg.__dict__, "precision": tlq.PREC_FP64, "cooling": tlq.COOL_EXACT})
-        with tlq.Context(cfg64) as ctx:
-            U1 = U0.copy(order="F")
-            ctx.borders(U1, 1)
-            ctx.upload(U1)
-            ctx.advance(args.warmup)
-            ctx.enable_timing(True)
-            ctx.advance(args.steps)
-            s = ctx.stats()
-            seq64_ms += (s.ms_stage1 + s.ms_stage2 + s.ms_cool) * args.steps
-    value = world * cells * args.steps / (ms / 1e3)
-    line = {"metric": "zone-updates/s of a 48-member wind-bubble ensemble on 1 GB300 (batched persistent step)",
-            "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": "ensemble of 48 wind bubbles, sizes uniform from {48,64,96,128}^3, v_w "
-                                   "log-uniform 500-3000 km/s, n log-uniform 0.1-10 cm^-3, mixed precision + "
-                                   "learned cooling surrogate",
-                       "surrogate_training_ms": rep["ms_generate"] + rep["ms_train"],
-                       "cells": cells, "members": len(members), "items": st.items, "persistent_blocks": st.blocks,
-                       "zlen_chosen": sorted(set(chosen)), "autotune_s": tune_s,
-                       "l2": "the members' state (~6 GB) exceeds L2"},
+
+    def one_after_another(over, with_net):
+        tot = 0.0
+        for cfg, U0 in members:
+            with tlq.Context(tlq.Config(**{**cfg.__dict__, **over})) as ctx:
+                if with_net:
+                    ctx.set_cooling_surrogate(*net)
+                U1 = U0.copy(order="F")
+                ctx.borders(U1, 1)
+                ctx.upload(U1)
+                ctx.advance(warmup)
+                ctx.enable_timing(True)
+                ctx.advance(steps)
+                s = ctx.stats()
+                tot += (s.ms_stage1 + s.ms_stage2 + s.ms_cool) * steps
+        return tot
+    seq_ms = one_after_another({}, True)  # per-member graphs, the same form
+    # what the reference computes: plain FP64 with the exact integrator
+    seq64_ms = one_after_another({"precision": tlq.PREC_FP64, "cooling": tlq.COOL_EXACT}, False)
+    return {"value": world * cells * steps / (ms / 1e3), "unit": UNIT, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "cells": cells, "members": len(members), "items": st.items,
+            "persistent_blocks": st.blocks, "zlen_chosen": sorted(set(chosen)), "autotune_s": tune_s,
             "members_failed": int(sum(1 for x in status if x != 0)),
-            "sequential": {"value": cells * args.steps / (seq_ms / 1e3), "ms_per_step": seq_ms / args.steps,
+            "sequential": {"value": cells * steps / (seq_ms / 1e3), "ms_per_step": seq_ms / steps,
                            "path": "each member alone, its own graph-replayed step, one after another"},
-            "speedup_vs_sequential": (seq_ms / args.steps) / (ms / args.steps),
-            "sequential_fp64": {"value": cells * args.steps / (seq64_ms / 1e3), "ms_per_step": seq64_ms / args.steps,
-                                "path": "each member alone in the plain FP64 form with the exact cooling integrator "
-                                        "(closed form), one after another"},
-            "speedup_vs_sequential_fp64": (seq64_ms / args.steps) / (ms / args.steps),
-            "gpu_launches": st.launches_per_step * args.steps, "clocks": clocks}
+            "speedup_vs_sequential": seq_ms / ms,
+            "sequential_fp64": {"value": cells * steps / (seq64_ms / 1e3), "ms_per_step": seq64_ms / steps,
+                                "path": "each member alone in the plain FP64 form with the exact cooling "
+                                        "integrator (closed form), one after another"},
+            "speedup_vs_sequential_fp64": seq64_ms / ms,
+            "gpu_launches": st.launches_per_step * steps, "clocks": clocks}
+
+
+ENSEMBLE_WORKLOAD = ("ensemble of 48 wind bubbles, sizes uniform from {48,64,96,128}^3, v_w log-uniform "
+                     "500-3000 km/s, n log-uniform 0.1-10 cm^-3, mixed precision + learned cooling surrogate")
+
+
+def run_ensemble(args, world, rank, dist):
+    """The ensemble workload as the bench's own line (--workload ensemble48)."""
+    import torch
+    from tlaloque_gb300 import build as tbuild
+    from tlaloque_gb300 import tlq
+    tbuild.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    members = ensemble_members()
+    with tlq.Context(members[0][0]) as tctx:  # one network: the members share the cooling table and physics
+        rep = tctx.train_cooling_surrogate(nsamples=args.train_samples, epochs=args.train_epochs)
+        net = tctx.get_cooling_surrogate()
+    r = ensemble_record(args.steps, args.warmup, net, world, dist)
+    line = {"metric": "zone-updates/s of a 48-member wind-bubble ensemble on 1 GB300 (batched persistent step)",
+            "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": ENSEMBLE_WORKLOAD, "surrogate_training_ms": rep["ms_generate"] + rep["ms_train"],
+                       "cells": r["cells"], "members": r["members"], "items": r["items"],
+                       "persistent_blocks": r["persistent_blocks"], "zlen_chosen": r["zlen_chosen"],
+                       "autotune_s": r["autotune_s"], "l2": "the members' state (~6 GB) exceeds L2"},
+            **{k: r[k] for k in ("members_failed", "sequential", "speedup_vs_sequential", "sequential_fp64",
+                                 "speedup_vs_sequential_fp64", "gpu_launches", "clocks")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -416,6 +427,8 @@ def main():
     ap.add_argument("--clumpy-n", type=int, default=256, help="mesh of the surrogate-active record")
     ap.add_argument("--sur-steps", type=int, default=100, help="timed steps of the surrogate-active record")
     ap.add_argument("--no-surrogate-active", action="store_true")
+    ap.add_argument("--ens-steps", type=int, default=10, help="timed steps of the ensemble record")
+    ap.add_argument("--no-ensemble", action="store_true", help="leave out the ensemble record")
     ap.add_argument("--sur-tol", type=float, default=1e-3, help="residual tolerance of the surrogate-active record")
     ap.add_argument("--mlp-tol", type=float, default=1e-3, help="residual tolerance of the workload's surrogate form")
     args = ap.parse_args()
@@ -441,6 +454,7 @@ def main():
     peak, peak_kind = load_peaks()
     stream = torch.cuda.Stream()
     forms = {}
+    ensemble = None
     import tempfile
     tune_cache = os.path.join(tempfile.gettempdir(), "tlq_autotune.json")
 
@@ -604,6 +618,10 @@ def main():
         head = sur
         if not args.no_surrogate_active:
             surrogate["active"] = surrogate_active(net, sub)
+        if not args.no_ensemble and args.workload == "wind256":
+            # the batched form on the ensemble workload (its own line: --workload ensemble48)
+            ensemble = {"workload": ENSEMBLE_WORKLOAD, **ensemble_record(args.ens_steps, args.warmup, net, world,
+                                                                          dist)}
     value = head["value"]
     ms_max = head["ms"]
     mix = head
@@ -670,6 +688,8 @@ def main():
         "gpu_launches": (5 if surrogate else 2) * args.steps,
         "hbm_gbs_step": bpz_m["step"] * cfg.cells * args.steps / (ms_max / 1e3) / 1e9,
     }
+    if ensemble is not None:
+        line["ensemble"] = ensemble
     if rank == 0 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1
         rate, steps, secs = cpu_oracle_rate(cfg, U0, args.cpu_budget, ncores)
