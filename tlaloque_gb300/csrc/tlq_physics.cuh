@@ -333,6 +333,34 @@ __device__ __forceinline__ bool near_boundary_or_wind(const Params& p, int i, in
   return false;
 }
 
+// near_boundary_or_wind ruled out for whole planes of a tile (columns
+// i0..i1 x j0..j1): `ij` when some column lies within two cells of an x or y
+// face, and the z range [klo, khi] of the spherical winds whose index boxes
+// meet the tile's columns.  Formed once per tile (the winds' boxes are read
+// from memory there, not per cell); plane k of the tile may hold a cell for
+// which near_boundary_or_wind is true only if may_be_special(k).
+struct TileSpecial {
+  bool ij;
+  int klo, khi;
+  __device__ __forceinline__ bool may_be_special(const Params& p, int k) const {
+    return ij || k <= 2 || k >= p.nz - 1 || (p.nplanes > 0 && k >= p.nz) || (k >= klo && k <= khi);
+  }
+};
+__device__ __forceinline__ TileSpecial tile_special(const Params& p, int i0, int i1, int j0, int j1) {
+  TileSpecial t;
+  t.ij = i0 <= 2 || j0 <= 2 || i1 >= p.nx - 1 || j1 >= p.ny - 1;
+  t.klo = 1 << 30;
+  t.khi = -(1 << 30);
+  for (int s = 0; s < p.nwinds; ++s) {
+    const Wind& w = p.winds[s];
+    if (i1 >= w.ilo && i0 <= w.ihi && j1 >= w.jlo && j0 <= w.jhi) {
+      t.klo = min(t.klo, w.klo);
+      t.khi = max(t.khi, w.khi);
+    }
+  }
+  return t;
+}
+
 // user_boundaries: the spherical winds, then the plane winds.
 __device__ __forceinline__ void winds_cell(const Params& p, int i, int j, int k, double* u) {
   for (int s = 0; s < p.nwinds; ++s) wind_cell(p, p.winds[s], i, j, k, u);

@@ -83,6 +83,7 @@ struct MixedSmem2 {
   float fz[2][5][MTY][MTX];
   uint64_t bar[4];
   double red[96];
+  TileSpecial tspec;  // the tile's boundary/wind pre-test (block-uniform)
   int flag;
   int abort;
 };
@@ -654,6 +655,7 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
   const int i = i0 + tx, j = j0 + ty;
   const bool cell_ok = (ty < MTY) && (i <= p.nx) && (j <= p.ny);
   const float etaf = p.f_eta;
+  const TileSpecial ts = tile_special(p, i0, min(i0 + MTX - 1, p.nx), j0, min(j0 + MTY - 1, p.ny));
   // k = k0 - 1 computes only the z face below the chunk, through the same
   // (single) copy of the face code as every other plane, so that a cell's
   // arithmetic does not depend on where the z-chunks begin
@@ -719,7 +721,8 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
     // the boundaries or the winds also need (ghost images, wind overwrite),
     // which take UPP = U - dU in FP64 from the state in HBM.
     float w[5];
-    bool fp64 = near_boundary_or_wind(p, i, j, k);
+    const bool nb = ts.may_be_special(p, k) && near_boundary_or_wind(p, i, j, k);
+    bool fp64 = nb;
     if (!fp64) {
       const float* A1 = cu(k);
       const int o = ly * G::PX + lx;
@@ -739,7 +742,7 @@ __device__ __forceinline__ void mixed_tile1(const CUtensorMap* tm, const StageAr
       double up[5];
 #pragma unroll
       for (int e = 0; e < 5; ++e) up[e] = a.uold[e * L.plane + c] - f2d(dU[e]);
-      if (near_boundary_or_wind(p, i, j, k)) {
+      if (nb) {
         write_ghost_prims(p, L, a.uppf, gm1, i, j, k, up);  // borders(UPP, 2)
         winds_cell(p, i, j, k, up);
       }
@@ -782,6 +785,7 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
   if (tid == 0) {
     for (int q = 0; q < 4; ++q) mbar_init(&s.bar[q], 1);
     s.abort = 0;
+    s.tspec = tile_special(p, i0, min(i0 + MTX - 1, p.nx), j0, min(j0 + MTY - 1, p.ny));
     fence_mbar_init();
   }
   __syncthreads();
@@ -863,7 +867,7 @@ __device__ __forceinline__ void mixed_tile2(const CUtensorMap* tm, const StageAr
       // U = U_old - dU + eta Lap in one FP64 addition of the FP32 increment
       // (an FP64 addition costs ~64 FP32 slots on GB300; the gate also keeps
       // the winds' FP64 distance and density off the FP64 pipe)
-      const bool special = near_boundary_or_wind(p, i, j, k);
+      const bool special = s.tspec.may_be_special(p, k) && near_boundary_or_wind(p, i, j, k);
       double un[5];
       if (!special) {
 #pragma unroll
