@@ -189,6 +189,31 @@ def test_all_fallback_is_the_exact_step(trained):
     assert got["t"] == ref["t"]
 
 
+def test_medium_at_the_floor_skips_the_network(trained):
+    """A dense medium just above the cooling table's first temperature (the
+    wind bubble's ambient at n = 10 cm^-3, without the wind and the point
+    mass): its cooling number is far above the single-step limit, and the
+    exact integrator takes every cell to the table's first temperature in
+    the first step.  Stage 2 applies that floor itself (no cell reaches the
+    network, the cells count as the exact integrator's) with the exact
+    integrator's bits: the step is bit for bit the mixed step with the exact
+    integrator."""
+    _, net = trained
+    cfg, U0 = problems.wind_bubble(24, n_amb=10.0)
+    cfg.winds = []
+    cfg.masses = None
+    ref = run(mixed_cfg(cfg, tlq.COOL_EXACT, **SUB), U0, 4)
+    got = run(mixed_cfg(cfg, tlq.COOL_MLP, **SUB), U0, 4, net=net)
+    assert got["rc"] == tlq.OK and got["it"] == ref["it"] == 4
+    assert got["mlp"] == 0 and got["fb"] >= 24 ** 3  # every cell in the first step
+    np.testing.assert_array_equal(interior(got["U"]), interior(ref["U"]))
+    assert got["t"] == ref["t"]
+    # at the floor: the cells' temperature is the table's first (to FP32 rounding)
+    rho, p = interior(got["W"])[0], interior(got["W"])[4]
+    T = p * cfg.mu0 * problems.AMU / (rho * problems.KB)
+    assert np.all(np.abs(T / cfg.cool_T[0] - 1.0) < 1e-5)
+
+
 # The judge: the plain FP64 step with the exact integrator (its single
 # exponential step up to a cooling number of 2e-3, the closed form above).
 SUB = dict(cool_sub_frac=2e-3)
