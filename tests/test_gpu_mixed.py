@@ -86,3 +86,31 @@ def test_mixed_sedov_shock_radius(gpu_lib, golden):
     ok = np.isfinite(prof)
     assert abs(rc_[ok][np.argmax(prof[ok])] - Rs) < 2.5 * cfg.dx
     assert rel_l1(interior(W)[0], interior(W64)[0]) < 1e-2
+
+
+@pytest.mark.parametrize("table", ["z1", "z1_uneven"])
+def test_mixed_cooling_on_reference_tables(gpu_lib, golden, table):
+    """The FP32 cooling of the mixed step on the reference's Z1.0.dat table
+    (nodes uniform in log T: a cell's segment is guessed from log10 T) and on
+    the same table with every other node of its lower half dropped (uneven:
+    the binary search), against the FP64 step, both with the exact
+    integrator: a 24^3 clumpy medium (log T uniform over 1e3-1e8 K) for 5
+    steps, in which most cells cool and many cross segments within a step."""
+    T, logL = golden["z1_T"], -golden["z1_b"]
+    if table == "z1_uneven":
+        half = len(T) // 2
+        keep = [q for q in range(len(T)) if q >= half or q % 2 == 0]
+        T, logL = T[keep], logL[keep]
+    cfg, U0 = problems.clumpy(24, seed=2)
+    cfg = tlq.Config(**{**cfg.__dict__, "cool_T": T, "cool_logL": logL, "cooling": tlq.COOL_EXACT,
+                        "cool_sub_frac": 2e-3})
+    U64, W64, (t64, it64, _, rc64), s64 = run_gpu(cfg, U0, 5, precision=tlq.PREC_FP64)
+    Um, Wm, (tm, itm, _, rcm), sm = run_gpu(cfg, U0, 5, precision=tlq.PREC_MIXED)
+    assert rc64 == tlq.OK and rcm == tlq.OK and it64 == itm == 5
+    U0i = interior(U0)
+    p0 = (cfg.gamma - 1.0) * (U0i[4] - 0.5 * (U0i[1] ** 2 + U0i[2] ** 2 + U0i[3] ** 2) / U0i[0])
+    changed = np.mean(np.abs(interior(W64)[4] / p0 - 1.0) > 1e-3)
+    assert changed > 0.3  # the cooling acts on a large part of the medium
+    assert rel_l1(interior(Wm)[0], interior(W64)[0]) <= 1e-6
+    assert rel_l1(interior(Wm)[4], interior(W64)[4]) <= 1e-5
+    assert abs(sm[4] - s64[4]) / abs(s64[4]) <= 1e-8
