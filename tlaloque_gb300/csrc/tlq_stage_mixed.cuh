@@ -363,41 +363,56 @@ __device__ __forceinline__ void prim_cons(const float* w, float igm1, float* u) 
   u[4] = __fmaf_rn(w[4], igm1, __fmul_rn(__fmul_rn(0.5f, w[0]), k2));
 }
 
-// One face flux, direction d (1 x, 2 y, 3 z), from the primitives of the
-// four cells along d (w0..w3; stage 1 reads only w1, w2), each `VS` floats
-// between variables, and the conserved values of the two cells beside the
-// face: stage 1 reads them (uL, uR: the FP32 image of U), stage 2 forms them
-// from w1, w2 (igm1 = 1/(gamma-1)).  Every face of both stages and of the
-// batched kernels goes through this one copy of the code.
-template <int STAGE, int LIM, int SOLV, int VS>
-__device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, float igm1, int d,
-                                          const float* w0, const float* w1, const float* w2, const float* w3,
-                                          const float* uL, const float* uR, float* ff) {
-  float wll[5], wl[5], wr[5], wrr[5], UL[5], UR[5];
+// One first-order face flux of stage 1, direction d (1 x, 2 y, 3 z; a
+// compile-time constant at every call), from the primitives of the two cells
+// beside the face (wl, wr) and their conserved values (uL, uR: the FP32
+// image of U), each `VS` floats between variables.
+template <int LIM, int SOLV, int VS>
+__device__ __forceinline__ void face_flux1(const Params& p, float gf, float g1f, int d, const float* w1,
+                                           const float* w2, const float* uL, const float* uR, float* ff) {
+  float wl[5], wr[5], UL[5], UR[5];
 #pragma unroll
   for (int e = 0; e < 5; ++e) {
     wl[e] = w1[e * VS];
     wr[e] = w2[e * VS];
-  }
-  if (STAGE == 1) {
-#pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      UL[e] = uL[e * VS];
-      UR[e] = uR[e * VS];
-    }
-  } else {
-    prim_cons(wl, igm1, UL);
-    prim_cons(wr, igm1, UR);
-  }
-  if (STAGE == 2) {
-#pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      wll[e] = w0[e * VS];
-      wrr[e] = w3[e * VS];
-    }
-    limiter(wll, wl, wr, wrr, LIM >= 0 ? LIM : p.limiter);
+    UL[e] = uL[e * VS];
+    UR[e] = uR[e * VS];
   }
   if (!riemann(SOLV >= 0 ? SOLV : p.solver, gf, g1f, ff, wl, wr, UL, UR, d)) {
+#pragma unroll
+    for (int e = 0; e < 5; ++e) ff[e] = NAN;
+  }
+}
+
+// A stage-2 face in its own frame: the velocity components of the four
+// cells are loaded normal first, then the two tangential ones in the
+// reference's order (on, o1, o2: their offsets from a cell's density, VS
+// floats per variable), so that the limiter and the Riemann solver run with
+// the face's direction fixed at x -- no selects on a runtime direction --
+// and ff comes back in the same frame (ff[1] the normal momentum flux).  The
+// tangential momentum fluxes are (rho u_n) u_t here, where the reference
+// forms (rho u_lo) u_hi by component index: the same value to FP32
+// rounding.
+template <int LIM, int SOLV, int VS>
+__device__ __forceinline__ void face_flux_frame(const Params& p, float gf, float g1f, float igm1, int on, int o1,
+                                                int o2, const float* w0, const float* w1, const float* w2,
+                                                const float* w3, float* ff) {
+  float wll[5], wl[5], wr[5], wrr[5], UL[5], UR[5];
+  auto load = [&](const float* w, float* v) {
+    v[0] = w[0];
+    v[1] = w[on];
+    v[2] = w[o1];
+    v[3] = w[o2];
+    v[4] = w[4 * VS];
+  };
+  load(w1, wl);
+  load(w2, wr);
+  prim_cons(wl, igm1, UL);
+  prim_cons(wr, igm1, UR);
+  load(w0, wll);
+  load(w3, wrr);
+  limiter(wll, wl, wr, wrr, LIM >= 0 ? LIM : p.limiter);
+  if (!riemann(SOLV >= 0 ? SOLV : p.solver, gf, g1f, ff, wl, wr, UL, UR, 1)) {
 #pragma unroll
     for (int e = 0; e < 5; ++e) ff[e] = NAN;
   }
@@ -413,8 +428,8 @@ __device__ __forceinline__ void face_flux(const Params& p, float gf, float g1f, 
 // each thread the left x face, the lower y face and the upper z face of one
 // cell, and the tile's right x edge (warp 0) and upper y edge (warp 1) as
 // second faces of their rounds.  Stage 2's faces (limiter and HLLC) are one
-// flat task list through one copy of the code (the rounds' three copies
-// measured slower there).
+// flat task list through one copy of the code, each face in its own frame
+// (face_flux_frame; the rounds' three copies measured slower there).
 template <int STAGE, int LIM, int SOLV, class Smem, class PrmOf, class CuOf>
 __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, int j0, int k, bool xy, float gf,
                                             float g1f, float igm1, PrmOf prm, CuOf cu) {
@@ -432,8 +447,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
         const int o = (fyl + OY) * PX + fxl + 1;  // cell i0 - 1 + fxl
         if ((i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny)) {
           float ff[5];
-          face_flux<1, LIM, SOLV, VS>(p, gf, g1f, igm1, 1, nullptr, pk + o, pk + o + 1, nullptr, ck + o, ck + o + 1,
-                                      ff);
+          face_flux1<LIM, SOLV, VS>(p, gf, g1f, 1, pk + o, pk + o + 1, ck + o, ck + o + 1, ff);
 #pragma unroll
           for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
         }
@@ -443,8 +457,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
         const int o = (fyl - 1 + OY) * PX + fxl + 2;  // cell j0 - 1 + fyl
         if ((i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny)) {
           float ff[5];
-          face_flux<1, LIM, SOLV, VS>(p, gf, g1f, igm1, 2, nullptr, pk + o, pk + o + PX, nullptr, ck + o,
-                                      ck + o + PX, ff);
+          face_flux1<LIM, SOLV, VS>(p, gf, g1f, 2, pk + o, pk + o + PX, ck + o, ck + o + PX, ff);
 #pragma unroll
           for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
         }
@@ -455,8 +468,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       const int o = (fyl + OY) * PX + fxl + 2;
       if (tid < NZF && (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny)) {
         float ff[5];
-        face_flux<1, LIM, SOLV, VS>(p, gf, g1f, igm1, 3, nullptr, pk + o, prm(k + 1) + o, nullptr, ck + o,
-                                    cu(k + 1) + o, ff);
+        face_flux1<LIM, SOLV, VS>(p, gf, g1f, 3, pk + o, prm(k + 1) + o, ck + o, cu(k + 1) + o, ff);
 #pragma unroll
         for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
       }
@@ -466,7 +478,7 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
   const int tbeg = xy ? 0 : NXF + NYF;
   for (int t = tbeg + (int)threadIdx.x; t < NXF + NYF + NZF; t += MNT) {
     int d, fxl, fyl;
-    const float *w0, *w1, *w2, *w3, *uL, *uR;
+    const float *w0, *w1, *w2, *w3;
     bool valid;
     if (t < NXF) {
       d = 1;
@@ -476,7 +488,6 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w0 = w1 - 1;
       w2 = w1 + 1;
       w3 = w1 + 2;
-      uL = uR = nullptr;
       valid = (i0 - 1 + fxl <= p.nx) && (j0 + fyl <= p.ny);
     } else if (t < NXF + NYF) {
       d = 2;
@@ -487,7 +498,6 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w0 = w1 - PX;
       w2 = w1 + PX;
       w3 = w1 + 2 * PX;
-      uL = uR = nullptr;
       valid = (i0 + fxl <= p.nx) && (j0 - 1 + fyl <= p.ny);
     } else {
       d = 3;
@@ -499,21 +509,30 @@ __device__ __forceinline__ void mixed_faces(const Params& p, Smem& s, int i0, in
       w1 = pk + o;
       w2 = prm(k + 1) + o;
       w3 = prm(k + 2) + o;
-      uL = uR = nullptr;
       valid = (i0 + fxl <= p.nx) && (j0 + fyl <= p.ny);
     }
     if (!valid) continue;
+    // the face's frame: normal component d, then the other two in order
+    const int on = d * VS, o1 = (d == 1 ? 2 : 1) * VS, o2 = (d == 3 ? 2 : 3) * VS;
     float ff[5];
-    face_flux<STAGE, LIM, SOLV, VS>(p, gf, g1f, igm1, d, w0, w1, w2, w3, uL, uR, ff);
+    face_flux_frame<LIM, SOLV, VS>(p, gf, g1f, igm1, on, o1, o2, w0, w1, w2, w3, ff);
     if (d == 1) {
 #pragma unroll
       for (int e = 0; e < 5; ++e) s.fx[e][fyl][fxl] = ff[e];
-    } else if (d == 2) {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) s.fy[e][fyl][fxl] = ff[e];
-    } else {
-#pragma unroll
-      for (int e = 0; e < 5; ++e) s.fz[(k + 1) & 1][e][fyl][fxl] = ff[e];
+    } else if (d == 2) {  // frame (y, x, z)
+      s.fy[0][fyl][fxl] = ff[0];
+      s.fy[1][fyl][fxl] = ff[2];
+      s.fy[2][fyl][fxl] = ff[1];
+      s.fy[3][fyl][fxl] = ff[3];
+      s.fy[4][fyl][fxl] = ff[4];
+    } else {  // frame (z, x, y)
+      float* fz = &s.fz[(k + 1) & 1][0][fyl][fxl];
+      constexpr int ZS = MTY * MTX;
+      fz[0] = ff[0];
+      fz[ZS] = ff[2];
+      fz[2 * ZS] = ff[3];
+      fz[3 * ZS] = ff[1];
+      fz[4 * ZS] = ff[4];
     }
   }
 }
